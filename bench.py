@@ -1,0 +1,360 @@
+"""Throughput benchmark: PEPS samples/s for amplitude + O_k + E_loc.
+
+A "step" is one Monte-Carlo sweep of every chain -- the reference's
+transition (all sites Metropolis with environment reuse) followed by
+estimate (O_k, E_loc, next bottom cache), kernels.py:131-245 -- i.e. one row
+of LocalEstimates per chain.  Default workload: 8x8 open-boundary Heisenberg,
+D=4, chi=16, ZipUp(16), 4096 chains, seeded synthetic tensors
+N(0,1)/sqrt(2 D^4).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU (torchrun): every rank runs its own 4096 chains (replicas; the
+chains are independent), value = all ranks' samples / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "PEPS samples/s (amp+grad log psi+E_loc), D=4 chi=16"
+UNIT = "samples/s"
+
+
+def _oracle_chunk(args):
+    """Time the FP64 NumPy restatement on one chunk of chains (runs in a worker process)."""
+    import numpy as np
+
+    from oracle import peps as oracle
+    from vmc_gb300.synthetic import WORKLOADS, initial_configs, random_tensors, uniform_stream
+
+    wname, n, seed = args
+    w = WORKLOADS[wname]
+    T = random_tensors(w.shape, w.bond_dim, w.phys_dim, seed=0)
+    n_sites = w.shape[0] * w.shape[1]
+    cfg = initial_configs(n, n_sites, w.phys_dim, seed=seed).astype(np.int64)
+    u = next(uniform_stream(n, n_sites, seed=seed))
+    strat = oracle.ZipUp(w.chi) if w.strategy == "ZipUp" else oracle.NoTruncation()
+    model = oracle.PEPS(T, w.shape, w.bond_dim, w.phys_dim, strategy=strat)
+    init, trans, est = oracle.build_mc_kernels(model, w.operator())
+    cache = init(T, cfg)
+    t0 = time.perf_counter()
+    c2, ctx = trans(T, cfg, u, cache)
+    est(T, c2, ctx)
+    return n, time.perf_counter() - t0
+
+
+def cpu_oracle_rate(wname, n_per_worker, workers, pool):
+    """Samples/s of the oracle over `workers` processes (each one sweep of its chunk)."""
+    t0 = time.perf_counter()
+    res = pool.map(_oracle_chunk, [(wname, n_per_worker, 100 + i) for i in range(workers)])
+    wall = time.perf_counter() - t0
+    n = sum(r[0] for r in res)
+    return n / wall, n, wall
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[4:8]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle restatement (the reference is JAX, absent on the box) on host cores."""
+    import multiprocessing as mp
+
+    from vmc_gb300.synthetic import WORKLOADS
+
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    cores = len(os.sched_getaffinity(0))
+    ctx = mp.get_context("spawn")
+    per = max(1, args.ref_chains_per_core)
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            cpu_oracle_rate(args.workload, per, cores, pool)
+        t0 = time.perf_counter()
+        n_total = 0
+        for _ in range(args.steps):
+            _, n, _ = cpu_oracle_rate(args.workload, per, cores, pool)
+            n_total += n
+        wall = time.perf_counter() - t0
+    value = n_total / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
+                   "strategy": f"{w.strategy}({w.chi})", "model": w.model,
+                   "chains_per_step": per * cores, "parallelism": "host processes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{per * cores} chains x 1 sweep per step, FP64 NumPy oracle restatement "
+                                   "(the reference's JAX CPU path cannot be installed: no jax/flax wheels)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def e2e_public_api(w, n, rank, dev, ustream, args, barrier):
+    """Same sweep through the user-facing API (PEPS + build_mc_kernels + make_mc_sampler),
+    with every step's uniforms copied from pinned host memory and E_loc, log|psi| and
+    sign read back to the host inside the timed region."""
+    import torch
+
+    from vmc_gb300.kernels import build_mc_kernels
+    from vmc_gb300.peps import PEPS, ZipUp
+    from vmc_gb300.sampling import make_mc_sampler
+    from vmc_gb300.synthetic import initial_configs, random_tensors
+
+    n_sites = w.shape[0] * w.shape[1]
+    model = PEPS(shape=w.shape, bond_dim=w.bond_dim, phys_dim=w.phys_dim, contraction_strategy=ZipUp(w.chi),
+                 device=dev, tensors=random_tensors(w.shape, w.bond_dim, w.phys_dim, seed=0))
+    init_cache, transition, estimate = build_mc_kernels(model, w.operator())
+    sampler = make_mc_sampler(transition, estimate)
+    cfg = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
+    cache = init_cache(model.tensors, cfg)
+    host_u = [torch.from_numpy(next(ustream)).pin_memory() for _ in range(args.warmup + args.steps)]
+    e_host = torch.empty(n, dtype=torch.float64).pin_memory()
+    la_host = torch.empty(n, dtype=torch.float64).pin_memory()
+    sg_host = torch.empty(n, dtype=torch.float64).pin_memory()
+
+    def step(i, cfg, cache):
+        u = host_u[i].to(dev, non_blocking=True)
+        (cfg, _, cache), (_, est) = sampler(model.tensors, cfg, u[None], cache, n_steps=1)
+        e_host.copy_(est.local_estimate[0], non_blocking=True)
+        la_host.copy_(est.log_amp[0], non_blocking=True)
+        sg_host.copy_(est.sign[0], non_blocking=True)
+        return cfg, cache
+
+    for i in range(args.warmup):
+        cfg, cache = step(i, cfg, cache)
+    barrier()
+    stream = torch.cuda.current_stream(dev)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for i in range(args.steps):
+        cfg, cache = step(args.warmup + i, cfg, cache)
+    t1.record(stream)
+    barrier()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    h2d = n * n_sites * 8
+    d2h = 3 * n * 8
+    return n * args.steps / elapsed, h2d, d2h
+
+
+def run_ours(args, rank, world, local_rank):
+    import multiprocessing as mp
+
+    import numpy as np
+
+    # the CPU baseline pool must exist before CUDA is initialised
+    pool = None
+    cores = len(os.sched_getaffinity(0))
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        pool = mp.get_context("spawn").Pool(cores)
+
+    import torch
+    import torch.distributed as dist
+
+    from vmc_gb300.engine import PEPSEngine
+    from vmc_gb300.lowering import pack_tensors
+    from vmc_gb300.synthetic import WORKLOADS, initial_configs, random_tensors, uniform_stream
+
+    w = WORKLOADS[args.workload]
+    n = args.chains or w.n_chains
+    dev = torch.device(f"cuda:{local_rank}")
+    torch.cuda.set_device(dev)
+    n_sites = w.shape[0] * w.shape[1]
+    eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev)
+    tens = torch.from_numpy(pack_tensors(random_tensors(w.shape, w.bond_dim, w.phys_dim, seed=0))).to(dev)
+    cfg0 = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
+    ustream = uniform_stream(n, n_sites, seed=1000 * rank)
+    total = args.warmup + args.steps
+    uni = torch.from_numpy(np.stack([next(ustream) for _ in range(total)])).to(dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---------------- device-resident throughput (value) ----------------
+    cfg = cfg0.clone()
+    cache = eng.init_cache(tens, cfg)
+    out = None
+    for i in range(args.warmup):
+        out = eng.sweep(tens, cfg, uni[i], cache, out=out)
+    barrier()
+    eng.raise_on_status()
+    stream = torch.cuda.current_stream(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(local_rank) as clocks:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            out = eng.sweep(tens, cfg, uni[args.warmup + i], cache, out=out)
+            ev[i][1].record(stream)
+        t_end.record(stream)
+        barrier()
+    eng.raise_on_status()
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    launch_ms = [a.elapsed_time(b) for a, b in ev]
+    t_all = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t_all, op=dist.ReduceOp.MAX)
+    elapsed = float(t_all.item())
+    value = world * n * args.steps / elapsed
+
+    # ---------------- end-to-end through the public API, host buffers ----------------
+    e2e_value, h2d, d2h = e2e_public_api(w, n, rank, dev, ustream, args, barrier)
+    if world > 1:
+        t = torch.tensor([n * args.steps / e2e_value], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_value = world * n * args.steps / float(t.item())
+
+    if rank != 0:
+        return
+    peaks, peak_kind = _peaks()
+    flops = w.flops_per_sample()
+    mean_launch_s = statistics.mean(launch_ms) / 1e3
+    achieved = n * flops / mean_launch_s / 1e12 if flops else None
+    peak = peaks.get("bf16_tflops")
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                "peak_kind": f"{peak_kind} bf16 burst (cuBLAS)", "kernel": "vmc::peps_kernel",
+                "flop_per_sample": flops, "units_per_launch": n}
+    cpu = None
+    if pool is not None:
+        per = max(1, args.cpu_chains_per_core)
+        rate, ns, wall = cpu_oracle_rate(w.name, per, cores, pool)
+        pool.close()
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{ns} chains x 1 sweep ({wall:.1f} s), FP64 NumPy oracle restatement over {cores} processes"}
+    clk = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
+                   "phys_dim": w.phys_dim, "strategy": f"{w.strategy}({w.chi})", "model": w.model,
+                   "chains_per_gpu": n, "global_chains": n * world, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (bottom-env cache "
+                         f"{eng.cache_bytes(n) / 1e9:.2f} GB read+written per step)"},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+        "kernel_ms_per_launch": statistics.mean(launch_ms),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="heis8x8_D4_chi16")
+    ap.add_argument("--chains", type=int, default=0)
+    ap.add_argument("--cpu-chains-per-core", type=int, default=12)
+    ap.add_argument("--ref-chains-per-core", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

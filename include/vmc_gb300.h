@@ -1,0 +1,180 @@
+/*
+ * vmc_gb300.h -- C ABI of the GB300 (sm_103a) PEPS evaluation engine.
+ *
+ * Plain C: pointers, sizes and integer status codes; no CUDA, torch or JAX
+ * types cross this boundary.  Device pointers are CUDA device addresses;
+ * `stream` is a cudaStream_t passed as void*.  Every compute entry point is
+ * stream-ordered and allocates nothing: the caller owns all buffers and
+ * passes a workspace sized by vmc_workspace_size().
+ *
+ * The entry points replace, for a batch of chains, the reference's PEPS
+ * kernels (fliingelephant/VMC, Python/JAX):
+ *   - vmc_peps_plan / vmc_peps_plan_set_operator: the static closure built by
+ *     build_mc_kernels (src/vmc/peps/standard/kernels.py:91-114) -- shape,
+ *     strategy, params_per_site and bucket_terms(operator.terms)
+ *     (src/vmc/operators/local_terms.py:165-200);
+ *   - vmc_peps_init_cache: init_cache (kernels.py:115-129);
+ *   - vmc_peps_sweep: one make_mc_sampler step, i.e. vmap(transition then
+ *     estimate) over chains (src/vmc/core/sampling.py:28-38,
+ *     kernels.py:131-245), fused into one launch;
+ *   - vmc_peps_amp_grad: _value_and_grad / peps_apply forward + hand-written
+ *     adjoint (src/vmc/peps/standard/compat.py:31-64,94-133);
+ *   - vmc_peps_local_energy: local_estimate (compat.py:136-194).
+ *
+ * Numerics: FP32 contractions with FP64 log-scales and FP64 energy
+ * accumulation.  Amplitudes are returned as (log|psi|, sign); log-derivatives
+ * O_k = dpsi/dA / psi are returned directly, so nothing underflows.
+ */
+#ifndef VMC_GB300_H_
+#define VMC_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int vmc_status;
+
+enum {
+  VMC_OK = 0,
+  VMC_ERR_INVALID = 1,     /* bad shape / dimension / null pointer */
+  VMC_ERR_UNSUPPORTED = 2, /* valid request the engine does not implement */
+  VMC_ERR_WORKSPACE = 3,   /* workspace smaller than vmc_workspace_size() */
+  VMC_ERR_CUDA = 4,        /* a CUDA runtime call failed */
+  VMC_ERR_NONFINITE = 5,   /* device status word reported NaN/Inf */
+  VMC_ERR_TIMEOUT = 6      /* a bounded device wait gave up */
+};
+
+/* dtype of the site tensors (the engine computes in FP32 either way). */
+enum { VMC_DTYPE_F32 = 0, VMC_DTYPE_C64 = 1 };
+
+/* Boundary-MPS strategy: strategy.py:44-92. */
+enum {
+  VMC_STRATEGY_NO_TRUNCATION = 0,
+  VMC_STRATEGY_ZIP_UP = 1,
+  VMC_STRATEGY_DENSITY_MATRIX = 2,
+  VMC_STRATEGY_VARIATIONAL = 3
+};
+
+/* Device status word bits (written by kernels, read with cudaMemcpy). */
+enum { VMC_DEV_NONFINITE = 1, VMC_DEV_TIMEOUT = 2 };
+
+typedef struct vmc_shape {
+  int n_rows;
+  int n_cols;
+} vmc_shape;
+
+typedef struct vmc_plan vmc_plan;
+
+/* Version and error strings. */
+const char* vmc_version(void);
+const char* vmc_status_string(vmc_status s);
+
+/*
+ * Create an immutable plan for an open-boundary n_rows x n_cols PEPS with
+ * bond dimension `bond_dim`, physical dimension `phys_dim` and boundary
+ * bond `chi` (truncate_bond_dimension).  `n_sweeps` is used by the
+ * variational strategy only.  Replaces the closure of
+ * build_mc_kernels (kernels.py:104-113) and PEPS.site_dims (model.py:27-35).
+ */
+vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys_dim,
+                         int dtype, int strategy, int n_sweeps, vmc_plan** out_plan);
+
+/*
+ * Attach the bucketed LocalHamiltonian (local_terms.py:165-200).  Terms of
+ * the same kind and location are summed by the caller.  All arrays are HOST
+ * arrays of float64, copied into the plan:
+ *   onesite[n_rows*n_cols][d][d], onesite_mask[n_rows*n_cols]
+ *   horiz[n_rows*(n_cols-1)][d*d][d*d], horiz_mask[...]
+ *   vert[(n_rows-1)*n_cols][d*d][d*d], vert_mask[...]
+ *   diagonal terms: n_diag terms; term t touches diag_nsites[t] sites listed
+ *   (row-major site ids) in diag_sites[diag_site_off[t] ...] and its table of
+ *   d^diag_nsites[t] values starts at diag_values[diag_value_off[t]].
+ * The local-energy convention is the reference's: an off-diagonal term adds
+ * sum_j op[j, s] psi(j) / psi (energy.py:176-200).
+ */
+vmc_status vmc_peps_plan_set_operator(vmc_plan* plan,
+                                      const double* onesite, const int* onesite_mask,
+                                      const double* horiz, const int* horiz_mask,
+                                      const double* vert, const int* vert_mask,
+                                      int n_diag, const int* diag_nsites,
+                                      const int* diag_site_off, const int* diag_sites,
+                                      const int* diag_value_off, const double* diag_values);
+
+void vmc_plan_destroy(vmc_plan* plan);
+
+/* Number of parameters per sample of the sliced log-derivative (sum of
+ * params_per_site, src/vmc/utils/smallo.py:23-35) and of the full tensors. */
+int64_t vmc_peps_n_params_sliced(const vmc_plan* plan);
+int64_t vmc_peps_n_params_full(const vmc_plan* plan);
+
+/* Bytes of the per-chain bottom-environment cache (Cache.bottom_envs,
+ * kernels.py:32-35) for n_chains chains, and of the scratch workspace one
+ * call needs.  The cache persists between sweeps; the workspace does not. */
+size_t vmc_cache_size(const vmc_plan* plan, int n_chains);
+size_t vmc_workspace_size(const vmc_plan* plan, int n_chains);
+
+/*
+ * init_cache (kernels.py:115-129): bottom environments of every row for
+ * configs[n_chains][n_sites] (int32 occupancies 0..d-1).
+ * tensors: FP32 site tensors packed site-major, each (d, up, down, left,
+ * right) C-order (the order of ravel_pytree over model.tensors).
+ */
+vmc_status vmc_peps_init_cache(const vmc_plan* plan, void* stream, const float* tensors,
+                               const int32_t* configs, int n_chains, void* cache,
+                               void* workspace, size_t workspace_bytes, int32_t* status_dev);
+
+/*
+ * One Monte-Carlo sweep for n_chains chains: transition (kernels.py:131-209)
+ * followed by estimate (kernels.py:211-245).
+ *   configs_inout[n_chains][n_sites] int32: updated in place.
+ *   uniforms[n_chains][n_sites] float64 in [0,1): the reference's per-site
+ *     jax.random.uniform(accept_key) draws (kernels.py:189-190).
+ *   deltas[n_chains][n_sites] int32 in [1,d) or NULL when d <= 2: the flip
+ *     offsets of kernels.py:170-175.
+ *   cache_inout: the bottom-environment cache (read by the transition,
+ *     rewritten by the estimate).
+ * Outputs (any may be NULL except out_E):
+ *   out_O[n_chains][n_params] FP32 log-derivatives dpsi/dA / psi, sliced
+ *     (full_gradient=0) or scattered into d x params (full_gradient=1)
+ *     (_assemble_log_derivatives, kernels.py:54-88);
+ *   out_p[n_chains][n_params_sliced] int8 active slice indices;
+ *   out_E[n_chains] FP64 local energies;
+ *   out_logamp[n_chains] FP64 log|psi| and out_sign[n_chains] FP64 sign;
+ *   out_margin[n_chains] FP32 min over sites of |min(1, ratio) - u| (the
+ *     distance of each accept decision from its threshold).
+ */
+vmc_status vmc_peps_sweep(const vmc_plan* plan, void* stream, const float* tensors,
+                          int32_t* configs_inout, const double* uniforms, const int32_t* deltas,
+                          int n_chains, void* cache_inout, int full_gradient, float* out_O,
+                          int8_t* out_p, double* out_E, double* out_logamp, double* out_sign,
+                          float* out_margin, void* workspace, size_t workspace_bytes,
+                          int32_t* status_dev);
+
+/*
+ * Amplitude and hand-written adjoint for samples[n][n_sites]
+ * (compat.py:31-64 peps_apply custom_vjp; compat.py:94-133 _value_and_grad;
+ * energy.py:276-301 _compute_all_gradients): log|psi|, sign and
+ * out_O = (dpsi/dA)/psi (sliced or full).  out_O may be NULL for values only.
+ */
+vmc_status vmc_peps_amp_grad(const vmc_plan* plan, void* stream, const float* tensors,
+                             const int32_t* samples, int n, int full_gradient, float* out_O,
+                             double* out_logamp, double* out_sign, void* workspace,
+                             size_t workspace_bytes, int32_t* status_dev);
+
+/*
+ * local_estimate (compat.py:136-194): E_loc for samples[n][n_sites] with the
+ * caller's amplitudes (amp = sign * exp(logamp)) as denominators.
+ */
+vmc_status vmc_peps_local_energy(const vmc_plan* plan, void* stream, const float* tensors,
+                                 const int32_t* samples, int n, const double* logamp,
+                                 const double* sign, double* out_E, void* workspace,
+                                 size_t workspace_bytes, int32_t* status_dev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VMC_GB300_H_ */

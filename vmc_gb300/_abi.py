@@ -1,0 +1,77 @@
+"""ctypes declarations of the C ABI in include/vmc_gb300.h.
+
+``bind(path)`` loads a shared library exporting that ABI and attaches the
+argument/return types of every entry point.  The package binds the CUDA
+build (``vmc_gb300/_native/libvmc_gb300.so``) through ``vmc_gb300._lib``.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+VMC_OK = 0
+VMC_ERR_INVALID = 1
+VMC_ERR_UNSUPPORTED = 2
+VMC_ERR_WORKSPACE = 3
+VMC_ERR_CUDA = 4
+VMC_ERR_NONFINITE = 5
+VMC_ERR_TIMEOUT = 6
+
+VMC_DTYPE_F32 = 0
+VMC_DTYPE_C64 = 1
+
+VMC_STRATEGY_NO_TRUNCATION = 0
+VMC_STRATEGY_ZIP_UP = 1
+VMC_STRATEGY_DENSITY_MATRIX = 2
+VMC_STRATEGY_VARIATIONAL = 3
+
+VMC_DEV_NONFINITE = 1
+VMC_DEV_TIMEOUT = 2
+
+
+class VmcShape(ct.Structure):
+    _fields_ = [("n_rows", ct.c_int), ("n_cols", ct.c_int)]
+
+
+_P = ct.c_void_p
+_I = ct.c_int
+_SZ = ct.c_size_t
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "vmc_version": (ct.c_char_p, []),
+    "vmc_status_string": (ct.c_char_p, [_I]),
+    "vmc_peps_plan": (_I, [ct.POINTER(VmcShape), _I, _I, _I, _I, _I, _I, ct.POINTER(_P)]),
+    "vmc_peps_plan_set_operator": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P]),
+    "vmc_plan_destroy": (None, [_P]),
+    "vmc_peps_n_params_sliced": (ct.c_int64, [_P]),
+    "vmc_peps_n_params_full": (ct.c_int64, [_P]),
+    "vmc_cache_size": (_SZ, [_P, _I]),
+    "vmc_workspace_size": (_SZ, [_P, _I]),
+    "vmc_peps_init_cache": (_I, [_P, _P, _P, _P, _I, _P, _P, _SZ, _P]),
+    "vmc_peps_sweep": (_I, [_P, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "vmc_peps_amp_grad": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _SZ, _P]),
+    "vmc_peps_local_energy": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _P]),
+}
+
+
+def bind(path: str) -> ct.CDLL:
+    lib = ct.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+class VmcError(RuntimeError):
+    """A C-ABI call returned a non-zero vmc_status."""
+
+    def __init__(self, status: int, where: str, lib=None):
+        msg = lib.vmc_status_string(status).decode() if lib is not None else str(status)
+        super().__init__(f"{where}: vmc_status {status} ({msg})")
+        self.status = status
+
+
+def check(lib, status: int, where: str) -> None:
+    if status != VMC_OK:
+        raise VmcError(status, where, lib)

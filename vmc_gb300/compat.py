@@ -1,0 +1,125 @@
+"""Evaluation surfaces of src/vmc/peps/standard/compat.py on the engine.
+
+* ``peps_apply``: amplitude with a hand-written adjoint (compat.py:31-64),
+  as a ``torch.autograd.Function``: the backward pass reuses the engine's
+  environment sweep (``vmc_peps_amp_grad``) instead of autodiff.
+* ``_value`` / ``_grad`` / ``_value_and_grad`` (compat.py:67-133).
+* ``local_estimate`` (compat.py:136-194).
+
+Samples may be occupancies (0..d-1) or +-1 spins, like the reference's
+``spin_to_occupancy`` (src/vmc/utils/utils.py:55-57).
+"""
+from __future__ import annotations
+
+import torch
+
+from .lowering import params_per_site
+
+__all__ = ["peps_apply", "log_value", "_value", "_grad", "_value_and_grad", "local_estimate",
+           "spin_to_occupancy", "occupancy_to_spin"]
+
+
+def spin_to_occupancy(spins):
+    """src/vmc/utils/utils.py:55-57 (idempotent on 0/1 occupancies)."""
+    return torch.div(spins + 1, 2, rounding_mode="floor").to(torch.int32)
+
+
+def occupancy_to_spin(occ):
+    """src/vmc/utils/utils.py:50-52."""
+    return (2 * occ - 1).to(torch.int32)
+
+
+def _samples(model, samples):
+    s = torch.as_tensor(samples, device=model.device)
+    if s.ndim == 1:
+        s = s[None]
+    n_sites = model.shape[0] * model.shape[1]
+    s = s.reshape(-1, n_sites)
+    if model.phys_dim == 2:
+        s = spin_to_occupancy(s)
+    return s.to(torch.int32).contiguous()
+
+
+class _PepsAmplitude(torch.autograd.Function):
+    """amp(theta) with d amp / d theta from the stored-environment adjoint (energy.py:276-301)."""
+
+    @staticmethod
+    def forward(ctx, packed, samples, engine):
+        logamp, sign, O = engine.amp_grad(packed.detach().contiguous(), samples, full_gradient=True,
+                                          want_O=packed.requires_grad)
+        amp = sign * torch.exp(logamp)
+        if O is not None:
+            ctx.save_for_backward(O, amp)
+        return amp
+
+    @staticmethod
+    def backward(ctx, g):
+        O, amp = ctx.saved_tensors
+        # d amp_i / d theta = amp_i * O_i  (O = dpsi/dtheta / psi, full layout)
+        grad = ((g * amp)[:, None] * O.to(torch.float64)).sum(0)
+        return grad.to(torch.float32), None, None
+
+
+def peps_apply(tensors, sample, shape, strategy, model=None):
+    """compat.py:31-40: amplitude(s) of `sample` (n, n_sites) or (n_sites,)."""
+    from .peps import PEPS
+
+    if model is None:
+        if isinstance(tensors, PEPS):
+            model = tensors
+        else:
+            raise TypeError("peps_apply needs the PEPS model (it carries the engine plan)")
+    packed = model.packed(tensors if not isinstance(tensors, PEPS) else None)
+    s = _samples(model, sample)
+    amp = _PepsAmplitude.apply(packed, s, model.engine())
+    return amp if torch.as_tensor(sample).ndim > 1 else amp[0]
+
+
+def log_value(model, samples, tensors=None):
+    """(log|psi|, sign) for a batch; never underflows."""
+    eng = model.engine()
+    logamp, sign, _ = eng.amp_grad(model.packed(tensors), _samples(model, samples), want_O=False)
+    return logamp, sign
+
+
+def _value(model, sample):
+    """compat.py:67-78 (float64 amplitudes)."""
+    la, sg = log_value(model, sample)
+    amp = sg * torch.exp(la)
+    return amp if torch.as_tensor(sample).ndim > 1 else amp[0]
+
+
+def _value_and_grad(model, sample, *, full_gradient=False):
+    """compat.py:94-133: (amp, dpsi/dA, p) with the sliced or full layout."""
+    eng = model.engine()
+    s = _samples(model, sample)
+    logamp, sign, O = eng.amp_grad(model.packed(), s, full_gradient=full_gradient, want_O=True)
+    amp = sign * torch.exp(logamp)
+    grads = O.to(torch.float64) * amp[:, None]
+    p = None
+    if not full_gradient:
+        pps = torch.as_tensor(params_per_site(model.shape, model.bond_dim), device=s.device)
+        p = torch.repeat_interleave(s.to(torch.int8), pps, dim=1)
+    if torch.as_tensor(sample).ndim == 1:
+        return amp[0], grads[0], None if p is None else p[0]
+    return amp, grads, p
+
+
+def _grad(model, sample, *, full_gradient=False):
+    """compat.py:81-91."""
+    _, g, p = _value_and_grad(model, sample, full_gradient=full_gradient)
+    return g, p
+
+
+def local_estimate(model, samples, operator, amps):
+    """compat.py:136-194: E_loc with the caller's amplitudes as denominators.
+
+    ``amps`` is a tensor of amplitudes or a (log|psi|, sign) pair."""
+    eng = model.engine(operator)
+    s = _samples(model, samples)
+    if isinstance(amps, tuple):
+        logamp, sign = amps
+    else:
+        a = torch.as_tensor(amps, device=s.device, dtype=torch.float64)
+        logamp, sign = torch.log(torch.abs(a)), torch.sign(a)
+    return eng.local_energy(model.packed(), s, logamp, sign)

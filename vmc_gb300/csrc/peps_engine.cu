@@ -1,0 +1,1189 @@
+// peps_engine.cu -- fused per-sample PEPS evaluation on GB300 (sm_103a).
+//
+// One CTA owns one chain at a time (persistent grid over chains) and runs the
+// whole reference sweep for it -- transition (kernels.py:131-209) and estimate
+// (kernels.py:211-245) -- from one launch.  All tensor contractions are CTA
+// GEMMs (device_common.cuh); the boundary-MPS truncation is a CTA-level
+// one-sided Jacobi SVD.  Boundary MPSs are renormalised tensor by tensor and
+// their log-norms are carried in FP64, so nothing underflows for any lattice.
+//
+// Layouts (row-major, last index fastest):
+//   site tensor A[p][u][v][l][r]           (d, up, down, left, right)
+//   boundary MPS tensor [left][phys][right]
+//   1-row environment   [top][mpo][bottom]
+//   2-row environment   [top][mpo row r][mpo row r+1][bottom]
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+#include <algorithm>
+
+#include "device_common.cuh"
+#include "../../include/vmc_gb300.h"
+
+#ifdef VMC_HOST_EMULATION
+thread_local vmc_dim3 threadIdx, blockIdx, blockDim, gridDim;
+#endif
+
+namespace vmc {
+
+constexpr int kThreads = 256;
+constexpr int kMaxVec = 512;   // max vectors in one truncation (chi * D)
+constexpr int kMaxCols = 64;   // max lattice columns
+constexpr int kMaxD = 4;       // max physical dimension
+constexpr int kPermKinds = 5;  // permuted copies of every site tensor
+enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4 };
+enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3 };
+
+// Device-side plan: scalars plus device pointers into one allocation.
+struct DevPlan {
+  int R, C, D, d, chi, strategy, n_sweeps, n_sites;
+  int np_sliced;          // sum of params_per_site
+  int TS, ES, E2S, SCR, MM;  // buffer sizes (floats)
+  int n_scr;              // number of SCR scratch buffers per slot
+  long long slot_floats;  // floats per workspace slot
+  long long perm_floats;  // floats of the permuted tensor pack
+  long long cache_floats_per_chain;  // bottom env tensors per chain
+  // per-site (n_sites)
+  const int* sdim;        // [n_sites][4] up, down, left, right
+  const int* site_off;    // packed params offset
+  const int* site_osl;    // offset in the sliced O vector
+  const int* perm_off;    // offset in the permuted pack
+  // bond dims
+  const int* tb;          // [(R+1)][(C+1)] top env bonds (row r = before row r)
+  const int* bb;          // [R][(C+1)] bottom env bonds (row r = rows r+1.. from below)
+  // operator
+  const float* onesite;   // [n_sites][d][d]
+  const int* onesite_mask;
+  const float* horiz;     // [R*(C-1)][d*d][d*d]
+  const int* horiz_mask;
+  const float* vert;      // [(R-1)*C][d*d][d*d]
+  const int* vert_mask;
+  const int* row_has_h;   // [R] any horizontal term in row
+  const int* row_has_v;   // [R] any vertical term between r and r+1
+  int n_diag;
+  const int* diag_nsites;
+  const int* diag_site_off;
+  const int* diag_sites;
+  const int* diag_value_off;
+  const double* diag_values;
+};
+
+struct Slot {
+  float* topc;   // (R+1)*C*TS
+  double* lt;    // R+1
+  float* brow[3];
+  float* renv;   // d*C*ES  [q][c]
+  float* lenv;   // (d+1)*ES
+  float* r2;     // C*E2S
+  float* l2[2];  // E2S
+  float* svm;    // MM
+  float* svc;    // MM
+  float* svq;    // MM
+  float* scr[24];
+};
+
+__host__ __device__ inline long long al64(long long n) { return (n + 63) & ~63LL; }
+
+__device__ inline Slot make_slot(const DevPlan& P, float* base) {
+  Slot s;
+  float* p = base;
+  s.topc = p; p += al64((long long)(P.R + 1) * P.C * P.TS);
+  s.lt = reinterpret_cast<double*>(p); p += al64(2 * (P.R + 2));
+  for (int i = 0; i < 3; ++i) { s.brow[i] = p; p += al64((long long)P.C * P.TS); }
+  s.renv = p; p += al64((long long)P.d * P.C * P.ES);
+  s.lenv = p; p += al64((long long)(P.d + 1) * P.ES);
+  s.r2 = p; p += al64((long long)P.C * P.E2S);
+  for (int i = 0; i < 2; ++i) { s.l2[i] = p; p += al64(P.E2S); }
+  s.svm = p; p += al64(P.MM);
+  s.svc = p; p += al64(P.MM);
+  s.svq = p; p += al64(P.MM);
+  for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
+  return s;
+}
+
+struct Shared {
+  double red[32];
+  int flag;
+  int sel[kMaxVec];
+  float sig[kMaxVec];
+  int spins[2][kMaxCols];
+  double bcast[8];
+};
+
+__device__ inline int site_id(const DevPlan& P, int r, int c) { return r * P.C + c; }
+__device__ inline int ssize(const DevPlan& P, int s) {
+  const int* d4 = P.sdim + 4 * s;
+  return d4[0] * d4[1] * d4[2] * d4[3];
+}
+__device__ inline const float* perm_of(const DevPlan& P, const float* perm, int s, int kind, int p) {
+  return perm + P.perm_off[s] + (size_t)(kind * P.d + p) * ssize(P, s);
+}
+__device__ inline const float* slice_of(const DevPlan& P, const float* tensors, int s, int p) {
+  return tensors + P.site_off[s] + (size_t)p * ssize(P, s);
+}
+
+// ---------------------------------------------------------------------------
+// Permuted copies of the site tensors (shared by all chains).
+// ---------------------------------------------------------------------------
+__global__ void permute_tensors_kernel(const DevPlan* __restrict__ Pp, const float* __restrict__ tensors,
+                                       float* __restrict__ perm) {
+  const DevPlan& P = *Pp;
+  for (int s = blockIdx.x; s < P.n_sites; s += gridDim.x) {
+    const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1], L = P.sdim[4 * s + 2], Rr = P.sdim[4 * s + 3];
+    const int sz = U * V * L * Rr;
+    const int total = P.d * sz;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int p = i / sz;
+      int t = i % sz;
+      const int r = t % Rr; t /= Rr;
+      const int l = t % L; t /= L;
+      const int v = t % V;
+      const int u = t / V;
+      const float x = tensors[P.site_off[s] + i];
+      float* base = perm + P.perm_off[s];
+      // [l][u][v][r]
+      base[(size_t)(P_ZIPT * P.d + p) * sz + ((l * U + u) * V + v) * Rr + r] = x;
+      // [l][v][u][r]
+      base[(size_t)(P_ZIPB * P.d + p) * sz + ((l * V + v) * U + u) * Rr + r] = x;
+      // [u][r][l][v]
+      base[(size_t)(P_RENV * P.d + p) * sz + ((u * Rr + r) * L + l) * V + v] = x;
+      // [l][u][r][v]
+      base[(size_t)(P_LENV * P.d + p) * sz + ((l * U + u) * Rr + r) * V + v] = x;
+      // [u][r][v][l]
+      base[(size_t)(P_R2 * P.d + p) * sz + ((u * Rr + r) * V + v) * L + l] = x;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Contraction steps.  Dimension names: ta/tb top-MPS bonds left/right of the
+// column, ba/bb bottom-MPS bonds, U/V up/down legs, Lb/Rb left/right legs.
+// ---------------------------------------------------------------------------
+
+// X1[a][u][rr][f] = sum_b T[a][u][b] R[b][rr][f]
+__device__ inline void renv_step1(const float* T, const float* Rin, float* X1, int ta, int U, int tb, int Rb,
+                                  int bb) {
+  cta_gemm(make_gemm(T, lin(tb), 1, Rin, lin(1), Rb * bb, X1, lin(Rb * bb), lin(1), ta * U, Rb * bb, tb));
+}
+// R'[a][l][e] = sum_{u,rr,v,f} X1[a][u][rr][f] A(u,v,l,rr) B[e][v][f]
+__device__ inline void renv_step23(const float* X1, const float* Aperm_renv, const float* B, float* X2, float* Rout,
+                                   int ta, int U, int Rb, int bb, int Lb, int V, int ba) {
+  cta_gemm(make_gemm(X1, two(bb, U * Rb * bb, 1), bb, Aperm_renv, lin(1), Lb * V, X2, two(bb, Lb * V * bb, 1),
+                     lin(bb), ta * bb, Lb * V, U * Rb));
+  cta_gemm(make_gemm(X2, lin(V * bb), 1, B, lin(V * bb), 1, Rout, lin(ba), lin(1), ta * Lb, ba, V * bb));
+}
+// Y1[e][b][l][u] = sum_a L[a][l][e] T[a][u][b]
+__device__ inline void lenv_step1(const float* Lin, const float* T, float* Y1, int ta, int Lb, int ba, int U,
+                                  int tb) {
+  cta_gemm(make_gemm(Lin, lin(1), Lb * ba, T, lin(1), U * tb, Y1, two(ba, U, tb * Lb * U), two(tb, 1, Lb * U),
+                     Lb * ba, U * tb, ta));
+}
+// L'[b][rr][f] = sum_{e,l,u,v} Y1[e][b][l][u] A(u,v,l,rr) B[e][v][f]
+__device__ inline void lenv_step23(const float* Y1, const float* Aperm_lenv, const float* B, float* Y2, float* Lout,
+                                   int ba, int tb, int Lb, int U, int Rb, int V, int bb) {
+  cta_gemm(make_gemm(Y1, lin(Lb * U), 1, Aperm_lenv, lin(1), Rb * V, Y2, two(tb, V, Rb * ba * V),
+                     two(V, ba * V, 1), ba * tb, Rb * V, Lb * U));
+  cta_gemm(make_gemm(Y2, lin(ba * V), 1, B, lin(1), bb, Lout, lin(bb), lin(1), tb * Rb, bb, ba * V));
+}
+// G[u][v][l][rr] = alpha * sum Y1[e][b][l][u] B[e][v][f] R[b][rr][f]
+__device__ inline void grad_env(const float* Y1, const float* B, const float* Rc, float* W, float* G, int ba,
+                                int V, int bb, int tb, int Rb, int Lb, int U, float alpha) {
+  cta_gemm(make_gemm(B, lin(bb), 1, Rc, lin(bb), 1, W, two(V, tb * V * Rb, Rb), two(Rb, V * Rb, 1), ba * V,
+                     tb * Rb, bb));
+  cta_gemm(make_gemm(Y1, lin(1), Lb * U, W, lin(1), V * Rb, G, two(U, Rb, V * Lb * Rb), two(Rb, Lb * Rb, 1),
+                     Lb * U, V * Rb, ba * tb, alpha));
+}
+
+// ---------------------------------------------------------------------------
+// Boundary-MPS row application (strategy.apply of strategy.py:118-150 and
+// contraction.py:59-65).  src/dst hold C tensors at stride TS.  Returns the
+// sum of log-norms divided out of the new tensors.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared& sh, const float* perm, const float* src,
+                            const int* bin, float* dst, const int* bout, int row, const int* spins,
+                            bool from_below) {
+  const int C = P.C;
+  double logsum = 0.0;
+  float* carry = S.scr[0];
+  float* carry_next = S.scr[1];
+  float* Z1 = S.scr[2];
+  if (threadIdx.x == 0) carry[0] = 1.f;
+  __syncthreads();
+  int kc = 1;
+  for (int c = 0; c < C; ++c) {
+    const int s = site_id(P, row, c);
+    const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1], Lb = P.sdim[4 * s + 2], Rb = P.sdim[4 * s + 3];
+    const int pin = from_below ? V : U;
+    const int pout = from_below ? U : V;
+    const float* Ap = perm_of(P, perm, s, from_below ? P_ZIPB : P_ZIPT, spins[c]);
+    const int din = bin[c], dn = bin[c + 1];
+    const float* m = src + (size_t)c * P.TS;
+    float* out = dst + (size_t)c * P.TS;
+    if (P.strategy == VMC_STRATEGY_NO_TRUNCATION) {
+      // out[d][l][q][r'][w] = sum_p m[d][p][r'] A(p, q, l, w)
+      const int ncol = dn * Rb;
+      cta_gemm(make_gemm(m, two(dn, pin * dn, 1), dn, Ap, three(pout, Rb, pin * pout * Rb, Rb, 1), pout * Rb, out,
+                         two(dn, Lb * pout * ncol, Rb), three(pout, Rb, pout * ncol, ncol, 1), din * dn,
+                         Lb * pout * Rb, pin));
+      const int n_el = din * Lb * pout * ncol;
+      const double nrm2 = cta_dot(out, out, n_el, sh.red);
+      const double nrm = sqrt(nrm2);
+      if (nrm > 0.0) {
+        cta_scale(out, (float)(1.0 / nrm), n_el);
+        logsum += log(nrm);
+      }
+      continue;
+    }
+    // Z1[k][l][p][r'] = sum_d carry[k][l][d] m[d][p][r']
+    cta_gemm(make_gemm(carry, lin(din), 1, m, lin(1), pin * dn, Z1, lin(pin * dn), lin(1), kc * Lb, pin * dn, din));
+    const int mrows = kc * pout;
+    const int ncols = dn * Rb;
+    if (c == C - 1) {
+      // last site: untruncated, out[k][q][(r',w)]
+      cta_gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, out, two(dn, pout * ncols, Rb),
+                         two(Rb, ncols, 1), kc * dn, pout * Rb, Lb * pin));
+      const int n_el = mrows * ncols;
+      const double nrm = sqrt(cta_dot(out, out, n_el, sh.red));
+      if (nrm > 0.0) {
+        cta_scale(out, (float)(1.0 / nrm), n_el);
+        logsum += log(nrm);
+      }
+      break;
+    }
+    const int kout = bout[c + 1];
+    const bool by_cols = mrows >= ncols;
+    float* mat = S.svm;
+    if (by_cols) {
+      const int ldv = mrows;
+      // vectors = columns; element (row, col) at col*ldv + row
+      cta_gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat, two(dn, pout, Rb * ldv),
+                         two(Rb, 1, ldv), kc * dn, pout * Rb, Lb * pin));
+      cta_copy(S.svc, mat, ncols * ldv);
+      if (kout < ncols || true) {
+        jacobi_orthogonalize(mat, ncols, mrows, ldv, nullptr, 0, 0, 2e-7f, 30, &sh.flag);
+      }
+      // column norms and top-kout selection
+      for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
+        float a = 0.f;
+        for (int i = 0; i < mrows; ++i) a = fmaf(mat[(size_t)j * ldv + i], mat[(size_t)j * ldv + i], a);
+        sh.sig[j] = a;
+      }
+      __syncthreads();
+      for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
+        int rank = 0;
+        const float sj = sh.sig[j];
+        for (int i = 0; i < ncols; ++i) {
+          const float si = sh.sig[i];
+          rank += (si > sj) || (si == sj && i < j);
+        }
+        if (rank < kout) sh.sel[rank] = j;
+      }
+      __syncthreads();
+      float smax = 0.f;
+      for (int i = 0; i < ncols; ++i) smax = fmaxf(smax, sh.sig[i]);
+      // out[(k,q)][k'] = col_sel[k'] / sigma
+      for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) {
+        const int i = e / kout, kk = e % kout;
+        const int j = sh.sel[kk];
+        const float s2 = sh.sig[j];
+        out[e] = (s2 > 1e-30f * smax && s2 > 0.f) ? mat[(size_t)j * ldv + i] / sqrtf(s2) : 0.f;
+      }
+      __syncthreads();
+      // carry'[k'][w][r'] = sum_i out[i][k'] * matc[i][(r',w)]
+      cta_gemm(make_gemm(out, lin(1), kout, S.svc, lin(ldv), 1, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols,
+                         mrows));
+    } else {
+      const int ldv = ncols;
+      // vectors = rows; element (row, col) at row*ldv + col
+      cta_gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat, two(dn, pout * ldv, Rb),
+                         two(Rb, ldv, 1), kc * dn, pout * Rb, Lb * pin));
+      if (kout >= mrows) {
+        // keep everything: U = I, carry = mat
+        for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) out[e] = (e / mrows == e % mrows) ? 1.f : 0.f;
+        for (int e = threadIdx.x; e < mrows * ncols; e += blockDim.x) {
+          const int i = e / ncols, col = e % ncols;
+          const int rp = col / Rb, w = col % Rb;
+          carry_next[(size_t)i * ncols + w * dn + rp] = mat[(size_t)i * ldv + col];
+        }
+        __syncthreads();
+      } else {
+        float* Q = S.svq;
+        const int ldq = mrows;
+        for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) Q[e] = (e / mrows == e % mrows) ? 1.f : 0.f;
+        __syncthreads();
+        jacobi_orthogonalize(mat, mrows, ncols, ldv, Q, mrows, ldq, 2e-7f, 30, &sh.flag);
+        for (int j = threadIdx.x; j < mrows; j += blockDim.x) {
+          float a = 0.f;
+          for (int i = 0; i < ncols; ++i) a = fmaf(mat[(size_t)j * ldv + i], mat[(size_t)j * ldv + i], a);
+          sh.sig[j] = a;
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < mrows; j += blockDim.x) {
+          int rank = 0;
+          const float sj = sh.sig[j];
+          for (int i = 0; i < mrows; ++i) {
+            const float si = sh.sig[i];
+            rank += (si > sj) || (si == sj && i < j);
+          }
+          if (rank < kout) sh.sel[rank] = j;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) {
+          const int i = e / kout, kk = e % kout;
+          out[e] = Q[(size_t)sh.sel[kk] * ldq + i];
+        }
+        for (int e = threadIdx.x; e < kout * ncols; e += blockDim.x) {
+          const int kk = e / ncols, col = e % ncols;
+          const int rp = col / Rb, w = col % Rb;
+          carry_next[(size_t)kk * ncols + w * dn + rp] = mat[(size_t)sh.sel[kk] * ldv + col];
+        }
+        __syncthreads();
+      }
+    }
+    // renormalise the new tensor
+    {
+      const int n_el = mrows * kout;
+      const double nrm = sqrt(cta_dot(out, out, n_el, sh.red));
+      if (nrm > 0.0) {
+        cta_scale(out, (float)(1.0 / nrm), n_el);
+        logsum += log(nrm);
+      }
+    }
+    // swap carry buffers
+    float* t = carry;
+    carry = carry_next;
+    carry_next = t;
+    kc = kout;
+  }
+  return logsum;
+}
+
+// contract_bottom (contraction.py:30-35): product of the row's matrices
+// t[:, 0, :], evaluated by one thread in FP64 using `tmp` (>= 2*max bond
+// doubles of workspace).
+__device__ __noinline__ double contract_bottom(const DevPlan& P, const float* row, const int* bonds, Shared& sh, double* tmp,
+                                  double* sign) {
+  if (threadIdx.x == 0) {
+    double* v = tmp;
+    double* w = tmp + kMaxVec;
+    v[0] = 1.0;
+    for (int c = 0; c < P.C; ++c) {
+      const int l = bonds[c], r = bonds[c + 1];
+      const float* t = row + (size_t)c * P.TS;
+      for (int j = 0; j < r; ++j) {
+        double a = 0.0;
+        for (int i = 0; i < l; ++i) a += v[i] * (double)t[i * r + j];
+        w[j] = a;
+      }
+      for (int j = 0; j < r; ++j) v[j] = w[j];
+    }
+    sh.bcast[0] = v[0];
+  }
+  __syncthreads();
+  const double val = sh.bcast[0];
+  __syncthreads();
+  *sign = val < 0 ? -1.0 : 1.0;
+  return val == 0.0 ? -INFINITY : log(fabs(val));
+}
+
+__device__ inline void fill_ones_row(const DevPlan& P, float* row) {
+  for (int c = threadIdx.x; c < P.C; c += blockDim.x) row[(size_t)c * P.TS] = 1.f;
+  __syncthreads();
+}
+
+// Right environments of one row: R[q][c] for c = C-1..0 (R_c covers columns
+// > c).  With open_q, R_c is produced for every spin q of site c+1
+// (renv[q][c]); otherwise only for its current spin (renv[spin][c] and also
+// stored at renv[0][c]... the caller reads renv_cur()).
+__device__ __noinline__ void right_envs(const DevPlan& P, const Slot& S, const float* perm, const float* top, const int* tbond,
+                           const float* bot, const int* bbond, int row, const int* spins, bool open_q) {
+  const int C = P.C;
+  float* X1 = S.scr[3];
+  float* X2 = S.scr[4];
+  // R_{C-1} = [1] for every q slot
+  for (int q = threadIdx.x; q < P.d; q += blockDim.x) S.renv[((size_t)q * C + (C - 1)) * P.ES] = 1.f;
+  __syncthreads();
+  for (int c = C - 1; c >= 1; --c) {
+    // absorb site c into R_c -> R_{c-1}
+    const int s = site_id(P, row, c);
+    const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1], Lb = P.sdim[4 * s + 2], Rb = P.sdim[4 * s + 3];
+    const int ta = tbond[c], tb = tbond[c + 1], ba = bbond[c], bb = bbond[c + 1];
+    const float* T = top + (size_t)c * P.TS;
+    const float* B = bot + (size_t)c * P.TS;
+    // R_c (current spin of site c+1) lives in slot spin(c+1); for c = C-1 all slots hold [1]
+    const int qin = (c == C - 1) ? 0 : spins[c + 1];
+    const float* Rin = S.renv + ((size_t)qin * C + c) * P.ES;
+    renv_step1(T, Rin, X1, ta, U, tb, Rb, bb);
+    for (int q = 0; q < P.d; ++q) {
+      if (!open_q && q != spins[c]) continue;
+      float* Rout = S.renv + ((size_t)q * C + (c - 1)) * P.ES;
+      renv_step23(X1, perm_of(P, perm, s, P_RENV, q), B, X2, Rout, ta, U, Rb, bb, Lb, V, ba);
+    }
+  }
+}
+
+__device__ inline const float* renv_cur(const DevPlan& P, const Slot& S, const int* spins, int c) {
+  const int q = (c == P.C - 1) ? 0 : spins[c + 1];
+  return S.renv + ((size_t)q * P.C + c) * P.ES;
+}
+
+// ---------------------------------------------------------------------------
+// Transition of one row (kernels.py:142-206): Metropolis along the row.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Shared& sh, const float* perm, const float* top,
+                               const int* tbond, const float* bot, const int* bbond, int row, int* spins,
+                               const double* uniforms, const int32_t* deltas, float* min_margin) {
+  const int C = P.C;
+  right_envs(P, S, perm, top, tbond, bot, bbond, row, spins, false);
+  float* Lc = S.lenv;                  // current left env
+  float* Lp0 = S.lenv + P.ES;          // L' for the current spin
+  float* Lp1 = S.lenv + 2 * P.ES;      // L' for the proposed spin
+  float* Y1 = S.scr[3];
+  float* Y2 = S.scr[4];
+  if (threadIdx.x == 0) Lc[0] = 1.f;
+  __syncthreads();
+  double amp_cur = 0.0;
+  for (int c = 0; c < C; ++c) {
+    const int s = site_id(P, row, c);
+    const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1], Lb = P.sdim[4 * s + 2], Rb = P.sdim[4 * s + 3];
+    const int ta = tbond[c], tb = tbond[c + 1], ba = bbond[c], bb = bbond[c + 1];
+    const float* T = top + (size_t)c * P.TS;
+    const float* B = bot + (size_t)c * P.TS;
+    const float* Rc = renv_cur(P, S, spins, c);
+    const int cur = spins[c];
+    int flip = cur;
+    if (P.d == 2) flip = 1 - cur;
+    else if (P.d > 2) flip = (cur + deltas[row * C + c]) % P.d;
+    lenv_step1(Lc, T, Y1, ta, Lb, ba, U, tb);
+    lenv_step23(Y1, perm_of(P, perm, s, P_LENV, cur), B, Y2, Lp0, ba, tb, Lb, U, Rb, V, bb);
+    const int n_env = tb * Rb * bb;
+    if (c == 0) amp_cur = cta_dot(Lp0, Rc, n_env, sh.red);
+    double amp_flip = amp_cur;
+    if (flip != cur) {
+      lenv_step23(Y1, perm_of(P, perm, s, P_LENV, flip), B, Y2, Lp1, ba, tb, Lb, U, Rb, V, bb);
+      amp_flip = cta_dot(Lp1, Rc, n_env, sh.red);
+    }
+    // _metropolis_ratio (contraction.py:88-94) and accept (kernels.py:188-193)
+    const double pc = amp_cur * amp_cur, pf = amp_flip * amp_flip;
+    double ratio;
+    if (pc > 0.0) ratio = pf / pc;
+    else ratio = pf > 0.0 ? INFINITY : 0.0;
+    const double thr = ratio < 1.0 ? ratio : 1.0;
+    const double u = uniforms[row * C + c];
+    const bool accept = (flip != cur) && (u < thr);
+    const float margin = (float)fabs(thr - u);
+    if (threadIdx.x == 0 && margin < *min_margin) *min_margin = margin;
+    if (accept) {
+      amp_cur = amp_flip;
+      if (threadIdx.x == 0) spins[c] = flip;
+    }
+    __syncthreads();
+    float* sel = accept ? Lp1 : Lp0;
+    cta_copy(Lc, sel, n_env);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Estimate of one row (energy.py:158-205): gradient envs, one-site and
+// horizontal energies.  `oscale` = exp(lt + lb - logamp) * sign(amp).
+// ---------------------------------------------------------------------------
+__device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Shared& sh, const float* perm, const float* tensors,
+                               const float* top, const int* tbond, const float* bot, const int* bbond, int row,
+                               const int* spins, double oscale, float* Orow, int full_gradient, bool want_grad,
+                               bool want_energy) {
+  const int C = P.C;
+  const bool has_h = want_energy && P.row_has_h[row];
+  right_envs(P, S, perm, top, tbond, bot, bbond, row, spins, has_h);
+  float* Lc = S.lenv;
+  float* Y1 = S.scr[3];
+  float* Y2 = S.scr[4];
+  float* W = S.scr[5];
+  float* Gtmp = S.scr[6];
+  if (threadIdx.x == 0) Lc[0] = 1.f;
+  __syncthreads();
+  double energy = 0.0;
+  for (int c = 0; c < C; ++c) {
+    const int s = site_id(P, row, c);
+    const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1], Lb = P.sdim[4 * s + 2], Rb = P.sdim[4 * s + 3];
+    const int ta = tbond[c], tb = tbond[c + 1], ba = bbond[c], bb = bbond[c + 1];
+    const float* T = top + (size_t)c * P.TS;
+    const float* B = bot + (size_t)c * P.TS;
+    const float* Rc = renv_cur(P, S, spins, c);
+    const int cur = spins[c];
+    const int sz = U * V * Lb * Rb;
+    lenv_step1(Lc, T, Y1, ta, Lb, ba, U, tb);
+    const bool os = want_energy && P.onesite_mask[s];
+    if (want_grad || os) {
+      float* G = Gtmp;
+      if (want_grad && Orow != nullptr) {
+        G = Orow + (full_gradient ? (size_t)P.d * P.site_osl[s] + (size_t)cur * sz : (size_t)P.site_osl[s]);
+      }
+      grad_env(Y1, B, Rc, W, G, ba, V, bb, tb, Rb, Lb, U, (float)oscale);
+      if (os) {
+        // amps_site[p] = sum A[p] . G  (already divided by psi); E += sum_p op[p, s] amps[p]
+        for (int p = 0; p < P.d; ++p) {
+          const double ap = cta_dot(slice_of(P, tensors, s, p), G, sz, sh.red);
+          energy += (double)P.onesite[((size_t)s * P.d + p) * P.d + cur] * ap;
+        }
+      }
+    }
+    const int n_env = tb * Rb * bb;
+    const bool hz = has_h && c < C - 1 && P.horiz_mask[row * (C - 1) + c];
+    if (hz) {
+      // L'^{(p)} for every p, R_c^{(q)} for every q: psi(p,q) = <L'^p, R^q>
+      const int sn = site_id(P, row, c + 1);
+      const int cur1 = spins[c + 1];
+      const float* op = P.horiz + (size_t)(row * (C - 1) + c) * P.d * P.d * P.d * P.d;
+      const int col = cur * P.d + cur1;
+      for (int p = 0; p < P.d; ++p) {
+        float* Lp = S.lenv + (size_t)(1 + p) * P.ES;
+        lenv_step23(Y1, perm_of(P, perm, s, P_LENV, p), B, Y2, Lp, ba, tb, Lb, U, Rb, V, bb);
+        for (int q = 0; q < P.d; ++q) {
+          const float* Rq = S.renv + ((size_t)q * C + c) * P.ES;
+          const double psi = cta_dot(Lp, Rq, n_env, sh.red);
+          energy += (double)op[(size_t)(p * P.d + q) * P.d * P.d + col] * psi * oscale;
+        }
+      }
+      (void)sn;
+      cta_copy(Lc, S.lenv + (size_t)(1 + cur) * P.ES, n_env);
+    } else if (c < C - 1) {
+      float* Lp = S.lenv + P.ES;
+      lenv_step23(Y1, perm_of(P, perm, s, P_LENV, cur), B, Y2, Lp, ba, tb, Lb, U, Rb, V, bb);
+      cta_copy(Lc, Lp, n_env);
+    }
+  }
+  return energy;
+}
+
+// ---------------------------------------------------------------------------
+// Vertical energy of the row pair (r, r+1) (energy.py:24-95).
+// top: top env of row r; bot: bottom env of row r+1.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, Shared& sh, const float* perm, const float* top,
+                                  const int* tbond, const float* bot, const int* bbond, int r, const int* sp0,
+                                  const int* sp1, double vscale) {
+  const int C = P.C;
+  float* P1 = S.scr[7];
+  float* P2 = S.scr[8];
+  float* P3 = S.scr[9];
+  // R2_{C-1} = [1]
+  if (threadIdx.x == 0) S.r2[(size_t)(C - 1) * P.E2S] = 1.f;
+  __syncthreads();
+  for (int c = C - 1; c >= 1; --c) {
+    const int s0 = site_id(P, r, c), s1 = site_id(P, r + 1, c);
+    const int U = P.sdim[4 * s0], V = P.sdim[4 * s0 + 1], Lb = P.sdim[4 * s0 + 2], Rb = P.sdim[4 * s0 + 3];
+    const int V1 = P.sdim[4 * s1 + 1], Lb1 = P.sdim[4 * s1 + 2], Rb1 = P.sdim[4 * s1 + 3];
+    const int ta = tbond[c], tb = tbond[c + 1], ba = bbond[c], bb = bbond[c + 1];
+    const float* T = top + (size_t)c * P.TS;
+    const float* B = bot + (size_t)c * P.TS;
+    const float* Rin = S.r2 + (size_t)c * P.E2S;
+    float* Rout = S.r2 + (size_t)(c - 1) * P.E2S;
+    // P1[a][u][rr][y][f] = sum_b T[a][u][b] R2[b][rr][y][f]
+    cta_gemm(make_gemm(T, lin(tb), 1, Rin, lin(1), Rb * Rb1 * bb, P1, lin(Rb * Rb1 * bb), lin(1), ta * U,
+                       Rb * Rb1 * bb, tb));
+    // P2[a][l][f][v][y] = sum_{u,rr} P1[a][u][rr][(y,f)] A(u,v,l,rr)
+    cta_gemm(make_gemm(P1, two(Rb1 * bb, U * Rb * Rb1 * bb, 1), Rb1 * bb, perm_of(P, perm, s0, P_RENV, sp0[c]),
+                       lin(1), Lb * V, P2, three(Rb1, bb, Lb * bb * V * Rb1, 1, V * Rb1), two(V, bb * V * Rb1, Rb1),
+                       ta * Rb1 * bb, Lb * V, U * Rb));
+    // P3[a][l][x][w][f] = sum_{v,y} P2[a][l][f][v][y] A'(v,w,x,y)
+    cta_gemm(make_gemm(P2, lin(V * Rb1), 1, perm_of(P, perm, s1, P_R2, sp1[c]), lin(1), V1 * Lb1, P3,
+                       two(bb, Lb1 * V1 * bb, 1), two(Lb1, bb, V1 * bb), ta * Lb * bb, V1 * Lb1, V * Rb1));
+    // R2'[a][l][x][e] = sum_{w,f} P3[a][l][x][w][f] B[e][w][f]
+    cta_gemm(make_gemm(P3, lin(V1 * bb), 1, B, lin(V1 * bb), 1, Rout, lin(ba), lin(1), ta * Lb * Lb1, ba, V1 * bb));
+  }
+  float* Lc = S.l2[0];
+  float* Ln = S.l2[1];
+  float* Q1 = S.scr[7];
+  float* Q2 = S.scr[8];
+  float* Q3 = S.scr[9];
+  float* W2 = S.scr[10];
+  if (threadIdx.x == 0) Lc[0] = 1.f;
+  __syncthreads();
+  double energy = 0.0;
+  for (int c = 0; c < C; ++c) {
+    const int s0 = site_id(P, r, c), s1 = site_id(P, r + 1, c);
+    const int U = P.sdim[4 * s0], V = P.sdim[4 * s0 + 1], Lb = P.sdim[4 * s0 + 2], Rb = P.sdim[4 * s0 + 3];
+    const int V1 = P.sdim[4 * s1 + 1], Lb1 = P.sdim[4 * s1 + 2], Rb1 = P.sdim[4 * s1 + 3];
+    const int ta = tbond[c], tb = tbond[c + 1], ba = bbond[c], bb = bbond[c + 1];
+    const float* T = top + (size_t)c * P.TS;
+    const float* B = bot + (size_t)c * P.TS;
+    // Q1[x][e][b][l][u] = sum_a L2[a][(l,x,e)] T[a][(u,b)]
+    cta_gemm(make_gemm(Lc, lin(1), Lb * Lb1 * ba, T, lin(1), U * tb, Q1, two(Lb1 * ba, U, tb * Lb * U),
+                       two(tb, 1, Lb * U), Lb * Lb1 * ba, U * tb, ta));
+    const bool vt = P.vert_mask[r * C + c];
+    const int q2n = Lb1 * ba * tb * Rb * V;  // elements of one Q2
+    // Q2[p][e][b][rr][x][v] = sum_{l,u} Q1[x][e][b][l][u] A[p](u,v,l,rr)
+    for (int p = 0; p < P.d; ++p) {
+      if (!vt && p != sp0[c]) continue;
+      float* Q2p = (p == sp0[c]) ? Q2 : S.scr[11 + p];
+      cta_gemm(make_gemm(Q1, lin(Lb * U), 1, perm_of(P, perm, s0, P_LENV, p), lin(1), Rb * V, Q2p,
+                         two(ba * tb, V, Rb * Lb1 * V), two(V, Lb1 * V, 1), Lb1 * ba * tb, Rb * V, Lb * U));
+    }
+    if (vt) {
+      const float* Rc = S.r2 + (size_t)c * P.E2S;
+      // W2[e][b][rr][w][y] = sum_f B[e][w][f] R2[b][rr][y][f]
+      cta_gemm(make_gemm(B, lin(bb), 1, Rc, lin(bb), 1, W2, two(V1, tb * Rb * V1 * Rb1, Rb1),
+                         three(Rb, Rb1, Rb * V1 * Rb1, V1 * Rb1, 1), ba * V1, tb * Rb * Rb1, bb));
+      const float* op = P.vert + (size_t)(r * C + c) * P.d * P.d * P.d * P.d;
+      const int col = sp0[c] * P.d + sp1[c];
+      for (int q = 0; q < P.d; ++q) {
+        float* Vq = S.scr[11 + kMaxD + q];
+        // Vq[e][b][rr][x][v] = sum_{w,y} A'[q][x][v][w][y] W2[e][b][rr][w][y]
+        cta_gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, q), lin(V1 * Rb1), 1, W2, lin(V1 * Rb1), 1, Vq, lin(1),
+                           lin(Lb1 * V), Lb1 * V, ba * tb * Rb, V1 * Rb1));
+        for (int p = 0; p < P.d; ++p) {
+          const float* Q2p = (p == sp0[c]) ? Q2 : S.scr[11 + p];
+          const double psi = cta_dot(Q2p, Vq, q2n, sh.red);
+          energy += (double)op[(size_t)(p * P.d + q) * P.d * P.d + col] * psi * vscale;
+        }
+      }
+    }
+    if (c < C - 1) {
+      // Q3[b][rr][y][e][w] = sum_{x,v} Q2[e][b][rr][x][v] A'(v,w,x,y)
+      cta_gemm(make_gemm(Q2, lin(Lb1 * V), 1, perm_of(P, perm, s1, P_ZIPT, sp1[c]), lin(1), V1 * Rb1, Q3,
+                         two(tb * Rb, V1, Rb1 * ba * V1), two(Rb1, 1, ba * V1), ba * tb * Rb, V1 * Rb1, Lb1 * V));
+      // L2'[b][rr][y][f] = sum_{e,w} Q3 B[e][w][f]
+      cta_gemm(make_gemm(Q3, lin(ba * V1), 1, B, lin(1), bb, Ln, lin(bb), lin(1), tb * Rb * Rb1, bb, ba * V1));
+      float* t = Lc;
+      Lc = Ln;
+      Ln = t;
+    }
+  }
+  return energy;
+}
+
+__device__ inline const int* tbonds(const DevPlan& P, int r) { return P.tb + (size_t)r * (P.C + 1); }
+__device__ inline const int* bbonds(const DevPlan& P, int r) { return P.bb + (size_t)r * (P.C + 1); }
+
+__device__ inline float* cache_row(const DevPlan& P, float* cache, int chain, int r) {
+  return cache + (size_t)chain * P.cache_floats_per_chain + (size_t)r * P.C * P.TS;
+}
+__device__ inline double* cache_logs(const DevPlan& P, float* cache, int n_chains, int chain) {
+  double* base = reinterpret_cast<double*>(cache + (size_t)n_chains * P.cache_floats_per_chain);
+  return base + (size_t)chain * P.R;
+}
+
+// ---------------------------------------------------------------------------
+// The fused kernel.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) peps_kernel(
+    const DevPlan* __restrict__ Pp, int mode, const float* __restrict__ tensors, const float* __restrict__ perm,
+    int32_t* configs, const double* __restrict__ uniforms, const int32_t* __restrict__ deltas, int n_chains,
+    float* cache, int full_gradient, float* out_O, int8_t* out_p, double* out_E, double* logamp_io,
+    double* sign_io, float* out_margin, float* ws, int32_t* status) {
+  const DevPlan& P = *Pp;
+  VMC_SHARED Shared sh;
+  const Slot S = make_slot(P, ws + P.perm_floats + (size_t)blockIdx.x * P.slot_floats);
+  const int R = P.R, C = P.C;
+  const int n_params = full_gradient ? P.d * P.np_sliced : P.np_sliced;
+
+  for (int chain = blockIdx.x; chain < n_chains; chain += gridDim.x) {
+    int32_t* cfg = configs + (size_t)chain * P.n_sites;
+
+    if (mode == MODE_INIT) {
+      // init_cache (kernels.py:115-129): bottom envs from the bottom up
+      double* lb = cache_logs(P, cache, n_chains, chain);
+      float* b = cache_row(P, cache, chain, R - 1);
+      fill_ones_row(P, b);
+      if (threadIdx.x == 0) lb[R - 1] = 0.0;
+      for (int r = R - 1; r >= 1; --r) {
+        for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
+        __syncthreads();
+        const double ls = apply_row(P, S, sh, perm, cache_row(P, cache, chain, r), bbonds(P, r),
+                                    cache_row(P, cache, chain, r - 1), bbonds(P, r - 1), r, sh.spins[0], true);
+        if (threadIdx.x == 0) lb[r - 1] = lb[r] + ls;
+        __syncthreads();
+      }
+      continue;
+    }
+
+    // ---------------- top-down pass: transition or forward ----------------
+    float min_margin = INFINITY;
+    fill_ones_row(P, S.topc);
+    if (threadIdx.x == 0) S.lt[0] = 0.0;
+    __syncthreads();
+    for (int r = 0; r < R; ++r) {
+      for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
+      __syncthreads();
+      float* top = S.topc + (size_t)r * C * P.TS;
+      if (mode == MODE_SWEEP) {
+        const float* bot = cache_row(P, cache, chain, r);
+        metropolis_row(P, S, sh, perm, top, tbonds(P, r), bot, bbonds(P, r), r, sh.spins[0],
+                       uniforms + (size_t)chain * P.n_sites, deltas ? deltas + (size_t)chain * P.n_sites : nullptr,
+                       &min_margin);
+        for (int c = threadIdx.x; c < C; c += blockDim.x) cfg[r * C + c] = sh.spins[0][c];
+        __syncthreads();
+      }
+      const double ls = apply_row(P, S, sh, perm, top, tbonds(P, r), S.topc + (size_t)(r + 1) * C * P.TS,
+                                  tbonds(P, r + 1), r, sh.spins[0], false);
+      if (threadIdx.x == 0) S.lt[r + 1] = S.lt[r] + ls;
+      __syncthreads();
+    }
+    double sgn = 1.0;
+    double logamp = S.lt[R] + contract_bottom(P, S.topc + (size_t)R * C * P.TS, tbonds(P, R), sh,
+                                             reinterpret_cast<double*>(S.scr[0]), &sgn);
+    if (mode == MODE_ENERGY) {
+      logamp = logamp_io[chain];
+      sgn = sign_io[chain];
+    } else if (threadIdx.x == 0) {
+      logamp_io[chain] = logamp;
+      sign_io[chain] = sgn;
+      if (out_margin && mode == MODE_SWEEP) out_margin[chain] = min_margin;
+    }
+    if (!isfinite(logamp) && threadIdx.x == 0) atomicOr(status, VMC_DEV_NONFINITE);
+
+    // ---------------- bottom-up estimate ----------------
+    const bool want_grad = (mode == MODE_SWEEP || mode == MODE_AMPGRAD);
+    const bool want_energy = (mode == MODE_SWEEP || mode == MODE_ENERGY);
+    float* Orow = out_O ? out_O + (size_t)chain * n_params : nullptr;
+    if (Orow && full_gradient) {
+      for (int i = threadIdx.x; i < n_params; i += blockDim.x) Orow[i] = 0.f;
+      __syncthreads();
+    }
+    double energy = 0.0;
+    if (want_energy) {
+      // diagonal terms (energy.py:150-156)
+      if (threadIdx.x == 0) {
+        for (int t = 0; t < P.n_diag; ++t) {
+          int idx = 0;
+          for (int k = 0; k < P.diag_nsites[t]; ++k) idx = idx * P.d + cfg[P.diag_sites[P.diag_site_off[t] + k]];
+          energy += P.diag_values[P.diag_value_off[t] + idx];
+        }
+      }
+    }
+    double* lbc = (mode == MODE_SWEEP) ? cache_logs(P, cache, n_chains, chain) : nullptr;
+    double lb_cur = 0.0, lb_prev = 0.0;
+    int ib_cur = 0, ib_prev = 1, ib_next = 2;
+    fill_ones_row(P, S.brow[ib_cur]);
+    for (int r = R - 1; r >= 0; --r) {
+      for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        sh.spins[0][c] = cfg[r * C + c];
+        if (r + 1 < R) sh.spins[1][c] = cfg[(r + 1) * C + c];
+      }
+      __syncthreads();
+      float* bcur = S.brow[ib_cur];
+      if (mode == MODE_SWEEP) {
+        cta_copy(cache_row(P, cache, chain, r), bcur, C * P.TS);
+        if (threadIdx.x == 0) lbc[r] = lb_cur;
+      }
+      const float* top = S.topc + (size_t)r * C * P.TS;
+      const double oscale = sgn * exp(S.lt[r] + lb_cur - logamp);
+      energy += estimate_row(P, S, sh, perm, tensors, top, tbonds(P, r), bcur, bbonds(P, r), r, sh.spins[0], oscale,
+                             Orow, full_gradient, want_grad, want_energy);
+      if (want_energy && r < R - 1 && P.row_has_v[r]) {
+        const double vscale = sgn * exp(S.lt[r] + lb_prev - logamp);
+        energy += vertical_energy(P, S, sh, perm, top, tbonds(P, r), S.brow[ib_prev], bbonds(P, r + 1), r,
+                                  sh.spins[0], sh.spins[1], vscale);
+      }
+      if (r > 0) {
+        const double ls = apply_row(P, S, sh, perm, bcur, bbonds(P, r), S.brow[ib_next], bbonds(P, r - 1), r,
+                                    sh.spins[0], true);
+        lb_prev = lb_cur;
+        lb_cur = lb_cur + ls;
+        const int t = ib_prev;
+        ib_prev = ib_cur;
+        ib_cur = ib_next;
+        ib_next = t;
+      }
+    }
+    if (want_energy && threadIdx.x == 0) {
+      out_E[chain] = energy;
+      if (!isfinite(energy)) atomicOr(status, VMC_DEV_NONFINITE);
+    }
+    if (out_p && mode == MODE_SWEEP) {
+      // active_slice_indices = repeat(config, params_per_site) (kernels.py:82-87)
+      for (int s = 0; s < P.n_sites; ++s) {
+        const int sz = ssize(P, s);
+        const int8_t v = (int8_t)cfg[s];
+        for (int i = threadIdx.x; i < sz; i += blockDim.x) out_p[(size_t)chain * P.np_sliced + P.site_osl[s] + i] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// Host side: plan construction.
+// ===========================================================================
+struct HostOp {
+  std::vector<float> onesite, horiz, vert;
+  std::vector<int> onesite_mask, horiz_mask, vert_mask, row_has_h, row_has_v;
+  std::vector<int> diag_nsites, diag_site_off, diag_sites, diag_value_off;
+  std::vector<double> diag_values;
+};
+
+}  // namespace vmc
+
+struct vmc_plan {
+  vmc::DevPlan hp;          // host copy with device pointers
+  vmc::DevPlan* dplan = nullptr;  // device copy
+  void* dbuf = nullptr;     // device arrays
+  std::vector<int> sdim, site_off, site_osl, perm_off, tb, bb;
+  vmc::HostOp op;
+  bool op_set = false;
+  int slots_max = 0;
+};
+
+namespace vmc {
+
+// Bond dimensions produced by applying one row MPO to a boundary MPS
+// (strategy.py:118-150; dims depend on shapes only).
+static std::vector<int> apply_bonds(const std::vector<int>& bin, const std::vector<int>& wb, int pout, int chi,
+                                    int strategy) {
+  const int C = (int)bin.size() - 1;
+  std::vector<int> out(C + 1, 1);
+  if (strategy == VMC_STRATEGY_NO_TRUNCATION) {
+    for (int i = 0; i <= C; ++i) out[i] = bin[i] * wb[i];
+    return out;
+  }
+  int left = bin[0] * wb[0];
+  out[0] = left;
+  for (int i = 0; i < C - 1; ++i) {
+    const int m = left * pout, n = bin[i + 1] * wb[i + 1];
+    const int k = std::min(chi, std::min(m, n));
+    out[i + 1] = k;
+    left = k;
+  }
+  out[C] = bin[C] * wb[C];
+  return out;
+}
+
+static vmc_status upload_plan(vmc_plan* pl) {
+  DevPlan& P = pl->hp;
+  HostOp& op = pl->op;
+  // gather all arrays into one device buffer
+  std::vector<char> blob;
+  auto push = [&](const void* data, size_t bytes) -> size_t {
+    size_t off = (blob.size() + 15) & ~size_t(15);
+    blob.resize(off + bytes);
+    if (data && bytes) std::memcpy(blob.data() + off, data, bytes);
+    return off;
+  };
+  const size_t o_sdim = push(pl->sdim.data(), pl->sdim.size() * 4);
+  const size_t o_soff = push(pl->site_off.data(), pl->site_off.size() * 4);
+  const size_t o_sosl = push(pl->site_osl.data(), pl->site_osl.size() * 4);
+  const size_t o_poff = push(pl->perm_off.data(), pl->perm_off.size() * 4);
+  const size_t o_tb = push(pl->tb.data(), pl->tb.size() * 4);
+  const size_t o_bb = push(pl->bb.data(), pl->bb.size() * 4);
+  const size_t o_os = push(op.onesite.data(), op.onesite.size() * 4);
+  const size_t o_osm = push(op.onesite_mask.data(), op.onesite_mask.size() * 4);
+  const size_t o_hz = push(op.horiz.data(), op.horiz.size() * 4);
+  const size_t o_hzm = push(op.horiz_mask.data(), op.horiz_mask.size() * 4);
+  const size_t o_vt = push(op.vert.data(), op.vert.size() * 4);
+  const size_t o_vtm = push(op.vert_mask.data(), op.vert_mask.size() * 4);
+  const size_t o_rh = push(op.row_has_h.data(), op.row_has_h.size() * 4);
+  const size_t o_rv = push(op.row_has_v.data(), op.row_has_v.size() * 4);
+  const size_t o_dn = push(op.diag_nsites.data(), op.diag_nsites.size() * 4);
+  const size_t o_dso = push(op.diag_site_off.data(), op.diag_site_off.size() * 4);
+  const size_t o_ds = push(op.diag_sites.data(), op.diag_sites.size() * 4);
+  const size_t o_dvo = push(op.diag_value_off.data(), op.diag_value_off.size() * 4);
+  const size_t o_dv = push(op.diag_values.data(), op.diag_values.size() * 8);
+  const size_t o_plan = push(nullptr, sizeof(DevPlan));
+  if (pl->dbuf) vmc_free(pl->dbuf);
+  pl->dbuf = nullptr;
+  if (vmc_alloc(&pl->dbuf, blob.size()) != cudaSuccess) return VMC_ERR_CUDA;
+  char* base = static_cast<char*>(pl->dbuf);
+  P.sdim = reinterpret_cast<const int*>(base + o_sdim);
+  P.site_off = reinterpret_cast<const int*>(base + o_soff);
+  P.site_osl = reinterpret_cast<const int*>(base + o_sosl);
+  P.perm_off = reinterpret_cast<const int*>(base + o_poff);
+  P.tb = reinterpret_cast<const int*>(base + o_tb);
+  P.bb = reinterpret_cast<const int*>(base + o_bb);
+  P.onesite = reinterpret_cast<const float*>(base + o_os);
+  P.onesite_mask = reinterpret_cast<const int*>(base + o_osm);
+  P.horiz = reinterpret_cast<const float*>(base + o_hz);
+  P.horiz_mask = reinterpret_cast<const int*>(base + o_hzm);
+  P.vert = reinterpret_cast<const float*>(base + o_vt);
+  P.vert_mask = reinterpret_cast<const int*>(base + o_vtm);
+  P.row_has_h = reinterpret_cast<const int*>(base + o_rh);
+  P.row_has_v = reinterpret_cast<const int*>(base + o_rv);
+  P.diag_nsites = reinterpret_cast<const int*>(base + o_dn);
+  P.diag_site_off = reinterpret_cast<const int*>(base + o_dso);
+  P.diag_sites = reinterpret_cast<const int*>(base + o_ds);
+  P.diag_value_off = reinterpret_cast<const int*>(base + o_dvo);
+  P.diag_values = reinterpret_cast<const double*>(base + o_dv);
+  std::memcpy(blob.data() + o_plan, &P, sizeof(DevPlan));
+  pl->dplan = reinterpret_cast<DevPlan*>(base + o_plan);
+  if (vmc_h2d(pl->dbuf, blob.data(), blob.size(), nullptr) != cudaSuccess) return VMC_ERR_CUDA;
+  if (vmc_sync(nullptr) != cudaSuccess) return VMC_ERR_CUDA;
+  return VMC_OK;
+}
+
+static void default_operator(vmc_plan* pl) {
+  DevPlan& P = pl->hp;
+  HostOp& op = pl->op;
+  const int d2 = P.d * P.d;
+  op.onesite.assign((size_t)P.n_sites * P.d * P.d, 0.f);
+  op.onesite_mask.assign(P.n_sites, 0);
+  op.horiz.assign((size_t)std::max(P.R * (P.C - 1), 1) * d2 * d2, 0.f);
+  op.horiz_mask.assign(std::max(P.R * (P.C - 1), 1), 0);
+  op.vert.assign((size_t)std::max((P.R - 1) * P.C, 1) * d2 * d2, 0.f);
+  op.vert_mask.assign(std::max((P.R - 1) * P.C, 1), 0);
+  op.row_has_h.assign(P.R, 0);
+  op.row_has_v.assign(P.R, 0);
+  op.diag_nsites.assign(1, 0);
+  op.diag_site_off.assign(1, 0);
+  op.diag_sites.assign(1, 0);
+  op.diag_value_off.assign(1, 0);
+  op.diag_values.assign(1, 0.0);
+  P.n_diag = 0;
+}
+
+}  // namespace vmc
+
+using namespace vmc;
+
+extern "C" {
+
+const char* vmc_version(void) { return "vmc_gb300 0.1 (sm_103a)"; }
+
+const char* vmc_status_string(vmc_status s) {
+  switch (s) {
+    case VMC_OK: return "ok";
+    case VMC_ERR_INVALID: return "invalid argument";
+    case VMC_ERR_UNSUPPORTED: return "unsupported configuration";
+    case VMC_ERR_WORKSPACE: return "workspace too small";
+    case VMC_ERR_CUDA: return "CUDA runtime error";
+    case VMC_ERR_NONFINITE: return "non-finite result";
+    case VMC_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+  }
+}
+
+vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype, int strategy,
+                         int n_sweeps, vmc_plan** out_plan) {
+  if (!shape || !out_plan) return VMC_ERR_INVALID;
+  *out_plan = nullptr;
+  const int R = shape->n_rows, C = shape->n_cols;
+  if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
+  if (phys_dim > kMaxD) return VMC_ERR_UNSUPPORTED;
+  if (dtype != VMC_DTYPE_F32) return VMC_ERR_UNSUPPORTED;
+  if (strategy == VMC_STRATEGY_VARIATIONAL) return VMC_ERR_UNSUPPORTED;
+  if (strategy < 0 || strategy > VMC_STRATEGY_VARIATIONAL) return VMC_ERR_INVALID;
+  vmc_plan* pl = new (std::nothrow) vmc_plan();
+  if (!pl) return VMC_ERR_INVALID;
+  DevPlan& P = pl->hp;
+  std::memset(&P, 0, sizeof(P));
+  P.R = R; P.C = C; P.D = bond_dim; P.d = phys_dim; P.chi = chi; P.strategy = strategy;
+  P.n_sweeps = n_sweeps; P.n_sites = R * C;
+  const int D = bond_dim, d = phys_dim;
+  pl->sdim.resize(4 * R * C);
+  pl->site_off.resize(R * C);
+  pl->site_osl.resize(R * C);
+  pl->perm_off.resize(R * C);
+  long long off = 0, osl = 0, poff = 0;
+  for (int r = 0; r < R; ++r)
+    for (int c = 0; c < C; ++c) {
+      const int s = r * C + c;
+      const int u = r == 0 ? 1 : D, v = r == R - 1 ? 1 : D, l = c == 0 ? 1 : D, rr = c == C - 1 ? 1 : D;
+      pl->sdim[4 * s] = u; pl->sdim[4 * s + 1] = v; pl->sdim[4 * s + 2] = l; pl->sdim[4 * s + 3] = rr;
+      const int sz = u * v * l * rr;
+      pl->site_off[s] = (int)off;
+      pl->site_osl[s] = (int)osl;
+      pl->perm_off[s] = (int)poff;
+      off += (long long)d * sz;
+      osl += sz;
+      poff += (long long)kPermKinds * d * sz;
+    }
+  P.np_sliced = (int)osl;
+  P.perm_floats = (poff + 63) & ~63LL;
+  // bond dims
+  pl->tb.assign((size_t)(R + 1) * (C + 1), 1);
+  pl->bb.assign((size_t)R * (C + 1), 1);
+  std::vector<int> wb(C + 1, 1);
+  for (int i = 1; i < C; ++i) wb[i] = D;
+  {
+    std::vector<int> cur(C + 1, 1);
+    for (int r = 0; r < R; ++r) {
+      for (int i = 0; i <= C; ++i) pl->tb[(size_t)r * (C + 1) + i] = cur[i];
+      const int pout = r == R - 1 ? 1 : D;
+      cur = apply_bonds(cur, wb, pout, chi, strategy);
+    }
+    for (int i = 0; i <= C; ++i) pl->tb[(size_t)R * (C + 1) + i] = cur[i];
+  }
+  {
+    std::vector<int> cur(C + 1, 1);
+    for (int r = R - 1; r >= 0; --r) {
+      for (int i = 0; i <= C; ++i) pl->bb[(size_t)r * (C + 1) + i] = cur[i];
+      const int pout = r == 0 ? 1 : D;
+      cur = apply_bonds(cur, wb, pout, chi, strategy);
+    }
+  }
+  // buffer sizes
+  long long TS = 1, ES = 1, E2S = 1, chimax = 1, MM = 1;
+  auto phys_top = [&](int r) { return r == 0 ? 1 : D; };   // phys of top env row r = up leg of row r
+  auto phys_bot = [&](int r) { return r == R - 1 ? 1 : D; };
+  for (int r = 0; r <= R; ++r)
+    for (int c = 0; c < C; ++c) {
+      const long long a = pl->tb[(size_t)r * (C + 1) + c], b = pl->tb[(size_t)r * (C + 1) + c + 1];
+      const int ph = r < R ? phys_top(r) : 1;
+      TS = std::max(TS, a * ph * b);
+      chimax = std::max(chimax, std::max(a, b));
+    }
+  for (int r = 0; r < R; ++r)
+    for (int c = 0; c < C; ++c) {
+      const long long a = pl->bb[(size_t)r * (C + 1) + c], b = pl->bb[(size_t)r * (C + 1) + c + 1];
+      TS = std::max(TS, a * phys_bot(r) * b);
+      chimax = std::max(chimax, std::max(a, b));
+    }
+  for (int r = 0; r < R; ++r)
+    for (int c = 0; c <= C; ++c) {
+      const long long t = pl->tb[(size_t)r * (C + 1) + c], b = pl->bb[(size_t)r * (C + 1) + c];
+      ES = std::max(ES, t * D * b);
+      if (r + 1 < R) E2S = std::max(E2S, t * D * D * (long long)pl->bb[(size_t)(r + 1) * (C + 1) + c]);
+    }
+  // truncation matrices: rows kc*pout <= chimax*D, cols <= chimax*D
+  MM = (chimax * D + 1) * (chimax * D + 1);
+  const long long SCR = std::max({chimax * chimax * D * D * D, TS * D * D, MM, 4LL * kMaxVec});
+  P.TS = (int)TS; P.ES = (int)ES; P.E2S = (int)E2S; P.MM = (int)MM; P.SCR = (int)SCR;
+  P.n_scr = 11 + 2 * kMaxD;
+  P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + 3 * al64((long long)C * TS) +
+                  al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
+                  2 * al64(E2S) + 3 * al64(MM) + (long long)P.n_scr * al64(SCR);
+  P.cache_floats_per_chain = al64((long long)R * C * TS);
+  if (chimax * D > kMaxVec) {
+    delete pl;
+    return VMC_ERR_UNSUPPORTED;
+  }
+  default_operator(pl);
+  vmc_status st = upload_plan(pl);
+  if (st != VMC_OK) {
+    vmc_plan_destroy(pl);
+    return st;
+  }
+  pl->slots_max = vmc_num_sms() * 4;
+  *out_plan = pl;
+  return VMC_OK;
+}
+
+vmc_status vmc_peps_plan_set_operator(vmc_plan* pl, const double* onesite, const int* onesite_mask,
+                                      const double* horiz, const int* horiz_mask, const double* vert,
+                                      const int* vert_mask, int n_diag, const int* diag_nsites,
+                                      const int* diag_site_off, const int* diag_sites, const int* diag_value_off,
+                                      const double* diag_values) {
+  if (!pl) return VMC_ERR_INVALID;
+  DevPlan& P = pl->hp;
+  HostOp& op = pl->op;
+  default_operator(pl);
+  const int d = P.d, d2 = d * d, R = P.R, C = P.C;
+  if (onesite && onesite_mask) {
+    for (int s = 0; s < P.n_sites; ++s) {
+      op.onesite_mask[s] = onesite_mask[s] != 0;
+      for (int i = 0; i < d * d; ++i) op.onesite[(size_t)s * d * d + i] = (float)onesite[(size_t)s * d * d + i];
+    }
+  }
+  if (horiz && horiz_mask && C > 1) {
+    for (int t = 0; t < R * (C - 1); ++t) {
+      op.horiz_mask[t] = horiz_mask[t] != 0;
+      if (op.horiz_mask[t]) op.row_has_h[t / (C - 1)] = 1;
+      for (int i = 0; i < d2 * d2; ++i) op.horiz[(size_t)t * d2 * d2 + i] = (float)horiz[(size_t)t * d2 * d2 + i];
+    }
+  }
+  if (vert && vert_mask && R > 1) {
+    for (int t = 0; t < (R - 1) * C; ++t) {
+      op.vert_mask[t] = vert_mask[t] != 0;
+      if (op.vert_mask[t]) op.row_has_v[t / C] = 1;
+      for (int i = 0; i < d2 * d2; ++i) op.vert[(size_t)t * d2 * d2 + i] = (float)vert[(size_t)t * d2 * d2 + i];
+    }
+  }
+  if (n_diag > 0) {
+    if (!diag_nsites || !diag_site_off || !diag_sites || !diag_value_off || !diag_values) return VMC_ERR_INVALID;
+    op.diag_nsites.assign(diag_nsites, diag_nsites + n_diag);
+    op.diag_site_off.assign(diag_site_off, diag_site_off + n_diag);
+    op.diag_value_off.assign(diag_value_off, diag_value_off + n_diag);
+    int n_sites_total = 0, n_values = 0;
+    for (int t = 0; t < n_diag; ++t) {
+      if (diag_nsites[t] < 1) return VMC_ERR_INVALID;
+      n_sites_total = std::max(n_sites_total, diag_site_off[t] + diag_nsites[t]);
+      int nv = 1;
+      for (int k = 0; k < diag_nsites[t]; ++k) nv *= d;
+      n_values = std::max(n_values, diag_value_off[t] + nv);
+    }
+    op.diag_sites.assign(diag_sites, diag_sites + n_sites_total);
+    for (int v : op.diag_sites)
+      if (v < 0 || v >= P.n_sites) return VMC_ERR_INVALID;
+    op.diag_values.assign(diag_values, diag_values + n_values);
+  }
+  P.n_diag = n_diag;
+  pl->op_set = true;
+  return upload_plan(pl);
+}
+
+void vmc_plan_destroy(vmc_plan* pl) {
+  if (!pl) return;
+  if (pl->dbuf) vmc_free(pl->dbuf);
+  delete pl;
+}
+
+int64_t vmc_peps_n_params_sliced(const vmc_plan* pl) { return pl ? pl->hp.np_sliced : 0; }
+int64_t vmc_peps_n_params_full(const vmc_plan* pl) { return pl ? (int64_t)pl->hp.np_sliced * pl->hp.d : 0; }
+
+size_t vmc_cache_size(const vmc_plan* pl, int n_chains) {
+  if (!pl || n_chains < 0) return 0;
+  return (size_t)n_chains * (pl->hp.cache_floats_per_chain * 4 + (size_t)pl->hp.R * 8);
+}
+
+static int n_slots(const vmc_plan* pl, int n_chains) { return std::max(1, std::min(n_chains, pl->slots_max)); }
+
+size_t vmc_workspace_size(const vmc_plan* pl, int n_chains) {
+  if (!pl || n_chains < 0) return 0;
+  return ((size_t)pl->hp.perm_floats + (size_t)n_slots(pl, n_chains) * pl->hp.slot_floats) * 4;
+}
+
+static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float* tensors, int32_t* configs,
+                         const double* uniforms, const int32_t* deltas, int n, void* cache, int full_gradient,
+                         float* out_O, int8_t* out_p, double* out_E, double* logamp, double* sign, float* margin,
+                         void* ws, size_t ws_bytes, int32_t* status) {
+  if (!pl || !tensors || !configs || n < 0 || !ws || !status) return VMC_ERR_INVALID;
+  if (n == 0) return VMC_OK;
+  if (ws_bytes < vmc_workspace_size(pl, n)) return VMC_ERR_WORKSPACE;
+  const int grid = n_slots(pl, n);
+  float* wsf = static_cast<float*>(ws);
+  VMC_LAUNCH(permute_tensors_kernel, std::min(pl->hp.n_sites, 1024), kThreads, 0, stream, pl->dplan, tensors, wsf);
+  VMC_LAUNCH(peps_kernel, grid, kThreads, 0, stream, pl->dplan, mode, tensors, wsf, configs, uniforms, deltas, n,
+             static_cast<float*>(cache), full_gradient, out_O, out_p, out_E, logamp, sign, margin, wsf, status);
+  return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
+}
+
+vmc_status vmc_peps_init_cache(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* configs,
+                               int n_chains, void* cache, void* workspace, size_t workspace_bytes,
+                               int32_t* status_dev) {
+  if (!cache) return VMC_ERR_INVALID;
+  return launch(pl, stream, MODE_INIT, tensors, const_cast<int32_t*>(configs), nullptr, nullptr, n_chains, cache, 0,
+                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, workspace, workspace_bytes, status_dev);
+}
+
+vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors, int32_t* configs_inout,
+                          const double* uniforms, const int32_t* deltas, int n_chains, void* cache_inout,
+                          int full_gradient, float* out_O, int8_t* out_p, double* out_E, double* out_logamp,
+                          double* out_sign, float* out_margin, void* workspace, size_t workspace_bytes,
+                          int32_t* status_dev) {
+  if (!pl || !uniforms || !cache_inout || !out_E || !out_logamp || !out_sign) return VMC_ERR_INVALID;
+  if (pl->hp.d > 2 && !deltas) return VMC_ERR_INVALID;
+  return launch(pl, stream, MODE_SWEEP, tensors, configs_inout, uniforms, deltas, n_chains, cache_inout,
+                full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, workspace, workspace_bytes,
+                status_dev);
+}
+
+vmc_status vmc_peps_amp_grad(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples, int n,
+                             int full_gradient, float* out_O, double* out_logamp, double* out_sign, void* workspace,
+                             size_t workspace_bytes, int32_t* status_dev) {
+  if (!pl || !out_logamp || !out_sign) return VMC_ERR_INVALID;
+  return launch(pl, stream, MODE_AMPGRAD, tensors, const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr,
+                full_gradient, out_O, nullptr, nullptr, out_logamp, out_sign, nullptr, workspace, workspace_bytes,
+                status_dev);
+}
+
+vmc_status vmc_peps_local_energy(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples,
+                                 int n, const double* logamp, const double* sign, double* out_E, void* workspace,
+                                 size_t workspace_bytes, int32_t* status_dev) {
+  if (!pl || !logamp || !sign || !out_E) return VMC_ERR_INVALID;
+  return launch(pl, stream, MODE_ENERGY, tensors, const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr, 0,
+                nullptr, nullptr, out_E, const_cast<double*>(logamp), const_cast<double*>(sign), nullptr, workspace,
+                workspace_bytes, status_dev);
+}
+
+}  // extern "C"

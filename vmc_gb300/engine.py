@@ -1,0 +1,230 @@
+"""Python handle on the C-ABI engine: plan, workspace, cache and calls.
+
+``PEPSEngine`` owns one ``vmc_plan`` and a device workspace; every call is
+issued on torch's current CUDA stream and takes/returns torch tensors that
+live on that device.  Nothing here computes on the CPU: if the CUDA library
+or the GPU is missing, construction raises ``EngineUnavailable``.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _abi
+from ._lib import EngineUnavailable
+from .lowering import lower_operator
+
+__all__ = ["PEPSEngine", "SweepResult", "STRATEGY_IDS"]
+
+STRATEGY_IDS = {
+    "NoTruncation": _abi.VMC_STRATEGY_NO_TRUNCATION,
+    "ZipUp": _abi.VMC_STRATEGY_ZIP_UP,
+    "DensityMatrix": _abi.VMC_STRATEGY_DENSITY_MATRIX,
+    "Variational": _abi.VMC_STRATEGY_VARIATIONAL,
+}
+
+
+def _vp(t):
+    if t is None:
+        return None
+    return ct.c_void_p(t.data_ptr())
+
+
+def _np_vp(a):
+    return a.ctypes.data_as(ct.c_void_p) if a is not None else None
+
+
+@dataclass
+class SweepResult:
+    configs: torch.Tensor        # (n, n_sites) int32, updated in place
+    O: torch.Tensor | None       # (n, n_params) float32
+    p: torch.Tensor | None       # (n, n_params_sliced) int8
+    E: torch.Tensor              # (n,) float64
+    logamp: torch.Tensor         # (n,) float64
+    sign: torch.Tensor           # (n,) float64
+    margin: torch.Tensor | None  # (n,) float32
+
+
+class PEPSEngine:
+    """Plan + workspace for one (shape, D, chi, d, strategy, operator)."""
+
+    def __init__(self, shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, operator=None,
+                 device=None, lib=None):
+        self.shape = (int(shape[0]), int(shape[1]))
+        self.bond_dim, self.chi, self.phys_dim = int(bond_dim), int(chi), int(phys_dim)
+        self.strategy = strategy
+        self.n_sites = self.shape[0] * self.shape[1]
+        if lib is None:
+            if not torch.cuda.is_available():
+                raise EngineUnavailable("vmc_gb300 needs a CUDA GPU; no CPU fallback exists")
+            from ._lib import lib as _load
+            lib = _load()
+            self.device = torch.device(device if device is not None else "cuda")
+            if self.device.type != "cuda":
+                raise EngineUnavailable("vmc_gb300 engine tensors must live on a CUDA device")
+        else:
+            self.device = torch.device(device if device is not None else "cpu")
+        self.lib = lib
+        plan = ct.c_void_p()
+        sid = STRATEGY_IDS[strategy] if isinstance(strategy, str) else int(strategy)
+        with torch.cuda.device(self.device) if self.device.type == "cuda" else _null():
+            st = lib.vmc_peps_plan(ct.byref(_abi.VmcShape(*self.shape)), self.bond_dim, self.chi,
+                                   self.phys_dim, _abi.VMC_DTYPE_F32, sid, int(n_sweeps), ct.byref(plan))
+        _abi.check(lib, st, "vmc_peps_plan")
+        self._plan = plan
+        self.n_params_sliced = int(lib.vmc_peps_n_params_sliced(plan))
+        self.n_params_full = int(lib.vmc_peps_n_params_full(plan))
+        self._ws = None
+        self._ws_n = -1
+        self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        if operator is not None:
+            self.set_operator(operator)
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None and plan.value:
+            try:
+                self.lib.vmc_plan_destroy(plan)
+            except Exception:
+                pass
+            self._plan = None
+
+    # ------------------------------------------------------------------ setup
+    def set_operator(self, operator):
+        lo = lower_operator(operator, self.shape, self.phys_dim)
+        st = self.lib.vmc_peps_plan_set_operator(
+            self._plan, _np_vp(lo.onesite), _np_vp(lo.onesite_mask), _np_vp(lo.horiz), _np_vp(lo.horiz_mask),
+            _np_vp(lo.vert), _np_vp(lo.vert_mask), lo.n_diag,
+            _np_vp(lo.diag_nsites) if lo.n_diag else None, _np_vp(lo.diag_site_off) if lo.n_diag else None,
+            _np_vp(lo.diag_sites) if lo.n_diag else None, _np_vp(lo.diag_value_off) if lo.n_diag else None,
+            _np_vp(lo.diag_values) if lo.n_diag else None)
+        _abi.check(self.lib, st, "vmc_peps_plan_set_operator")
+
+    def cache_bytes(self, n):
+        return int(self.lib.vmc_cache_size(self._plan, int(n)))
+
+    def workspace(self, n):
+        need = int(self.lib.vmc_workspace_size(self._plan, int(n)))
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def new_cache(self, n):
+        return torch.empty(self.cache_bytes(n), dtype=torch.uint8, device=self.device)
+
+    def _stream(self):
+        if self.device.type == "cuda":
+            return ct.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        return None
+
+    def _check_tensors(self, tensors):
+        if tensors.dtype != torch.float32 or tensors.device != self.device or not tensors.is_contiguous():
+            raise ValueError("packed tensors must be a contiguous float32 vector on the engine device")
+        if tensors.numel() != self.n_params_full:
+            raise ValueError(f"expected {self.n_params_full} packed parameters, got {tensors.numel()}")
+
+    def _configs(self, configs):
+        c = configs.reshape(-1, self.n_sites)
+        if c.dtype != torch.int32 or c.device != self.device or not c.is_contiguous():
+            raise ValueError("configs must be a contiguous int32 (n, n_sites) tensor on the engine device")
+        return c
+
+    def status(self, reset=True) -> int:
+        v = int(self._status.item())
+        if reset and v:
+            self._status.zero_()
+        return v
+
+    def raise_on_status(self):
+        v = self.status()
+        if v & _abi.VMC_DEV_NONFINITE:
+            raise FloatingPointError("engine reported a non-finite amplitude or energy")
+        if v & _abi.VMC_DEV_TIMEOUT:
+            raise TimeoutError("engine reported a device-side timeout")
+
+    # ------------------------------------------------------------------ calls
+    def init_cache(self, tensors, configs, cache=None):
+        self._check_tensors(tensors)
+        c = self._configs(configs)
+        n = c.shape[0]
+        if cache is None:
+            cache = self.new_cache(n)
+        ws = self.workspace(n)
+        st = self.lib.vmc_peps_init_cache(self._plan, self._stream(), _vp(tensors), _vp(c), n, _vp(cache),
+                                          _vp(ws), ws.numel(), _vp(self._status))
+        _abi.check(self.lib, st, "vmc_peps_init_cache")
+        return cache
+
+    def sweep(self, tensors, configs, uniforms, cache, deltas=None, full_gradient=False, want_O=True,
+              want_p=True, want_margin=True, out=None):
+        self._check_tensors(tensors)
+        c = self._configs(configs)
+        n = c.shape[0]
+        u = uniforms.reshape(n, self.n_sites)
+        if u.dtype != torch.float64 or u.device != self.device or not u.is_contiguous():
+            raise ValueError("uniforms must be a contiguous float64 (n, n_sites) tensor on the engine device")
+        if self.phys_dim > 2:
+            if deltas is None:
+                raise ValueError("d > 2 needs explicit flip offsets (deltas)")
+            deltas = deltas.reshape(n, self.n_sites).to(torch.int32).contiguous()
+        else:
+            deltas = None
+        np_ = self.n_params_full if full_gradient else self.n_params_sliced
+        dev = self.device
+        if out is None:
+            out = SweepResult(
+                configs=c,
+                O=torch.empty((n, np_), dtype=torch.float32, device=dev) if want_O else None,
+                p=torch.empty((n, self.n_params_sliced), dtype=torch.int8, device=dev) if want_p else None,
+                E=torch.empty(n, dtype=torch.float64, device=dev),
+                logamp=torch.empty(n, dtype=torch.float64, device=dev),
+                sign=torch.empty(n, dtype=torch.float64, device=dev),
+                margin=torch.empty(n, dtype=torch.float32, device=dev) if want_margin else None,
+            )
+        ws = self.workspace(n)
+        st = self.lib.vmc_peps_sweep(self._plan, self._stream(), _vp(tensors), _vp(c), _vp(u), _vp(deltas), n,
+                                     _vp(cache), int(bool(full_gradient)), _vp(out.O), _vp(out.p), _vp(out.E),
+                                     _vp(out.logamp), _vp(out.sign), _vp(out.margin), _vp(ws), ws.numel(),
+                                     _vp(self._status))
+        _abi.check(self.lib, st, "vmc_peps_sweep")
+        return out
+
+    def amp_grad(self, tensors, samples, full_gradient=False, want_O=True):
+        self._check_tensors(tensors)
+        c = self._configs(samples)
+        n = c.shape[0]
+        dev = self.device
+        np_ = self.n_params_full if full_gradient else self.n_params_sliced
+        O = torch.empty((n, np_), dtype=torch.float32, device=dev) if want_O else None
+        logamp = torch.empty(n, dtype=torch.float64, device=dev)
+        sign = torch.empty(n, dtype=torch.float64, device=dev)
+        ws = self.workspace(n)
+        st = self.lib.vmc_peps_amp_grad(self._plan, self._stream(), _vp(tensors), _vp(c), n,
+                                        int(bool(full_gradient)), _vp(O), _vp(logamp), _vp(sign), _vp(ws),
+                                        ws.numel(), _vp(self._status))
+        _abi.check(self.lib, st, "vmc_peps_amp_grad")
+        return logamp, sign, O
+
+    def local_energy(self, tensors, samples, logamp, sign):
+        self._check_tensors(tensors)
+        c = self._configs(samples)
+        n = c.shape[0]
+        E = torch.empty(n, dtype=torch.float64, device=self.device)
+        ws = self.workspace(n)
+        la = logamp.to(torch.float64).contiguous()
+        sg = sign.to(torch.float64).contiguous()
+        st = self.lib.vmc_peps_local_energy(self._plan, self._stream(), _vp(tensors), _vp(c), n, _vp(la),
+                                            _vp(sg), _vp(E), _vp(ws), ws.numel(), _vp(self._status))
+        _abi.check(self.lib, st, "vmc_peps_local_energy")
+        return E
+
+
+class _null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False

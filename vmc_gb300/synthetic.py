@@ -1,0 +1,83 @@
+"""Seeded synthetic PEPS workloads (no public dataset exists for this path).
+
+Tensors are i.i.d. N(0,1)/sqrt(d * D^4) drawn from NumPy ``PCG64(seed)``;
+initial configurations are uniform in {0..d-1} from ``PCG64(seed + 2)``;
+per-site Metropolis uniforms for sweep k come from ``PCG64(seed + 1)``
+(one (n_chains, n_sites) block per sweep, in sweep order).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .lowering import site_dims
+from .operators import heisenberg, transverse_field_ising
+
+__all__ = ["Workload", "random_tensors", "initial_configs", "uniform_stream", "WORKLOADS"]
+
+
+def random_tensors(shape, bond_dim, phys_dim=2, seed=0, dtype=np.float64):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n_rows, n_cols = shape
+    scale = 1.0 / np.sqrt(phys_dim * bond_dim ** 4)
+    out = []
+    for r in range(n_rows):
+        row = []
+        for c in range(n_cols):
+            dims = (phys_dim,) + site_dims(r, c, n_rows, n_cols, bond_dim)
+            row.append((rng.standard_normal(dims) * scale).astype(dtype))
+        out.append(row)
+    return out
+
+
+def initial_configs(n_chains, n_sites, phys_dim=2, seed=0):
+    rng = np.random.Generator(np.random.PCG64(seed + 2))
+    return rng.integers(0, phys_dim, size=(n_chains, n_sites)).astype(np.int32)
+
+
+def uniform_stream(n_chains, n_sites, seed=0):
+    """Generator of (n_chains, n_sites) float64 uniform blocks, one per sweep."""
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    while True:
+        yield rng.random((n_chains, n_sites))
+
+
+@dataclass(frozen=True)
+class Workload:
+    name: str
+    shape: tuple
+    bond_dim: int
+    chi: int
+    phys_dim: int
+    model: str       # "heisenberg" | "tfim"
+    n_chains: int
+    strategy: str = "ZipUp"
+
+    def operator(self):
+        if self.model == "heisenberg":
+            return heisenberg(self.shape)
+        return transverse_field_ising(self.shape, J=1.0, h=3.0)
+
+    def flops_per_sample(self):
+        """Algorithmic FLOP per sample counted with the reference's einsum orders (SVD/QR excluded)."""
+        return _ALGO_FLOPS.get((self.shape, self.bond_dim, self.chi, self.model))
+
+
+_ALGO_FLOPS = {
+    ((8, 8), 4, 16, "heisenberg"): 234.9e6,
+    ((8, 8), 4, 16, "tfim"): 69.0e6,
+    ((10, 10), 4, 16, "tfim"): 137.0e6,
+    ((6, 6), 4, 16, "heisenberg"): 71.2e6,
+    ((8, 8), 5, 25, "heisenberg"): 1.54e9,
+    ((12, 12), 6, 36, "heisenberg"): 27.1e9,
+    ((16, 16), 6, 48, "heisenberg"): 112.5e9,
+}
+
+WORKLOADS = {
+    # 4x4 TFIM, J=1 h=3, D=2, ZipUp(4), 256 samples (the CPU-runnable exact case)
+    "tfim4x4_D2_chi4": Workload("tfim4x4_D2_chi4", (4, 4), 2, 4, 2, "tfim", 256),
+    # 8x8 Heisenberg, D=4, chi=16, 4096 samples per sweep (headline)
+    "heis8x8_D4_chi16": Workload("heis8x8_D4_chi16", (8, 8), 4, 16, 2, "heisenberg", 4096),
+    "heis6x6_D4_chi16": Workload("heis6x6_D4_chi16", (6, 6), 4, 16, 2, "heisenberg", 4096),
+}
