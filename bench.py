@@ -31,6 +31,12 @@ METRIC = "PEPS samples/s (amp+grad log psi+E_loc), D=4 chi=16"
 UNIT = "samples/s"
 
 
+def _worker_init():
+    # one BLAS thread per worker process: the pool already uses every core
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
+
+
 def _oracle_chunk(args):
     """Time the FP64 NumPy restatement on one chunk of chains (runs in a worker process)."""
     import numpy as np
@@ -140,7 +146,7 @@ def run_reference(args, rank, world):
     cores = len(os.sched_getaffinity(0))
     ctx = mp.get_context("spawn")
     per = max(1, args.ref_chains_per_core)
-    with ctx.Pool(cores) as pool:
+    with ctx.Pool(cores, initializer=_worker_init) as pool:
         for _ in range(args.warmup):
             cpu_oracle_rate(args.workload, per, cores, pool)
         t0 = time.perf_counter()
@@ -222,7 +228,7 @@ def run_ours(args, rank, world, local_rank):
     pool = None
     cores = len(os.sched_getaffinity(0))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        pool = mp.get_context("spawn").Pool(cores)
+        pool = mp.get_context("spawn").Pool(cores, initializer=_worker_init)
 
     import torch
     import torch.distributed as dist
@@ -331,8 +337,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="heis8x8_D4_chi16")
     ap.add_argument("--chains", type=int, default=0)
-    ap.add_argument("--cpu-chains-per-core", type=int, default=12)
-    ap.add_argument("--ref-chains-per-core", type=int, default=4)
+    ap.add_argument("--cpu-chains-per-core", type=int, default=2)
+    ap.add_argument("--ref-chains-per-core", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

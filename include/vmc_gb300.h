@@ -144,14 +144,17 @@ vmc_status vmc_peps_init_cache(const vmc_plan* plan, void* stream, const float* 
  *   out_E[n_chains] FP64 local energies;
  *   out_logamp[n_chains] FP64 log|psi| and out_sign[n_chains] FP64 sign;
  *   out_margin[n_chains] FP32 min over sites of |min(1, ratio) - u| (the
- *     distance of each accept decision from its threshold).
+ *     distance of each accept decision from its threshold);
+ *   out_gap[n_chains] FP32 min over truncating cuts of the relative gap
+ *     (l_k - l_{k+1}) / l_k of the eigenvalues of theta theta^T (small values
+ *     mark samples whose kept subspace is ill-conditioned).
  */
 vmc_status vmc_peps_sweep(const vmc_plan* plan, void* stream, const float* tensors,
                           int32_t* configs_inout, const double* uniforms, const int32_t* deltas,
                           int n_chains, void* cache_inout, int full_gradient, float* out_O,
                           int8_t* out_p, double* out_E, double* out_logamp, double* out_sign,
-                          float* out_margin, void* workspace, size_t workspace_bytes,
-                          int32_t* status_dev);
+                          float* out_margin, float* out_gap, void* workspace,
+                          size_t workspace_bytes, int32_t* status_dev);
 
 /*
  * Amplitude and hand-written adjoint for samples[n][n_sites]
@@ -161,7 +164,7 @@ vmc_status vmc_peps_sweep(const vmc_plan* plan, void* stream, const float* tenso
  */
 vmc_status vmc_peps_amp_grad(const vmc_plan* plan, void* stream, const float* tensors,
                              const int32_t* samples, int n, int full_gradient, float* out_O,
-                             double* out_logamp, double* out_sign, void* workspace,
+                             double* out_logamp, double* out_sign, float* out_gap, void* workspace,
                              size_t workspace_bytes, int32_t* status_dev);
 
 /*

@@ -13,6 +13,10 @@
 
 namespace vmc {
 
+#if defined(VMC_HOST_EMULATION) && defined(VMC_PHASE_TIMERS)
+inline unsigned long long jacobi_sweep_hist[32];
+#endif
+
 // offset(i) with i = (i1 * n2 + i2) * n3 + i3  ->  i1*s1 + i2*s2 + i3*s3
 struct IMap {
   int n2, n3, s1, s2, s3;
@@ -254,6 +258,10 @@ __device__ inline void jacobi_orthogonalize(float* V, int nv, int len, int ldv, 
     }
     const int any = *sflag;
     __syncthreads();
+#if defined(VMC_HOST_EMULATION) && defined(VMC_PHASE_TIMERS)
+    jacobi_sweep_hist[sweep < 31 ? sweep : 31] += !any;
+    if (any && sweep == max_sweeps - 1) jacobi_sweep_hist[31]++;
+#endif
     if (!any) break;
   }
 }

@@ -19,8 +19,10 @@
 #include <new>
 #include <vector>
 #include <algorithm>
+#include <cstdlib>
 
 #include "device_common.cuh"
+#include "truncation.cuh"
 #include "../../include/vmc_gb300.h"
 
 #ifdef VMC_HOST_EMULATION
@@ -34,14 +36,50 @@ constexpr int kMaxVec = 512;   // max vectors in one truncation (chi * D)
 constexpr int kMaxCols = 64;   // max lattice columns
 constexpr int kMaxD = 4;       // max physical dimension
 constexpr int kPermKinds = 5;  // permuted copies of every site tensor
+constexpr float kJacobiTol = 5e-7f;  // stop when every |a_p.a_q| <= tol |a_p||a_q|
+constexpr int kJacobiSweeps = 16;
+constexpr long long kMaxArenaSmemBytes = 96 * 1024;
 enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4 };
 enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3 };
+
+// Optional per-phase cycle counters (build with -DVMC_PHASE_TIMERS); thread 0
+// of every CTA accumulates clock64() deltas.  Off in the product build.
+enum Phase { PH_T_RENV = 0, PH_T_METRO, PH_T_ZIP, PH_JACOBI, PH_E_RENV, PH_E_LEFT, PH_E_VERT, PH_B_ZIP, PH_CHAIN,
+             PH_COUNT };
+#if defined(VMC_PHASE_TIMERS) && !defined(VMC_HOST_EMULATION)
+__device__ unsigned long long g_phase[PH_COUNT];
+#define VMC_TSTART(v) long long v = clock64()
+#define VMC_TSTOP(v, ph) \
+  do { if (threadIdx.x == 0) atomicAdd(&g_phase[ph], (unsigned long long)(clock64() - (v))); } while (0)
+#elif defined(VMC_PHASE_TIMERS) && defined(VMC_HOST_EMULATION)
+}  // namespace vmc
+#include <chrono>
+namespace vmc {
+unsigned long long g_phase[PH_COUNT];
+inline long long host_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+#define VMC_TSTART(v) long long v = host_ns()
+#define VMC_TSTOP(v, ph) (g_phase[ph] += (unsigned long long)(host_ns() - (v)))
+#else
+#define VMC_TSTART(v) (void)0
+#define VMC_TSTOP(v, ph) (void)0
+#endif
 
 // Device-side plan: scalars plus device pointers into one allocation.
 struct DevPlan {
   int R, C, D, d, chi, strategy, n_sweeps, n_sites;
   int np_sliced;          // sum of params_per_site
   int TS, ES, E2S, SCR, MM;  // buffer sizes (floats)
+  int nmax, kmax;         // largest truncation matrix side / kept bond
+  int trunc_method;       // 0: Gram + tridiagonal eigensolver, 1: one-sided Jacobi
+  int arena_in_smem;      // truncation arena in dynamic shared memory
+  long long arena_floats;
+  int scr1;               // size of one 1-row GEMM intermediate (floats)
+  int vchunk, vbuf;       // vertical-energy chunk (bond values) and buffer size (floats)
+  int vert_in_smem;       // vertical-energy buffers live in the shared-memory arena
+  int onerow_in_smem;     // 1-row intermediates share the shared-memory arena
   int n_scr;              // number of SCR scratch buffers per slot
   long long slot_floats;  // floats per workspace slot
   long long perm_floats;  // floats of the permuted tensor pack
@@ -79,9 +117,7 @@ struct Slot {
   float* lenv;   // (d+1)*ES
   float* r2;     // C*E2S
   float* l2[2];  // E2S
-  float* svm;    // MM
-  float* svc;    // MM
-  float* svq;    // MM
+  float* arena;  // truncation arena when it does not fit shared memory
   float* scr[24];
 };
 
@@ -97,9 +133,7 @@ __device__ inline Slot make_slot(const DevPlan& P, float* base) {
   s.lenv = p; p += al64((long long)(P.d + 1) * P.ES);
   s.r2 = p; p += al64((long long)P.C * P.E2S);
   for (int i = 0; i < 2; ++i) { s.l2[i] = p; p += al64(P.E2S); }
-  s.svm = p; p += al64(P.MM);
-  s.svc = p; p += al64(P.MM);
-  s.svq = p; p += al64(P.MM);
+  s.arena = p; p += P.arena_in_smem ? 0 : al64(P.arena_floats);
   for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
   return s;
 }
@@ -200,11 +234,65 @@ __device__ inline void grad_env(const float* Y1, const float* B, const float* Rc
 // ---------------------------------------------------------------------------
 // Boundary-MPS row application (strategy.apply of strategy.py:118-150 and
 // contraction.py:59-65).  src/dst hold C tensors at stride TS.  Returns the
-// sum of log-norms divided out of the new tensors.
+// sum of log-norms divided out of the new tensors.  The truncation matrices
+// live in `arena` (shared memory when they fit).  *min_gap receives the
+// smallest relative eigen-gap (l_k - l_{k+1}) / l_k of theta theta^T seen at
+// a truncating cut.
 // ---------------------------------------------------------------------------
-__device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared& sh, const float* perm, const float* src,
-                            const int* bin, float* dst, const int* bout, int row, const int* spins,
-                            bool from_below) {
+struct Arena {
+  float* mat;
+  float* G;
+  float* Y;
+  EigScratch eig;
+};
+
+__device__ inline Arena make_arena(const DevPlan& P, float* base) {
+  Arena a;
+  const int nmax = P.nmax, ld = P.nmax | 1, kmax = P.kmax;
+  float* p = base;
+  a.mat = p; p += al64((long long)nmax * ld);
+  a.G = p; p += al64((long long)nmax * ld);
+  a.Y = p; p += al64((long long)nmax * (P.trunc_method == 1 ? ld : kmax));
+  a.eig.S = p; p += al64((long long)kmax * kmax);
+  a.eig.lu = p; p += al64(4LL * kmax * nmax);
+  a.eig.sw = reinterpret_cast<unsigned char*>(p); p += al64(((long long)kmax * nmax + 3) / 4);
+  a.eig.d = p; p += al64(nmax);
+  a.eig.e = p; p += al64(nmax);
+  a.eig.e2 = p; p += al64(nmax);
+  a.eig.tau = p; p += al64(nmax);
+  a.eig.v = p; p += al64(nmax);
+  a.eig.p = p; p += al64(nmax);
+  a.eig.lam = p; p += al64(nmax + 1);
+  a.eig.cvec = p; p += al64(nmax);
+  a.eig.part = p; p += 64;
+  a.eig.flag = reinterpret_cast<int*>(p); p += 64;
+  return a;
+}
+
+__host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_method) {
+  const int ld = nmax | 1;
+  return 2 * al64((long long)nmax * ld) + al64((long long)nmax * (trunc_method == 1 ? ld : kmax)) +
+         al64((long long)kmax * kmax) + al64(4LL * kmax * nmax) + al64(((long long)kmax * nmax + 3) / 4) +
+         7 * al64(nmax) + al64(nmax + 1) + 128;
+}
+
+// Select the kout largest of sig[0..nv) into sh.sel (ties by index).
+__device__ inline void select_topk(Shared& sh, int nv, int kout) {
+  for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+    int rank = 0;
+    const float sj = sh.sig[j];
+    for (int i = 0; i < nv; ++i) {
+      const float si = sh.sig[i];
+      rank += (si > sj) || (si == sj && i < j);
+    }
+    if (rank < kout) sh.sel[rank] = j;
+  }
+  __syncthreads();
+}
+
+__device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared& sh, const float* perm,
+                                         const float* src, const int* bin, float* dst, const int* bout, int row,
+                                         const int* spins, bool from_below, const Arena& ar, float* min_gap) {
   const int C = P.C;
   double logsum = 0.0;
   float* carry = S.scr[0];
@@ -229,8 +317,7 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
                          two(dn, Lb * pout * ncol, Rb), three(pout, Rb, pout * ncol, ncol, 1), din * dn,
                          Lb * pout * Rb, pin));
       const int n_el = din * Lb * pout * ncol;
-      const double nrm2 = cta_dot(out, out, n_el, sh.red);
-      const double nrm = sqrt(nrm2);
+      const double nrm = sqrt(cta_dot(out, out, n_el, sh.red));
       if (nrm > 0.0) {
         cta_scale(out, (float)(1.0 / nrm), n_el);
         logsum += log(nrm);
@@ -254,94 +341,121 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
       break;
     }
     const int kout = bout[c + 1];
-    const bool by_cols = mrows >= ncols;
-    float* mat = S.svm;
-    if (by_cols) {
-      const int ldv = mrows;
-      // vectors = columns; element (row, col) at col*ldv + row
-      cta_gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat, two(dn, pout, Rb * ldv),
-                         two(Rb, 1, ldv), kc * dn, pout * Rb, Lb * pin));
-      cta_copy(S.svc, mat, ncols * ldv);
-      if (kout < ncols || true) {
-        jacobi_orthogonalize(mat, ncols, mrows, ldv, nullptr, 0, 0, 2e-7f, 30, &sh.flag);
-      }
-      // column norms and top-kout selection
-      for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
-        float a = 0.f;
-        for (int i = 0; i < mrows; ++i) a = fmaf(mat[(size_t)j * ldv + i], mat[(size_t)j * ldv + i], a);
-        sh.sig[j] = a;
+    // theta as a row-major matrix: mat[(k,q)][(r',w)], odd leading dimension
+    const int ldm = ncols | 1;
+    float* mat = ar.mat;
+    cta_gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat, two(dn, pout * ldm, Rb),
+                       two(Rb, ldm, 1), kc * dn, pout * Rb, Lb * pin));
+    if (mrows <= ncols && kout >= mrows) {
+      // every row direction is kept: U = I, carry = theta
+      for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) out[e] = (e / mrows == e % mrows) ? 1.f : 0.f;
+      for (int e = threadIdx.x; e < mrows * ncols; e += blockDim.x) {
+        const int i = e / ncols, col = e % ncols;
+        carry_next[(size_t)i * ncols + (col % Rb) * dn + col / Rb] = mat[(size_t)i * ldm + col];
       }
       __syncthreads();
-      for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
-        int rank = 0;
-        const float sj = sh.sig[j];
-        for (int i = 0; i < ncols; ++i) {
-          const float si = sh.sig[i];
-          rank += (si > sj) || (si == sj && i < j);
-        }
-        if (rank < kout) sh.sel[rank] = j;
-      }
-      __syncthreads();
-      float smax = 0.f;
-      for (int i = 0; i < ncols; ++i) smax = fmaxf(smax, sh.sig[i]);
-      // out[(k,q)][k'] = col_sel[k'] / sigma
-      for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) {
-        const int i = e / kout, kk = e % kout;
-        const int j = sh.sel[kk];
-        const float s2 = sh.sig[j];
-        out[e] = (s2 > 1e-30f * smax && s2 > 0.f) ? mat[(size_t)j * ldv + i] / sqrtf(s2) : 0.f;
-      }
-      __syncthreads();
-      // carry'[k'][w][r'] = sum_i out[i][k'] * matc[i][(r',w)]
-      cta_gemm(make_gemm(out, lin(1), kout, S.svc, lin(ldv), 1, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols,
-                         mrows));
-    } else {
-      const int ldv = ncols;
-      // vectors = rows; element (row, col) at row*ldv + col
-      cta_gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat, two(dn, pout * ldv, Rb),
-                         two(Rb, ldv, 1), kc * dn, pout * Rb, Lb * pin));
-      if (kout >= mrows) {
-        // keep everything: U = I, carry = mat
-        for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) out[e] = (e / mrows == e % mrows) ? 1.f : 0.f;
+    } else if (P.trunc_method == 1) {
+      // ---- reference path: one-sided Jacobi on the smaller set of vectors ----
+      if (mrows >= ncols) {
+        // vectors = columns: transpose into G (column j at G + j*ldc), keep theta in mat
+        const int ldc = mrows | 1;
+        float* V = ar.G;
         for (int e = threadIdx.x; e < mrows * ncols; e += blockDim.x) {
-          const int i = e / ncols, col = e % ncols;
-          const int rp = col / Rb, w = col % Rb;
-          carry_next[(size_t)i * ncols + w * dn + rp] = mat[(size_t)i * ldv + col];
+          const int i = e / ncols, j = e % ncols;
+          V[(size_t)j * ldc + i] = mat[(size_t)i * ldm + j];
         }
         __syncthreads();
-      } else {
-        float* Q = S.svq;
-        const int ldq = mrows;
-        for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) Q[e] = (e / mrows == e % mrows) ? 1.f : 0.f;
-        __syncthreads();
-        jacobi_orthogonalize(mat, mrows, ncols, ldv, Q, mrows, ldq, 2e-7f, 30, &sh.flag);
-        for (int j = threadIdx.x; j < mrows; j += blockDim.x) {
+        {
+          VMC_TSTART(tj);
+          jacobi_orthogonalize(V, ncols, mrows, ldc, nullptr, 0, 0, kJacobiTol, kJacobiSweeps, &sh.flag);
+          VMC_TSTOP(tj, PH_JACOBI);
+        }
+        for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
           float a = 0.f;
-          for (int i = 0; i < ncols; ++i) a = fmaf(mat[(size_t)j * ldv + i], mat[(size_t)j * ldv + i], a);
+          for (int i = 0; i < mrows; ++i) a = fmaf(V[(size_t)j * ldc + i], V[(size_t)j * ldc + i], a);
           sh.sig[j] = a;
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < mrows; j += blockDim.x) {
-          int rank = 0;
-          const float sj = sh.sig[j];
-          for (int i = 0; i < mrows; ++i) {
-            const float si = sh.sig[i];
-            rank += (si > sj) || (si == sj && i < j);
-          }
-          if (rank < kout) sh.sel[rank] = j;
+        select_topk(sh, ncols, kout);
+        float smax = 0.f;
+        for (int i = 0; i < ncols; ++i) smax = fmaxf(smax, sh.sig[i]);
+        for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) {
+          const int i = e / kout, kk = e % kout;
+          const int j = sh.sel[kk];
+          const float s2 = sh.sig[j];
+          out[e] = (s2 > 1e-30f * smax && s2 > 0.f) ? V[(size_t)j * ldc + i] / sqrtf(s2) : 0.f;
         }
         __syncthreads();
+        cta_gemm(make_gemm(out, lin(1), kout, mat, lin(1), ldm, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols,
+                           mrows));
+      } else {
+        float* Q = ar.Y;
+        const int ldq = mrows;
+        for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) Q[e] = (e / mrows == e % mrows) ? 1.f : 0.f;
+        __syncthreads();
+        VMC_TSTART(tj);
+        jacobi_orthogonalize(mat, mrows, ncols, ldm, Q, mrows, ldq, kJacobiTol, kJacobiSweeps, &sh.flag);
+        VMC_TSTOP(tj, PH_JACOBI);
+        for (int j = threadIdx.x; j < mrows; j += blockDim.x) {
+          float a = 0.f;
+          for (int i = 0; i < ncols; ++i) a = fmaf(mat[(size_t)j * ldm + i], mat[(size_t)j * ldm + i], a);
+          sh.sig[j] = a;
+        }
+        __syncthreads();
+        select_topk(sh, mrows, kout);
         for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) {
           const int i = e / kout, kk = e % kout;
           out[e] = Q[(size_t)sh.sel[kk] * ldq + i];
         }
         for (int e = threadIdx.x; e < kout * ncols; e += blockDim.x) {
           const int kk = e / ncols, col = e % ncols;
-          const int rp = col / Rb, w = col % Rb;
-          carry_next[(size_t)kk * ncols + w * dn + rp] = mat[(size_t)sh.sel[kk] * ldv + col];
+          carry_next[(size_t)kk * ncols + (col % Rb) * dn + col / Rb] = mat[(size_t)sh.sel[kk] * ldm + col];
         }
         __syncthreads();
       }
+    } else {
+      // ---- Gram + tridiagonal eigensolver on the smaller side ----
+      VMC_TSTART(tj);
+      const bool rows_side = mrows <= ncols;
+      const int nG = rows_side ? mrows : ncols;
+      const int ldg = nG | 1;
+      if (rows_side) {
+        // G = theta theta^T
+        cta_gemm(make_gemm(mat, lin(ldm), 1, mat, lin(ldm), 1, ar.G, lin(ldg), lin(1), nG, nG, ncols));
+      } else {
+        // G = theta^T theta
+        cta_gemm(make_gemm(mat, lin(1), ldm, mat, lin(1), ldm, ar.G, lin(ldg), lin(1), nG, nG, mrows));
+      }
+      cta_sym_topk(ar.G, nG, ldg, kout, ar.Y, kout, ar.eig, sh.red);
+      if (threadIdx.x == 0 && kout < nG) {
+        const float lk = ar.eig.lam[kout - 1], lk1 = ar.eig.lam[kout];
+        const float gap = lk > 0.f ? (lk - lk1) / lk : 0.f;
+        if (gap < *min_gap) *min_gap = gap;
+      }
+      if (rows_side) {
+        for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) out[e] = ar.Y[e];
+        __syncthreads();
+      } else {
+        // U = theta V / |theta V| column-wise
+        cta_gemm(make_gemm(mat, lin(ldm), 1, ar.Y, lin(1), kout, out, lin(kout), lin(1), mrows, kout, ncols));
+        for (int t = threadIdx.x; t < kout; t += blockDim.x) {
+          float a = 0.f;
+          for (int i = 0; i < mrows; ++i) a = fmaf(out[(size_t)i * kout + t], out[(size_t)i * kout + t], a);
+          sh.sig[t] = a;
+        }
+        __syncthreads();
+        float smax = 0.f;
+        for (int t = 0; t < kout; ++t) smax = fmaxf(smax, sh.sig[t]);
+        for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) {
+          const float s2 = sh.sig[e % kout];
+          out[e] = (s2 > 1e-30f * smax && s2 > 0.f) ? out[e] / sqrtf(s2) : 0.f;
+        }
+        __syncthreads();
+      }
+      // carry'[k'][w][r'] = sum_i U[i][k'] theta[i][(r',w)]
+      cta_gemm(make_gemm(out, lin(1), kout, mat, lin(1), ldm, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols,
+                         mrows));
+      VMC_TSTOP(tj, PH_JACOBI);
     }
     // renormalise the new tensor
     {
@@ -352,7 +466,6 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
         logsum += log(nrm);
       }
     }
-    // swap carry buffers
     float* t = carry;
     carry = carry_next;
     carry_next = t;
@@ -437,7 +550,10 @@ __device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Sha
                                const int* tbond, const float* bot, const int* bbond, int row, int* spins,
                                const double* uniforms, const int32_t* deltas, float* min_margin) {
   const int C = P.C;
+  VMC_TSTART(tr);
   right_envs(P, S, perm, top, tbond, bot, bbond, row, spins, false);
+  VMC_TSTOP(tr, PH_T_RENV);
+  VMC_TSTART(tm);
   float* Lc = S.lenv;                  // current left env
   float* Lp0 = S.lenv + P.ES;          // L' for the current spin
   float* Lp1 = S.lenv + 2 * P.ES;      // L' for the proposed spin
@@ -484,6 +600,7 @@ __device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Sha
     float* sel = accept ? Lp1 : Lp0;
     cta_copy(Lc, sel, n_env);
   }
+  VMC_TSTOP(tm, PH_T_METRO);
 }
 
 // ---------------------------------------------------------------------------
@@ -496,7 +613,10 @@ __device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Sha
                                bool want_energy) {
   const int C = P.C;
   const bool has_h = want_energy && P.row_has_h[row];
+  VMC_TSTART(tr);
   right_envs(P, S, perm, top, tbond, bot, bbond, row, spins, has_h);
+  VMC_TSTOP(tr, PH_E_RENV);
+  VMC_TSTART(tl);
   float* Lc = S.lenv;
   float* Y1 = S.scr[3];
   float* Y2 = S.scr[4];
@@ -555,20 +675,21 @@ __device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Sha
       cta_copy(Lc, Lp, n_env);
     }
   }
+  VMC_TSTOP(tl, PH_E_LEFT);
   return energy;
 }
 
 // ---------------------------------------------------------------------------
 // Vertical energy of the row pair (r, r+1) (energy.py:24-95).
-// top: top env of row r; bot: bottom env of row r+1.
+// top: top env of row r; bot: bottom env of row r+1.  Every step is chunked
+// over one bond index (`vc` values at a time) so its intermediates fit the
+// buffers vb[0..1+2d) of P.vbuf floats (shared memory when it fits).
 // ---------------------------------------------------------------------------
-__device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, Shared& sh, const float* perm, const float* top,
-                                  const int* tbond, const float* bot, const int* bbond, int r, const int* sp0,
-                                  const int* sp1, double vscale) {
-  const int C = P.C;
-  float* P1 = S.scr[7];
-  float* P2 = S.scr[8];
-  float* P3 = S.scr[9];
+__device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, Shared& sh, const float* perm,
+                                               const float* top, const int* tbond, const float* bot,
+                                               const int* bbond, int r, const int* sp0, const int* sp1,
+                                               double vscale, float* const* vb) {
+  const int C = P.C, d = P.d;
   // R2_{C-1} = [1]
   if (threadIdx.x == 0) S.r2[(size_t)(C - 1) * P.E2S] = 1.f;
   __syncthreads();
@@ -581,25 +702,27 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
     const float* B = bot + (size_t)c * P.TS;
     const float* Rin = S.r2 + (size_t)c * P.E2S;
     float* Rout = S.r2 + (size_t)(c - 1) * P.E2S;
-    // P1[a][u][rr][y][f] = sum_b T[a][u][b] R2[b][rr][y][f]
-    cta_gemm(make_gemm(T, lin(tb), 1, Rin, lin(1), Rb * Rb1 * bb, P1, lin(Rb * Rb1 * bb), lin(1), ta * U,
-                       Rb * Rb1 * bb, tb));
-    // P2[a][l][f][v][y] = sum_{u,rr} P1[a][u][rr][(y,f)] A(u,v,l,rr)
-    cta_gemm(make_gemm(P1, two(Rb1 * bb, U * Rb * Rb1 * bb, 1), Rb1 * bb, perm_of(P, perm, s0, P_RENV, sp0[c]),
-                       lin(1), Lb * V, P2, three(Rb1, bb, Lb * bb * V * Rb1, 1, V * Rb1), two(V, bb * V * Rb1, Rb1),
-                       ta * Rb1 * bb, Lb * V, U * Rb));
-    // P3[a][l][x][w][f] = sum_{v,y} P2[a][l][f][v][y] A'(v,w,x,y)
-    cta_gemm(make_gemm(P2, lin(V * Rb1), 1, perm_of(P, perm, s1, P_R2, sp1[c]), lin(1), V1 * Lb1, P3,
-                       two(bb, Lb1 * V1 * bb, 1), two(Lb1, bb, V1 * bb), ta * Lb * bb, V1 * Lb1, V * Rb1));
-    // R2'[a][l][x][e] = sum_{w,f} P3[a][l][x][w][f] B[e][w][f]
-    cta_gemm(make_gemm(P3, lin(V1 * bb), 1, B, lin(V1 * bb), 1, Rout, lin(ba), lin(1), ta * Lb * Lb1, ba, V1 * bb));
+    const float* A0 = perm_of(P, perm, s0, P_RENV, sp0[c]);
+    const float* A1 = perm_of(P, perm, s1, P_R2, sp1[c]);
+    for (int a0 = 0; a0 < ta; a0 += P.vchunk) {
+      const int na = P.vchunk < ta - a0 ? P.vchunk : ta - a0;
+      // P1[a][u][rr][y][f] = sum_b T[a][u][b] R2[b][rr][y][f]
+      cta_gemm(make_gemm(T + (size_t)a0 * U * tb, lin(tb), 1, Rin, lin(1), Rb * Rb1 * bb, vb[0], lin(Rb * Rb1 * bb),
+                         lin(1), na * U, Rb * Rb1 * bb, tb));
+      // P2[a][l][f][v][y] = sum_{u,rr} P1[a][u][rr][(y,f)] A(u,v,l,rr)
+      cta_gemm(make_gemm(vb[0], two(Rb1 * bb, U * Rb * Rb1 * bb, 1), Rb1 * bb, A0, lin(1), Lb * V, vb[1],
+                         three(Rb1, bb, Lb * bb * V * Rb1, 1, V * Rb1), two(V, bb * V * Rb1, Rb1), na * Rb1 * bb,
+                         Lb * V, U * Rb));
+      // P3[a][l][x][w][f] = sum_{v,y} P2[a][l][f][v][y] A'(v,w,x,y)
+      cta_gemm(make_gemm(vb[1], lin(V * Rb1), 1, A1, lin(1), V1 * Lb1, vb[0], two(bb, Lb1 * V1 * bb, 1),
+                         two(Lb1, bb, V1 * bb), na * Lb * bb, V1 * Lb1, V * Rb1));
+      // R2'[a][l][x][e] = sum_{w,f} P3[a][l][x][w][f] B[e][w][f]
+      cta_gemm(make_gemm(vb[0], lin(V1 * bb), 1, B, lin(V1 * bb), 1, Rout + (size_t)a0 * Lb * Lb1 * ba, lin(ba),
+                         lin(1), na * Lb * Lb1, ba, V1 * bb));
+    }
   }
   float* Lc = S.l2[0];
   float* Ln = S.l2[1];
-  float* Q1 = S.scr[7];
-  float* Q2 = S.scr[8];
-  float* Q3 = S.scr[9];
-  float* W2 = S.scr[10];
   if (threadIdx.x == 0) Lc[0] = 1.f;
   __syncthreads();
   double energy = 0.0;
@@ -610,43 +733,57 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
     const int ta = tbond[c], tb = tbond[c + 1], ba = bbond[c], bb = bbond[c + 1];
     const float* T = top + (size_t)c * P.TS;
     const float* B = bot + (size_t)c * P.TS;
-    // Q1[x][e][b][l][u] = sum_a L2[a][(l,x,e)] T[a][(u,b)]
-    cta_gemm(make_gemm(Lc, lin(1), Lb * Lb1 * ba, T, lin(1), U * tb, Q1, two(Lb1 * ba, U, tb * Lb * U),
-                       two(tb, 1, Lb * U), Lb * Lb1 * ba, U * tb, ta));
+    const float* Rc = S.r2 + (size_t)c * P.E2S;
     const bool vt = P.vert_mask[r * C + c];
-    const int q2n = Lb1 * ba * tb * Rb * V;  // elements of one Q2
-    // Q2[p][e][b][rr][x][v] = sum_{l,u} Q1[x][e][b][l][u] A[p](u,v,l,rr)
-    for (int p = 0; p < P.d; ++p) {
-      if (!vt && p != sp0[c]) continue;
-      float* Q2p = (p == sp0[c]) ? Q2 : S.scr[11 + p];
-      cta_gemm(make_gemm(Q1, lin(Lb * U), 1, perm_of(P, perm, s0, P_LENV, p), lin(1), Rb * V, Q2p,
-                         two(ba * tb, V, Rb * Lb1 * V), two(V, Lb1 * V, 1), Lb1 * ba * tb, Rb * V, Lb * U));
-    }
-    if (vt) {
-      const float* Rc = S.r2 + (size_t)c * P.E2S;
-      // W2[e][b][rr][w][y] = sum_f B[e][w][f] R2[b][rr][y][f]
-      cta_gemm(make_gemm(B, lin(bb), 1, Rc, lin(bb), 1, W2, two(V1, tb * Rb * V1 * Rb1, Rb1),
-                         three(Rb, Rb1, Rb * V1 * Rb1, V1 * Rb1, 1), ba * V1, tb * Rb * Rb1, bb));
-      const float* op = P.vert + (size_t)(r * C + c) * P.d * P.d * P.d * P.d;
-      const int col = sp0[c] * P.d + sp1[c];
-      for (int q = 0; q < P.d; ++q) {
-        float* Vq = S.scr[11 + kMaxD + q];
-        // Vq[e][b][rr][x][v] = sum_{w,y} A'[q][x][v][w][y] W2[e][b][rr][w][y]
-        cta_gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, q), lin(V1 * Rb1), 1, W2, lin(V1 * Rb1), 1, Vq, lin(1),
-                           lin(Lb1 * V), Lb1 * V, ba * tb * Rb, V1 * Rb1));
-        for (int p = 0; p < P.d; ++p) {
-          const float* Q2p = (p == sp0[c]) ? Q2 : S.scr[11 + p];
-          const double psi = cta_dot(Q2p, Vq, q2n, sh.red);
-          energy += (double)op[(size_t)(p * P.d + q) * P.d * P.d + col] * psi * vscale;
+    const bool last = (c == C - 1);
+    if (!vt && last) break;
+    double psi[kMaxD * kMaxD];
+    for (int i = 0; i < d * d; ++i) psi[i] = 0.0;
+    const int s_cur = sp0[c];
+    for (int b0 = 0; b0 < tb; b0 += P.vchunk) {
+      const int nb = P.vchunk < tb - b0 ? P.vchunk : tb - b0;
+      float* Q1 = vb[0];
+      // Q1[x][e][b][l][u] = sum_a L2[a][(l,x,e)] T[a][u][b0+b]
+      cta_gemm(make_gemm(Lc, lin(1), Lb * Lb1 * ba, T + b0, two(nb, tb, 1), U * tb, Q1,
+                         two(Lb1 * ba, U, nb * Lb * U), two(nb, 1, Lb * U), Lb * Lb1 * ba, U * nb, ta));
+      // Q2[p][e][b][rr][x][v] = sum_{l,u} Q1[x][e][b][l][u] A[p](u,v,l,rr)
+      for (int p = 0; p < d; ++p) {
+        if (!vt && p != s_cur) continue;
+        cta_gemm(make_gemm(Q1, lin(Lb * U), 1, perm_of(P, perm, s0, P_LENV, p), lin(1), Rb * V, vb[1 + p],
+                           two(ba * nb, V, Rb * Lb1 * V), two(V, Lb1 * V, 1), Lb1 * ba * nb, Rb * V, Lb * U));
+      }
+      if (vt) {
+        float* W2 = vb[0];
+        // W2[e][b][rr][w][y] = sum_f B[e][w][f] R2[b0+b][rr][y][f]
+        cta_gemm(make_gemm(B, lin(bb), 1, Rc + (size_t)b0 * Rb * Rb1 * bb, lin(bb), 1, W2,
+                           two(V1, nb * Rb * V1 * Rb1, Rb1), three(Rb, Rb1, Rb * V1 * Rb1, V1 * Rb1, 1), ba * V1,
+                           nb * Rb * Rb1, bb));
+        const int q2n = Lb1 * ba * nb * Rb * V;
+        for (int q = 0; q < d; ++q) {
+          float* Vq = vb[1 + d + q];
+          // Vq[e][b][rr][x][v] = sum_{w,y} A'[q][x][v][w][y] W2[e][b][rr][w][y]
+          cta_gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, q), lin(V1 * Rb1), 1, W2, lin(V1 * Rb1), 1, Vq, lin(1),
+                             lin(Lb1 * V), Lb1 * V, ba * nb * Rb, V1 * Rb1));
+          for (int p = 0; p < d; ++p) psi[p * d + q] += cta_dot(vb[1 + p], Vq, q2n, sh.red);
         }
       }
+      if (!last) {
+        float* Q3 = vb[0];
+        // Q3[b][rr][y][e][w] = sum_{x,v} Q2[s][e][b][rr][x][v] A'(v,w,x,y)
+        cta_gemm(make_gemm(vb[1 + s_cur], lin(Lb1 * V), 1, perm_of(P, perm, s1, P_ZIPT, sp1[c]), lin(1), V1 * Rb1,
+                           Q3, two(nb * Rb, V1, Rb1 * ba * V1), two(Rb1, 1, ba * V1), ba * nb * Rb, V1 * Rb1,
+                           Lb1 * V));
+        // L2'[b0+b][rr][y][f] = sum_{e,w} Q3 B[e][w][f]
+        cta_gemm(make_gemm(Q3, lin(ba * V1), 1, B, lin(1), bb, Ln + (size_t)b0 * Rb * Rb1 * bb, lin(bb), lin(1),
+                           nb * Rb * Rb1, bb, ba * V1));
+      }
     }
-    if (c < C - 1) {
-      // Q3[b][rr][y][e][w] = sum_{x,v} Q2[e][b][rr][x][v] A'(v,w,x,y)
-      cta_gemm(make_gemm(Q2, lin(Lb1 * V), 1, perm_of(P, perm, s1, P_ZIPT, sp1[c]), lin(1), V1 * Rb1, Q3,
-                         two(tb * Rb, V1, Rb1 * ba * V1), two(Rb1, 1, ba * V1), ba * tb * Rb, V1 * Rb1, Lb1 * V));
-      // L2'[b][rr][y][f] = sum_{e,w} Q3 B[e][w][f]
-      cta_gemm(make_gemm(Q3, lin(ba * V1), 1, B, lin(1), bb, Ln, lin(bb), lin(1), tb * Rb * Rb1, bb, ba * V1));
+    if (vt) {
+      const float* op = P.vert + (size_t)(r * C + c) * d * d * d * d;
+      const int col = s_cur * d + sp1[c];
+      for (int j = 0; j < d * d; ++j) energy += (double)op[(size_t)j * d * d + col] * psi[j] * vscale;
+    }
+    if (!last) {
       float* t = Lc;
       Lc = Ln;
       Ln = t;
@@ -673,15 +810,35 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
     const DevPlan* __restrict__ Pp, int mode, const float* __restrict__ tensors, const float* __restrict__ perm,
     int32_t* configs, const double* __restrict__ uniforms, const int32_t* __restrict__ deltas, int n_chains,
     float* cache, int full_gradient, float* out_O, int8_t* out_p, double* out_E, double* logamp_io,
-    double* sign_io, float* out_margin, float* ws, int32_t* status) {
+    double* sign_io, float* out_margin, float* out_gap, float* ws, int32_t* status) {
   const DevPlan& P = *Pp;
   VMC_SHARED Shared sh;
-  const Slot S = make_slot(P, ws + P.perm_floats + (size_t)blockIdx.x * P.slot_floats);
+  Slot S = make_slot(P, ws + P.perm_floats + (size_t)blockIdx.x * P.slot_floats);
+#ifdef VMC_HOST_EMULATION
+  static float* dyn_smem = nullptr;
+  static long long dyn_floats = 0;
+  if (P.arena_in_smem && dyn_floats < P.arena_floats) {
+    std::free(dyn_smem);
+    dyn_smem = static_cast<float*>(std::malloc(sizeof(float) * P.arena_floats));
+    dyn_floats = P.arena_floats;
+  }
+#else
+  extern __shared__ float dyn_smem[];
+#endif
+  const Arena ar = make_arena(P, P.arena_in_smem ? dyn_smem : S.arena);
+  if (P.onerow_in_smem) {
+    // the 1-row environment GEMM intermediates are never live during a truncation
+    for (int i = 0; i < 4; ++i) S.scr[3 + i] = dyn_smem + (size_t)i * P.scr1;
+  }
+  float* vbuf[1 + 2 * kMaxD];
+  for (int i = 0; i < 1 + 2 * P.d; ++i)
+    vbuf[i] = P.vert_in_smem ? dyn_smem + (size_t)i * P.vbuf : S.scr[7 + i];
   const int R = P.R, C = P.C;
   const int n_params = full_gradient ? P.d * P.np_sliced : P.np_sliced;
 
   for (int chain = blockIdx.x; chain < n_chains; chain += gridDim.x) {
     int32_t* cfg = configs + (size_t)chain * P.n_sites;
+    float min_gap = INFINITY;
 
     if (mode == MODE_INIT) {
       // init_cache (kernels.py:115-129): bottom envs from the bottom up
@@ -693,7 +850,8 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
         for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
         __syncthreads();
         const double ls = apply_row(P, S, sh, perm, cache_row(P, cache, chain, r), bbonds(P, r),
-                                    cache_row(P, cache, chain, r - 1), bbonds(P, r - 1), r, sh.spins[0], true);
+                                    cache_row(P, cache, chain, r - 1), bbonds(P, r - 1), r, sh.spins[0], true, ar,
+                                    &min_gap);
         if (threadIdx.x == 0) lb[r - 1] = lb[r] + ls;
         __syncthreads();
       }
@@ -701,6 +859,7 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
     }
 
     // ---------------- top-down pass: transition or forward ----------------
+    VMC_TSTART(tchain);
     float min_margin = INFINITY;
     fill_ones_row(P, S.topc);
     if (threadIdx.x == 0) S.lt[0] = 0.0;
@@ -717,8 +876,10 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
         for (int c = threadIdx.x; c < C; c += blockDim.x) cfg[r * C + c] = sh.spins[0][c];
         __syncthreads();
       }
+      VMC_TSTART(tz);
       const double ls = apply_row(P, S, sh, perm, top, tbonds(P, r), S.topc + (size_t)(r + 1) * C * P.TS,
-                                  tbonds(P, r + 1), r, sh.spins[0], false);
+                                  tbonds(P, r + 1), r, sh.spins[0], false, ar, &min_gap);
+      VMC_TSTOP(tz, PH_T_ZIP);
       if (threadIdx.x == 0) S.lt[r + 1] = S.lt[r] + ls;
       __syncthreads();
     }
@@ -775,12 +936,16 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
                              Orow, full_gradient, want_grad, want_energy);
       if (want_energy && r < R - 1 && P.row_has_v[r]) {
         const double vscale = sgn * exp(S.lt[r] + lb_prev - logamp);
+        VMC_TSTART(tv);
         energy += vertical_energy(P, S, sh, perm, top, tbonds(P, r), S.brow[ib_prev], bbonds(P, r + 1), r,
-                                  sh.spins[0], sh.spins[1], vscale);
+                                  sh.spins[0], sh.spins[1], vscale, vbuf);
+        VMC_TSTOP(tv, PH_E_VERT);
       }
       if (r > 0) {
+        VMC_TSTART(tb);
         const double ls = apply_row(P, S, sh, perm, bcur, bbonds(P, r), S.brow[ib_next], bbonds(P, r - 1), r,
-                                    sh.spins[0], true);
+                                    sh.spins[0], true, ar, &min_gap);
+        VMC_TSTOP(tb, PH_B_ZIP);
         lb_prev = lb_cur;
         lb_cur = lb_cur + ls;
         const int t = ib_prev;
@@ -789,6 +954,7 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
         ib_next = t;
       }
     }
+    if (out_gap && threadIdx.x == 0) out_gap[chain] = min_gap;
     if (want_energy && threadIdx.x == 0) {
       out_E[chain] = energy;
       if (!isfinite(energy)) atomicOr(status, VMC_DEV_NONFINITE);
@@ -802,6 +968,7 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
       }
     }
     __syncthreads();
+    VMC_TSTOP(tchain, PH_CHAIN);
   }
 }
 
@@ -1038,11 +1205,48 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   // truncation matrices: rows kc*pout <= chimax*D, cols <= chimax*D
   MM = (chimax * D + 1) * (chimax * D + 1);
   const long long SCR = std::max({chimax * chimax * D * D * D, TS * D * D, MM, 4LL * kMaxVec});
+  P.nmax = (int)(chimax * D);
+  P.kmax = (int)std::min<long long>(chi, chimax * D);
+  {
+    const char* tm = std::getenv("VMC_TRUNCATION");
+    P.trunc_method = (tm && std::strcmp(tm, "jacobi") == 0) ? 1 : 0;
+  }
+  P.arena_floats = arena_floats(P.nmax, P.kmax, P.trunc_method);
+  P.arena_in_smem = P.arena_floats * 4 <= kMaxArenaSmemBytes ? 1 : 0;
+  P.scr1 = (int)al64(std::max(chimax * chimax * D * D, (long long)D * D * D * D));
+  {
+    // one bond value of a vertical-energy intermediate holds <= chimax * D^3 floats
+    const long long unit = chimax * D * D * D;
+    const long long nbuf = 1 + 2LL * d;
+    long long ch = (kMaxArenaSmemBytes / 4) / (nbuf * unit);
+    ch = std::max(1LL, std::min(ch, chimax));
+    if (const char* vc = std::getenv("VMC_VCHUNK")) ch = std::max(1LL, std::min(ch, (long long)std::atoi(vc)));
+    P.vchunk = (int)ch;
+    P.vbuf = (int)al64(ch * unit);
+    P.vert_in_smem = nbuf * P.vbuf * 4 <= kMaxArenaSmemBytes ? 1 : 0;
+    if (!P.vert_in_smem) {
+      // global scratch buffers (SCR floats each) hold whole steps
+      P.vchunk = (int)chimax;
+      P.vbuf = (int)SCR;
+    }
+  }
+  P.onerow_in_smem = 0;
+  if (P.arena_in_smem && std::max(P.arena_floats, 4LL * P.scr1) * 4 <= kMaxArenaSmemBytes) {
+    P.onerow_in_smem = 1;
+    P.arena_floats = std::max(P.arena_floats, 4LL * P.scr1);
+  }
+  if (P.arena_in_smem && P.vert_in_smem) {
+    P.arena_floats = std::max(P.arena_floats, (1 + 2LL * d) * P.vbuf);
+  } else {
+    P.vert_in_smem = 0;
+    P.vchunk = (int)chimax;
+    P.vbuf = (int)SCR;
+  }
   P.TS = (int)TS; P.ES = (int)ES; P.E2S = (int)E2S; P.MM = (int)MM; P.SCR = (int)SCR;
   P.n_scr = 11 + 2 * kMaxD;
   P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + 3 * al64((long long)C * TS) +
                   al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
-                  2 * al64(E2S) + 3 * al64(MM) + (long long)P.n_scr * al64(SCR);
+                  2 * al64(E2S) + (P.arena_in_smem ? 0 : al64(P.arena_floats)) + (long long)P.n_scr * al64(SCR);
   P.cache_floats_per_chain = al64((long long)R * C * TS);
   if (chimax * D > kMaxVec) {
     delete pl;
@@ -1136,45 +1340,72 @@ size_t vmc_workspace_size(const vmc_plan* pl, int n_chains) {
 static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float* tensors, int32_t* configs,
                          const double* uniforms, const int32_t* deltas, int n, void* cache, int full_gradient,
                          float* out_O, int8_t* out_p, double* out_E, double* logamp, double* sign, float* margin,
-                         void* ws, size_t ws_bytes, int32_t* status) {
+                         float* gap, void* ws, size_t ws_bytes, int32_t* status) {
   if (!pl || !tensors || !configs || n < 0 || !ws || !status) return VMC_ERR_INVALID;
   if (n == 0) return VMC_OK;
   if (ws_bytes < vmc_workspace_size(pl, n)) return VMC_ERR_WORKSPACE;
   const int grid = n_slots(pl, n);
   float* wsf = static_cast<float*>(ws);
   VMC_LAUNCH(permute_tensors_kernel, std::min(pl->hp.n_sites, 1024), kThreads, 0, stream, pl->dplan, tensors, wsf);
-  VMC_LAUNCH(peps_kernel, grid, kThreads, 0, stream, pl->dplan, mode, tensors, wsf, configs, uniforms, deltas, n,
-             static_cast<float*>(cache), full_gradient, out_O, out_p, out_E, logamp, sign, margin, wsf, status);
+  const size_t smem = pl->hp.arena_in_smem ? (size_t)pl->hp.arena_floats * 4 : 0;
+#ifndef VMC_HOST_EMULATION
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return VMC_ERR_CUDA;
+#endif
+  VMC_LAUNCH(peps_kernel, grid, kThreads, smem, stream, pl->dplan, mode, tensors, wsf, configs, uniforms, deltas, n,
+             static_cast<float*>(cache), full_gradient, out_O, out_p, out_E, logamp, sign, margin, gap, wsf, status);
   return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
 }
+
+#if defined(VMC_PHASE_TIMERS) && defined(VMC_HOST_EMULATION)
+int vmc_debug_phase_timers(unsigned long long* host_out) {
+  for (int i = 0; i < PH_COUNT; ++i) { host_out[i] = g_phase[i]; g_phase[i] = 0; }
+  return PH_COUNT;
+}
+#endif
+#if defined(VMC_PHASE_TIMERS) && !defined(VMC_HOST_EMULATION)
+// Debug-only (not part of the product ABI): read and reset the phase counters.
+int vmc_debug_phase_timers(unsigned long long* host_out) {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return -(int)e;
+  e = cudaMemcpyFromSymbol(host_out, g_phase, sizeof(unsigned long long) * PH_COUNT);
+  if (e != cudaSuccess) return -1000 - (int)e;
+  unsigned long long z[PH_COUNT] = {0};
+  e = cudaMemcpyToSymbol(g_phase, z, sizeof(z));
+  if (e != cudaSuccess) return -2000 - (int)e;
+  return PH_COUNT;
+}
+#endif
 
 vmc_status vmc_peps_init_cache(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* configs,
                                int n_chains, void* cache, void* workspace, size_t workspace_bytes,
                                int32_t* status_dev) {
   if (!cache) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_INIT, tensors, const_cast<int32_t*>(configs), nullptr, nullptr, n_chains, cache, 0,
-                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, workspace, workspace_bytes, status_dev);
+                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, workspace, workspace_bytes,
+                status_dev);
 }
 
 vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors, int32_t* configs_inout,
                           const double* uniforms, const int32_t* deltas, int n_chains, void* cache_inout,
                           int full_gradient, float* out_O, int8_t* out_p, double* out_E, double* out_logamp,
-                          double* out_sign, float* out_margin, void* workspace, size_t workspace_bytes,
-                          int32_t* status_dev) {
+                          double* out_sign, float* out_margin, float* out_gap, void* workspace,
+                          size_t workspace_bytes, int32_t* status_dev) {
   if (!pl || !uniforms || !cache_inout || !out_E || !out_logamp || !out_sign) return VMC_ERR_INVALID;
   if (pl->hp.d > 2 && !deltas) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_SWEEP, tensors, configs_inout, uniforms, deltas, n_chains, cache_inout,
-                full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, workspace, workspace_bytes,
-                status_dev);
+                full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, out_gap, workspace,
+                workspace_bytes, status_dev);
 }
 
 vmc_status vmc_peps_amp_grad(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples, int n,
-                             int full_gradient, float* out_O, double* out_logamp, double* out_sign, void* workspace,
-                             size_t workspace_bytes, int32_t* status_dev) {
+                             int full_gradient, float* out_O, double* out_logamp, double* out_sign, float* out_gap,
+                             void* workspace, size_t workspace_bytes, int32_t* status_dev) {
   if (!pl || !out_logamp || !out_sign) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_AMPGRAD, tensors, const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr,
-                full_gradient, out_O, nullptr, nullptr, out_logamp, out_sign, nullptr, workspace, workspace_bytes,
-                status_dev);
+                full_gradient, out_O, nullptr, nullptr, out_logamp, out_sign, nullptr, out_gap, workspace,
+                workspace_bytes, status_dev);
 }
 
 vmc_status vmc_peps_local_energy(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples,
@@ -1182,8 +1413,8 @@ vmc_status vmc_peps_local_energy(const vmc_plan* pl, void* stream, const float* 
                                  size_t workspace_bytes, int32_t* status_dev) {
   if (!pl || !logamp || !sign || !out_E) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_ENERGY, tensors, const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr, 0,
-                nullptr, nullptr, out_E, const_cast<double*>(logamp), const_cast<double*>(sign), nullptr, workspace,
-                workspace_bytes, status_dev);
+                nullptr, nullptr, out_E, const_cast<double*>(logamp), const_cast<double*>(sign), nullptr, nullptr,
+                workspace, workspace_bytes, status_dev);
 }
 
 }  // extern "C"

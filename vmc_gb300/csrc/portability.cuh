@@ -31,8 +31,14 @@ struct vmc_dim3 {
 extern thread_local vmc_dim3 threadIdx, blockIdx, blockDim, gridDim;
 
 inline void __syncthreads() {}
+inline void __syncwarp(unsigned = 0xffffffffu) {}
 inline float __shfl_xor_sync(unsigned, float v, int, int = 32) { return v; }
 inline double __shfl_xor_sync(unsigned, double v, int, int = 32) { return v; }
+inline unsigned __ballot_sync(unsigned, int pred) { return pred ? 1u : 0u; }
+inline int __popc(unsigned v) { return __builtin_popcount(v); }
+inline float __shfl_sync(unsigned, float v, int, int = 32) { return v; }
+inline int __shfl_sync(unsigned, int v, int, int = 32) { return v; }
+inline float __fdividef(float a, float b) { return a / b; }
 inline int atomicOr(int* p, int v) {
   int o = *p;
   *p |= v;

@@ -1,0 +1,448 @@
+// truncation.cuh -- CTA-level dominant invariant subspace of a small symmetric
+// matrix, for the boundary-MPS truncation (strategy.py:128-150: keep the top-k
+// left singular vectors of theta).
+//
+// The amplitude only depends on the kept subspace, so the truncation works on
+// the Gram matrix G = M M^T (or M^T M) of the theta matrix M:
+//   1. Householder tridiagonalisation  G = Q T Q^T   (3 barriers per column),
+//   2. multisection bisection with Sturm counts for the k (+1) largest
+//      eigenvalues of T (groups of 8 lanes per eigenvalue),
+//   3. inverse iteration on the tridiagonal T for each eigenvalue (one thread
+//      per eigenvector, LU with partial pivoting),
+//   4. CholQR2 re-orthonormalisation of the k vectors (warp Cholesky),
+//   5. back-transformation with the stored reflectors: U = Q Y.
+// All arrays may live in shared or global memory.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace vmc {
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#ifndef VMC_HOST_EMULATION
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+#endif
+  return v;
+}
+
+__device__ __forceinline__ void warp_sync() {
+#ifndef VMC_HOST_EMULATION
+  __syncwarp();
+#endif
+}
+
+// In-place Householder tridiagonalisation of the symmetric n x n matrix A
+// (row-major, leading dimension lda).  On exit d[0..n-1], e[0..n-2] hold T,
+// tau[j] and A[j+1+i][j] (i >= 1; v_j[0] = 1 implicit) the reflectors
+// H_j = I - tau_j v_j v_j^T with G = H_0 ... H_{n-3} T H_{n-3} ... H_0.
+// `v`, `p` are n floats of scratch; `part` holds >= 64 floats.
+// Per column: 3 barriers; the matrix-vector product uses `rg` threads per row
+// and the rank-2 update a 2-D thread grid (no integer division).
+__device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, float* e, float* tau, float* v,
+                                          float* p, float* part) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = (nt + 31) >> 5;
+  if (n == 1) {
+    if (tid == 0) d[0] = A[0];
+    __syncthreads();
+    return;
+  }
+  // threads per row in the matvec (power of two, <= 32)
+  int rg = 1;
+  while (rg * 2 <= 32 && rg * 2 * n <= nt) rg *= 2;
+  const int rrow = tid / rg, rlane = tid % rg, nrow_thr = nt / rg;
+  const unsigned rmask = (rg == 32) ? 0xffffffffu : (((1u << rg) - 1u) << ((tid & 31) & ~(rg - 1)));
+  // 2-D grid for the update: gx columns x gy rows
+  int gx = 1;
+  while (gx * gx < nt) gx *= 2;
+  if (gx > nt) gx = nt;
+  const int gy = nt / gx;
+  const int ux = tid % gx, uy = tid / gx;
+  {
+    float s = 0.f;
+    for (int i = 2 + tid; i < n; i += nt) s = fmaf(A[(size_t)i * lda], A[(size_t)i * lda], s);
+    s = warp_sum_f(s);
+    if (lane == 0) part[warp] = s;
+  }
+  __syncthreads();
+  for (int j = 0; j < n - 2; ++j) {
+    const int m = n - j - 1;
+    float xn2 = 0.f;
+    for (int w = 0; w < nwarps; ++w) xn2 += part[w];
+    const float alpha = A[(size_t)(j + 1) * lda + j];
+    float tj = 0.f, beta = alpha, scal = 0.f;
+    if (xn2 > 0.f) {
+      beta = -copysignf(sqrtf(alpha * alpha + xn2), alpha);
+      tj = (beta - alpha) / beta;
+      scal = 1.f / (alpha - beta);
+    }
+    for (int i = tid; i < m; i += nt) {
+      const float vi = (i == 0) ? 1.f : A[(size_t)(j + 1 + i) * lda + j] * scal;
+      v[i] = vi;
+      if (i > 0) A[(size_t)(j + 1 + i) * lda + j] = vi;
+    }
+    if (tid == 0) {
+      d[j] = A[(size_t)j * lda + j];
+      e[j] = beta;
+      tau[j] = tj;
+    }
+    __syncthreads();  // (1) v visible
+    float* As = A + (size_t)(j + 1) * lda + (j + 1);
+    if (tj == 0.f) {
+      float s = 0.f;
+      for (int i = 2 + tid; i < m; i += nt) s = fmaf(As[(size_t)i * lda], As[(size_t)i * lda], s);
+      s = warp_sum_f(s);
+      if (lane == 0) part[warp] = s;
+      __syncthreads();
+      continue;
+    }
+    // p = tau * A_sub v, rg threads per row; partial p.v per warp
+    float pv = 0.f;
+    for (int i = rrow; i < m; i += nrow_thr) {
+      const float* row = As + (size_t)i * lda;
+      float s = 0.f;
+      for (int l = rlane; l < m; l += rg) s = fmaf(row[l], v[l], s);
+#ifndef VMC_HOST_EMULATION
+      for (int o = rg / 2; o > 0; o >>= 1) s += __shfl_xor_sync(rmask, s, o, rg);
+#endif
+      const float pi = tj * s;
+      if (rlane == 0) {
+        p[i] = pi;
+        pv = fmaf(pi, v[i], pv);
+      }
+    }
+    pv = warp_sum_f(pv);
+    if (lane == 0) part[32 + warp] = pv;
+    __syncthreads();  // (2) p visible
+    float ptv = 0.f;
+    for (int w = 0; w < nwarps; ++w) ptv += part[32 + w];
+    const float K = 0.5f * tj * ptv;
+    // A_sub -= v w^T + w v^T, w = p - K v
+    float s = 0.f;
+    for (int i = uy; i < m; i += gy) {
+      const float vi = v[i], wi = p[i] - K * vi;
+      float* arow = As + (size_t)i * lda;
+      for (int l = ux; l < m; l += gx) {
+        const float vl = v[l], wl = p[l] - K * vl;
+        const float nv = arow[l] - vi * wl - wi * vl;
+        arow[l] = nv;
+        if (l == 0 && i >= 2) s = fmaf(nv, nv, s);
+      }
+    }
+    s = warp_sum_f(s);
+    if (lane == 0) part[warp] = s;
+    __syncthreads();  // (3) trailing matrix updated
+  }
+  if (tid == 0) {
+    d[n - 2] = A[(size_t)(n - 2) * lda + n - 2];
+    e[n - 2] = A[(size_t)(n - 1) * lda + n - 2];
+    d[n - 1] = A[(size_t)(n - 1) * lda + n - 1];
+  }
+  __syncthreads();
+  (void)rmask;
+}
+
+// Number of eigenvalues of T (d, e2 = e^2) smaller than x.
+__device__ __forceinline__ int sturm_count(const float* d, const float* e2, int n, float x, float pivmin) {
+  float q = d[0] - x;
+  if (fabsf(q) < pivmin) q = -pivmin;
+  int cnt = q < 0.f;
+  for (int i = 1; i < n; ++i) {
+    q = (d[i] - x) - __fdividef(e2[i - 1], q);
+    if (fabsf(q) < pivmin) q = -pivmin;
+    cnt += q < 0.f;
+  }
+  return cnt;
+}
+
+// The kk largest eigenvalues of T, descending, into lam[0..kk-1].
+// e2 receives e^2 (n-1 floats of scratch).  Returns the Gershgorin scale |T|.
+__device__ inline float cta_top_eigenvalues(const float* d, const float* e, float* e2, int n, int kk, float* lam) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < n - 1; i += nt) e2[i] = e[i] * e[i];
+  __syncthreads();
+  float lo = 3.4e38f, hi = -3.4e38f, e2max = 0.f;
+  for (int i = 0; i < n; ++i) {
+    const float r = (i > 0 ? fabsf(e[i - 1]) : 0.f) + (i < n - 1 ? fabsf(e[i]) : 0.f);
+    lo = fminf(lo, d[i] - r);
+    hi = fmaxf(hi, d[i] + r);
+    if (i < n - 1) e2max = fmaxf(e2max, e2[i]);
+  }
+  const float tnorm = fmaxf(fabsf(lo), fabsf(hi));
+  const float pivmin = 1e-30f * fmaxf(1.f, e2max);
+  const float span = hi - lo;
+  lo -= 1e-6f * span + 1e-30f;
+  hi += 1e-6f * span + 1e-30f;
+  int G = nt >= 8 ? 8 : 1;
+  const int ngroups = nt / G;
+  const int l = tid % G;
+  const int base = (tid & 31) & ~(G - 1);
+  const unsigned gmask = (G == 1) ? 1u : (0xffu << base);
+  const int npts = G > 1 ? G - 1 : 1;
+  const int rounds = (kk + ngroups - 1) / ngroups;
+  for (int rd = 0; rd < rounds; ++rd) {
+    const int t = rd * ngroups + tid / G;
+    const bool valid = t < kk && tid / G < ngroups;
+    const int idx = n - 1 - (valid ? t : 0);
+    float a = lo, b = hi;
+    const int max_it = npts > 1 ? 14 : 64;
+    for (int it = 0; it < max_it; ++it) {
+      const float step = (b - a) / (float)(npts + 1);
+      int pred = 0;
+      if (l < npts) pred = sturm_count(d, e2, n, a + (float)(l + 1) * step, pivmin) <= idx;
+#ifdef VMC_HOST_EMULATION
+      const unsigned bits = (unsigned)pred;
+#else
+      const unsigned bits = (__ballot_sync(gmask, pred) >> base) & ((1u << G) - 1u);
+#endif
+      const int L = __popc(bits);
+      const float na = (L == 0) ? a : a + (float)L * step;
+      const float nb = (L == npts) ? b : a + (float)(L + 1) * step;
+      a = na;
+      b = nb;
+      if (b - a <= 2.5e-7f * fmaxf(fabsf(a), fabsf(b)) + pivmin) break;
+    }
+    if (valid && l == 0) lam[t] = 0.5f * (a + b);
+  }
+  __syncthreads();
+  return tnorm;
+}
+
+// One eigenvector of T for eigenvalue lam by inverse iteration (serial; one
+// thread).  x receives the normalised vector with stride xs.  u0/u1/u2/mul
+// are n floats each and sw n bytes of private scratch.
+// If n_orth > 0, every iterate is orthogonalised against the n_orth vectors
+// `orth` (stride xs, column offset 1 apart) -- used for clusters of nearly
+// equal eigenvalues.
+__device__ inline void tri_inverse_iteration(const float* d, const float* e, int n, float lam, float tnorm, float* x,
+                                             int xs, float* u0, float* u1, float* u2, float* mul,
+                                             unsigned char* sw, unsigned seed, const float* orth = nullptr,
+                                             int n_orth = 0) {
+  const float tiny = 1.2e-7f * fmaxf(tnorm, 1e-30f);
+  float al = d[0] - lam;
+  float be = n > 1 ? e[0] : 0.f;
+  for (int i = 0; i < n - 1; ++i) {
+    const float c = e[i];
+    const float a1 = d[i + 1] - lam;
+    const float b1 = (i + 1 < n - 1) ? e[i + 1] : 0.f;
+    if (fabsf(al) >= fabsf(c)) {
+      float piv = al;
+      if (fabsf(piv) < tiny) piv = copysignf(tiny, piv == 0.f ? 1.f : piv);
+      const float m = c / piv;
+      sw[i] = 0;
+      u0[i] = piv;
+      u1[i] = be;
+      u2[i] = 0.f;
+      mul[i] = m;
+      al = a1 - m * be;
+      be = b1;
+    } else {
+      const float m = al / c;
+      sw[i] = 1;
+      u0[i] = c;
+      u1[i] = a1;
+      u2[i] = b1;
+      mul[i] = m;
+      al = be - m * a1;
+      be = -m * b1;
+    }
+  }
+  if (fabsf(al) < tiny) al = copysignf(tiny, al == 0.f ? 1.f : al);
+  u0[n - 1] = al;
+  // start vector: deterministic pseudo-random entries in [0.5, 1.5)
+  unsigned h = seed * 2654435761u + 12345u;
+  for (int i = 0; i < n; ++i) {
+    h = h * 1664525u + 1013904223u;
+    x[(size_t)i * xs] = 0.5f + (float)(h >> 8) * (1.f / 16777216.f);
+  }
+  for (int iter = 0; iter < 2; ++iter) {
+    // forward: apply the row operations to the right-hand side (in x)
+    float act = x[0];
+    for (int i = 0; i < n - 1; ++i) {
+      const float r1 = x[(size_t)(i + 1) * xs];
+      if (!sw[i]) {
+        x[(size_t)i * xs] = act;
+        act = r1 - mul[i] * act;
+      } else {
+        x[(size_t)i * xs] = r1;
+        act = act - mul[i] * r1;
+      }
+    }
+    x[(size_t)(n - 1) * xs] = act;
+    // back substitution
+    float xn1 = 0.f, xn2 = 0.f, amax = 0.f;
+    for (int i = n - 1; i >= 0; --i) {
+      const float xi = (x[(size_t)i * xs] - u1[i] * xn1 - u2[i] * xn2) / u0[i];
+      x[(size_t)i * xs] = xi;
+      xn2 = xn1;
+      xn1 = xi;
+      amax = fmaxf(amax, fabsf(xi));
+    }
+    const float sc = amax > 0.f ? 1.f / amax : 1.f;
+    for (int i = 0; i < n; ++i) x[(size_t)i * xs] *= sc;
+    for (int o = 0; o < n_orth; ++o) {
+      const float* y = orth + o;
+      float dot = 0.f, yy = 0.f;
+      for (int i = 0; i < n; ++i) {
+        dot = fmaf(y[(size_t)i * xs], x[(size_t)i * xs], dot);
+        yy = fmaf(y[(size_t)i * xs], y[(size_t)i * xs], yy);
+      }
+      const float c = yy > 0.f ? dot / yy : 0.f;
+      for (int i = 0; i < n; ++i) x[(size_t)i * xs] -= c * y[(size_t)i * xs];
+    }
+  }
+  float nrm = 0.f;
+  for (int i = 0; i < n; ++i) nrm = fmaf(x[(size_t)i * xs], x[(size_t)i * xs], nrm);
+  const float sc = nrm > 0.f ? 1.f / sqrtf(nrm) : 0.f;
+  for (int i = 0; i < n; ++i) x[(size_t)i * xs] *= sc;
+}
+
+// Orthonormalise the k columns of Y (n x k, row stride ldy) by CholQR: S = Y^T Y,
+// S = R^T R (warp 0), Y <- Y R^-1.  Returns false if S is numerically singular.
+__device__ inline bool cta_cholqr(float* Y, int n, int k, int ldy, float* S, int* flag) {
+  const int tid = threadIdx.x;
+  cta_gemm(make_gemm(Y, lin(1), ldy, Y, lin(1), ldy, S, lin(k), lin(1), k, k, n));
+  if (tid == 0) *flag = 0;
+  __syncthreads();
+  const int nl = blockDim.x < 32 ? blockDim.x : 32;
+  if (tid < 32) {
+    for (int j = 0; j < k; ++j) {
+      const float sjj = S[j * k + j];
+      if (!(sjj > 1e-10f)) {
+        if (tid == 0) *flag = 1;
+        break;
+      }
+      const float rjj = sqrtf(sjj);
+      warp_sync();
+      for (int c = j + 1 + tid; c < k; c += nl) S[j * k + c] /= rjj;
+      if (tid == 0) S[j * k + j] = rjj;
+      warp_sync();
+      for (int c = j + 1 + tid; c < k; c += nl) {
+        const float rjc = S[j * k + c];
+        for (int i = j + 1; i <= c; ++i) S[i * k + c] -= S[j * k + i] * rjc;
+      }
+      warp_sync();
+    }
+  }
+  __syncthreads();
+  if (*flag) return false;
+  // Y <- Y R^-1, one row per thread
+  for (int i = tid; i < n; i += blockDim.x) {
+    float* y = Y + (size_t)i * ldy;
+    for (int t = 0; t < k; ++t) {
+      float v = y[t];
+      for (int s = 0; s < t; ++s) v -= y[s] * S[s * k + t];
+      y[t] = v / S[t * k + t];
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+// Modified Gram-Schmidt fallback (serial over columns, parallel over rows).
+__device__ inline void cta_mgs(float* Y, int n, int k, int ldy, double* red) {
+  for (int t = 0; t < k; ++t) {
+    for (int s = 0; s < t; ++s) {
+      double dot = 0.0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) dot += (double)Y[(size_t)i * ldy + s] * Y[(size_t)i * ldy + t];
+      dot = cta_sum(dot, red);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) Y[(size_t)i * ldy + t] -= (float)dot * Y[(size_t)i * ldy + s];
+      __syncthreads();
+    }
+    double nn = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) nn += (double)Y[(size_t)i * ldy + t] * Y[(size_t)i * ldy + t];
+    nn = cta_sum(nn, red);
+    const float sc = nn > 0.0 ? (float)(1.0 / sqrt(nn)) : 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) Y[(size_t)i * ldy + t] *= sc;
+    __syncthreads();
+  }
+}
+
+// Apply Q = H_0 ... H_{n-3} to Y (n x k):  Y <- Q Y.
+__device__ inline void cta_back_transform(const float* A, int n, int lda, const float* tau, float* Y, int k, int ldy,
+                                          float* cvec) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int g = nt / (k > 0 ? k : 1);
+  if (g > 32) g = 32;
+  int gp = 1;
+  while (gp * 2 <= g) gp *= 2;
+  g = gp;
+  const int ngroups = nt / g;
+  const int grp = tid / g, lig = tid % g;
+  const unsigned gmask = (g == 32) ? 0xffffffffu : (((1u << g) - 1u) << ((tid & 31) & ~(g - 1)));
+  int gx = 1;
+  while (gx * 2 <= k && gx * 2 <= nt) gx *= 2;
+  const int gy = nt / gx;
+  const int ux = tid % gx, uy = tid / gx;
+  for (int j = n - 3; j >= 0; --j) {
+    const float tj = tau[j];
+    if (tj == 0.f) continue;
+    const int m = n - j - 1;
+    for (int t = grp; t < k; t += ngroups) {
+      float s = 0.f;
+      for (int i = lig; i < m; i += g) {
+        const float vi = (i == 0) ? 1.f : A[(size_t)(j + 1 + i) * lda + j];
+        s = fmaf(vi, Y[(size_t)(j + 1 + i) * ldy + t], s);
+      }
+#ifndef VMC_HOST_EMULATION
+      for (int o = g / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, g);
+#endif
+      if (lig == 0) cvec[t] = tj * s;
+    }
+    __syncthreads();
+    for (int i = uy; i < m; i += gy) {
+      const float vi = (i == 0) ? 1.f : A[(size_t)(j + 1 + i) * lda + j];
+      float* yrow = Y + (size_t)(j + 1 + i) * ldy;
+      for (int t = ux; t < k; t += gx) yrow[t] -= vi * cvec[t];
+    }
+    __syncthreads();
+  }
+  (void)gmask;
+}
+
+// Scratch for cta_sym_topk (all pointers into shared or global memory).
+struct EigScratch {
+  float *d, *e, *e2, *tau, *v, *p, *lam, *cvec, *part;
+  float* S;                // k*k
+  float* lu;               // k * 4 * n
+  unsigned char* sw;       // k * n
+  int* flag;
+};
+
+// Y (n x k, row stride ldy) <- orthonormal basis of the dominant k-dimensional
+// invariant subspace of the symmetric matrix G (destroyed).  lam[0..kk-1]
+// receives the kk = min(k+1, n) largest eigenvalues.
+__device__ inline void cta_sym_topk(float* G, int n, int ldg, int k, float* Y, int ldy, const EigScratch& w,
+                                    double* red) {
+  cta_tridiagonalize(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);
+  const int kk = k + 1 <= n ? k + 1 : n;
+  const float tnorm = cta_top_eigenvalues(w.d, w.e, w.e2, n, kk, w.lam);
+  for (int t = threadIdx.x; t < k; t += blockDim.x) {
+    float* lu = w.lu + (size_t)t * 4 * n;
+    tri_inverse_iteration(w.d, w.e, n, w.lam[t], tnorm, Y + t, ldy, lu, lu + n, lu + 2 * n, lu + 3 * n,
+                          w.sw + (size_t)t * n, 977u * (unsigned)t + 1u);
+  }
+  __syncthreads();
+  // clusters of nearly equal eigenvalues: re-iterate serially, keeping each
+  // vector orthogonal to the earlier members of its cluster
+  if (threadIdx.x == 0) {
+    int start = 0;
+    for (int t = 1; t < k; ++t) {
+      if (w.lam[t - 1] - w.lam[t] < 1e-3f * tnorm) {
+        float* lu = w.lu + (size_t)t * 4 * n;
+        tri_inverse_iteration(w.d, w.e, n, w.lam[t], tnorm, Y + t, ldy, lu, lu + n, lu + 2 * n, lu + 3 * n,
+                              w.sw + (size_t)t * n, 977u * (unsigned)t + 1u, Y + start, t - start);
+      } else {
+        start = t;
+      }
+    }
+  }
+  __syncthreads();
+  bool ok = cta_cholqr(Y, n, k, ldy, w.S, w.flag);
+  if (ok) ok = cta_cholqr(Y, n, k, ldy, w.S, w.flag);
+  if (!ok) cta_mgs(Y, n, k, ldy, red);
+  cta_back_transform(G, n, ldg, w.tau, Y, k, ldy, w.cvec);
+}
+
+}  // namespace vmc

@@ -46,6 +46,7 @@ class SweepResult:
     logamp: torch.Tensor         # (n,) float64
     sign: torch.Tensor           # (n,) float64
     margin: torch.Tensor | None  # (n,) float32
+    gap: torch.Tensor | None = None  # (n,) float32 smallest relative eigen-gap at a cut
 
 
 class PEPSEngine:
@@ -183,16 +184,17 @@ class PEPSEngine:
                 logamp=torch.empty(n, dtype=torch.float64, device=dev),
                 sign=torch.empty(n, dtype=torch.float64, device=dev),
                 margin=torch.empty(n, dtype=torch.float32, device=dev) if want_margin else None,
+                gap=torch.empty(n, dtype=torch.float32, device=dev) if want_margin else None,
             )
         ws = self.workspace(n)
         st = self.lib.vmc_peps_sweep(self._plan, self._stream(), _vp(tensors), _vp(c), _vp(u), _vp(deltas), n,
                                      _vp(cache), int(bool(full_gradient)), _vp(out.O), _vp(out.p), _vp(out.E),
-                                     _vp(out.logamp), _vp(out.sign), _vp(out.margin), _vp(ws), ws.numel(),
-                                     _vp(self._status))
+                                     _vp(out.logamp), _vp(out.sign), _vp(out.margin), _vp(out.gap), _vp(ws),
+                                     ws.numel(), _vp(self._status))
         _abi.check(self.lib, st, "vmc_peps_sweep")
         return out
 
-    def amp_grad(self, tensors, samples, full_gradient=False, want_O=True):
+    def amp_grad(self, tensors, samples, full_gradient=False, want_O=True, want_gap=False):
         self._check_tensors(tensors)
         c = self._configs(samples)
         n = c.shape[0]
@@ -201,11 +203,14 @@ class PEPSEngine:
         O = torch.empty((n, np_), dtype=torch.float32, device=dev) if want_O else None
         logamp = torch.empty(n, dtype=torch.float64, device=dev)
         sign = torch.empty(n, dtype=torch.float64, device=dev)
+        gap = torch.empty(n, dtype=torch.float32, device=dev) if want_gap else None
         ws = self.workspace(n)
         st = self.lib.vmc_peps_amp_grad(self._plan, self._stream(), _vp(tensors), _vp(c), n,
-                                        int(bool(full_gradient)), _vp(O), _vp(logamp), _vp(sign), _vp(ws),
-                                        ws.numel(), _vp(self._status))
+                                        int(bool(full_gradient)), _vp(O), _vp(logamp), _vp(sign), _vp(gap),
+                                        _vp(ws), ws.numel(), _vp(self._status))
         _abi.check(self.lib, st, "vmc_peps_amp_grad")
+        if want_gap:
+            return logamp, sign, O, gap
         return logamp, sign, O
 
     def local_energy(self, tensors, samples, logamp, sign):
