@@ -1,0 +1,68 @@
+"""Helpers shared by the tests: seeded models and engine-vs-oracle runners."""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import peps as oracle
+from vmc_gb300.operators import heisenberg, transverse_field_ising
+from vmc_gb300.synthetic import initial_configs, random_tensors, uniform_stream
+
+
+def uniform_init_tensors(shape, bond_dim, phys_dim=2, seed=0):
+    """The reference's initialiser: i.i.d. uniform [0, 1) entries (src/vmc/utils/utils.py:22-47)."""
+    rng = np.random.default_rng(seed)
+    n_rows, n_cols = shape
+    return [[rng.random((phys_dim,) + oracle.PEPS.site_dims(r, c, n_rows, n_cols, bond_dim))
+             for c in range(n_cols)] for r in range(n_rows)]
+
+
+def fp32(tensors):
+    return [[np.asarray(t, dtype=np.float32).astype(np.float64) for t in row] for row in tensors]
+
+
+def oracle_strategy(name, chi):
+    return {"NoTruncation": lambda: oracle.NoTruncation(), "ZipUp": lambda: oracle.ZipUp(chi),
+            "DensityMatrix": lambda: oracle.DensityMatrix(chi)}[name]()
+
+
+def hamiltonian(kind, shape):
+    return heisenberg(shape) if kind == "heisenberg" else transverse_field_ising(shape)
+
+
+def oracle_sweep(tensors, shape, bond_dim, strategy, chi, operator, configs, uniforms, full_gradient=False,
+                 deltas=None):
+    """One transition + estimate of the FP64 oracle; returns (configs', ctx, LocalEstimates)."""
+    model = oracle.PEPS(tensors, shape, bond_dim, phys_dim=np.asarray(tensors[0][0]).shape[0],
+                        strategy=oracle_strategy(strategy, chi))
+    init, trans, est = oracle.build_mc_kernels(model, operator, full_gradient=full_gradient)
+    cfg = np.asarray(configs, dtype=np.int64)
+    cache = init(tensors, cfg)
+    c2, ctx = trans(tensors, cfg, uniforms, cache, deltas)
+    _, le = est(tensors, c2, ctx)
+    return c2, ctx, le
+
+
+def make_case(shape, bond_dim, n_chains, seed=0, phys_dim=2):
+    T = random_tensors(shape, bond_dim, phys_dim, seed=seed)
+    n_sites = shape[0] * shape[1]
+    cfg = initial_configs(n_chains, n_sites, phys_dim, seed=seed)
+    u = next(uniform_stream(n_chains, n_sites, seed=seed))
+    return T, cfg, u
+
+
+# Tolerances of the FP32 engine against the FP64 oracle.  Without active
+# truncation the engine is at the FP32 rounding level.  With truncation the
+# kept subspace at a cut moves by ~eps_fp32 / (relative singular-value gap),
+# so a few ill-conditioned samples sit far above the median.
+EXACT_TOL = 2e-5
+TRUNC_MEDIAN_TOL = 2e-5
+TRUNC_MAX_TOL = 2e-3
+
+
+def assert_parity(rel_errors, truncating):
+    rel_errors = np.asarray(rel_errors, dtype=np.float64)
+    if not truncating:
+        assert np.max(rel_errors) < EXACT_TOL, np.max(rel_errors)
+    else:
+        assert np.median(rel_errors) < TRUNC_MEDIAN_TOL, np.median(rel_errors)
+        assert np.max(rel_errors) < TRUNC_MAX_TOL, np.max(rel_errors)

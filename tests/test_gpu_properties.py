@@ -1,0 +1,83 @@
+"""Full-size (8x8, D=4, chi=16, 4096 chains) size-independent properties of the CUDA engine.
+
+The oracle cannot run 4096 config-2 chains in seconds, so the full workload is
+checked through properties that hold exactly (or to truncation accuracy):
+  * with every uniform u = 0 each proposal with psi' != 0 is accepted, so one
+    sweep flips every site (bit-exact);
+  * two runs on the same inputs are bitwise identical (determinism);
+  * psi is linear in each site tensor, so sum(A[s] * O) per site equals the
+    row-r amplitude over the transition amplitude (1 up to truncation error);
+  * every output is finite and the device status word stays clear.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from vmc_gb300.engine import PEPSEngine
+from vmc_gb300.lowering import pack_tensors, params_per_site
+from vmc_gb300.operators import heisenberg
+from vmc_gb300.synthetic import initial_configs, random_tensors, uniform_stream
+
+pytestmark = pytest.mark.gpu
+
+SHAPE, D, CHI, N = (8, 8), 4, 16, 4096
+
+
+@pytest.fixture(scope="module")
+def full_case(cuda_device):
+    T = random_tensors(SHAPE, D, seed=0)
+    eng = PEPSEngine(SHAPE, D, CHI, 2, "ZipUp", operator=heisenberg(SHAPE), device=cuda_device)
+    tens = torch.from_numpy(pack_tensors(T)).to(cuda_device)
+    cfg = torch.from_numpy(initial_configs(N, 64, seed=0)).to(cuda_device)
+    u = torch.from_numpy(next(uniform_stream(N, 64, seed=0))).to(cuda_device)
+    return eng, T, tens, cfg, u
+
+
+def _sweep(eng, tens, cfg, u):
+    c = cfg.clone()
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, u, cache)
+    torch.cuda.synchronize()
+    eng.raise_on_status()
+    return res
+
+
+def test_zero_uniforms_flip_every_site(full_case):
+    eng, _, tens, cfg, _ = full_case
+    res = _sweep(eng, tens, cfg, torch.zeros_like(full_case[4]))
+    assert torch.equal(res.configs, 1 - cfg)
+
+
+def test_bitwise_deterministic(full_case):
+    eng, _, tens, cfg, u = full_case
+    a = _sweep(eng, tens, cfg, u)
+    b = _sweep(eng, tens, cfg, u)
+    assert torch.equal(a.configs, b.configs)
+    assert torch.equal(a.E, b.E) and torch.equal(a.O, b.O) and torch.equal(a.logamp, b.logamp)
+
+
+def test_outputs_finite_and_linear_in_each_site(full_case):
+    eng, T, tens, cfg, u = full_case
+    res = _sweep(eng, tens, cfg, u)
+    assert torch.isfinite(res.E).all() and torch.isfinite(res.O).all() and torch.isfinite(res.logamp).all()
+    # sum_{u,d,l,r} A[r][c][s] * O[r][c] = psi_row(r) / psi ~ 1
+    pps = params_per_site(SHAPE, D)
+    cfg_new = res.configs
+    off = 0
+    devs = []
+    for site in range(64):
+        r, c = divmod(site, 8)
+        A = torch.from_numpy(np.asarray(T[r][c], dtype=np.float32)).to(cfg.device).reshape(2, -1)
+        o = res.O[:, off:off + pps[site]]
+        a_sel = A[cfg_new[:, site].long()]
+        devs.append(((a_sel * o).sum(1).double() - 1).abs())
+        off += pps[site]
+    dev = torch.stack(devs)
+    assert float(dev.median()) < 1e-3
+    assert float(dev.max()) < 0.2
+    # configs changed on roughly half the sites (random uniforms, |psi'|^2/|psi|^2 ~ O(1))
+    frac = (res.configs != cfg).double().mean().item()
+    assert 0.2 < frac < 0.8
+    assert res.p.shape == (N, sum(pps))

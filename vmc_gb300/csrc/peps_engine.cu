@@ -22,6 +22,7 @@
 #include <cstdlib>
 
 #include "device_common.cuh"
+#include "phase_timers.cuh"
 #include "truncation.cuh"
 #include "../../include/vmc_gb300.h"
 
@@ -42,30 +43,6 @@ constexpr long long kMaxArenaSmemBytes = 96 * 1024;
 enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4 };
 enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3 };
 
-// Optional per-phase cycle counters (build with -DVMC_PHASE_TIMERS); thread 0
-// of every CTA accumulates clock64() deltas.  Off in the product build.
-enum Phase { PH_T_RENV = 0, PH_T_METRO, PH_T_ZIP, PH_JACOBI, PH_E_RENV, PH_E_LEFT, PH_E_VERT, PH_B_ZIP, PH_CHAIN,
-             PH_COUNT };
-#if defined(VMC_PHASE_TIMERS) && !defined(VMC_HOST_EMULATION)
-__device__ unsigned long long g_phase[PH_COUNT];
-#define VMC_TSTART(v) long long v = clock64()
-#define VMC_TSTOP(v, ph) \
-  do { if (threadIdx.x == 0) atomicAdd(&g_phase[ph], (unsigned long long)(clock64() - (v))); } while (0)
-#elif defined(VMC_PHASE_TIMERS) && defined(VMC_HOST_EMULATION)
-}  // namespace vmc
-#include <chrono>
-namespace vmc {
-unsigned long long g_phase[PH_COUNT];
-inline long long host_ns() {
-  return std::chrono::duration_cast<std::chrono::nanoseconds>(
-             std::chrono::steady_clock::now().time_since_epoch()).count();
-}
-#define VMC_TSTART(v) long long v = host_ns()
-#define VMC_TSTOP(v, ph) (g_phase[ph] += (unsigned long long)(host_ns() - (v)))
-#else
-#define VMC_TSTART(v) (void)0
-#define VMC_TSTOP(v, ph) (void)0
-#endif
 
 // Device-side plan: scalars plus device pointers into one allocation.
 struct DevPlan {
@@ -75,6 +52,8 @@ struct DevPlan {
   int nmax, kmax;         // largest truncation matrix side / kept bond
   int trunc_method;       // 0: Gram + tridiagonal eigensolver, 1: one-sided Jacobi
   int arena_in_smem;      // truncation arena in dynamic shared memory
+  int mat_in_smem;        // theta matrix inside the arena (else in a separate global slot region)
+  int threads;            // CTA size of the fused kernel
   long long arena_floats;
   int scr1;               // size of one 1-row GEMM intermediate (floats)
   int vchunk, vbuf;       // vertical-energy chunk (bond values) and buffer size (floats)
@@ -133,7 +112,8 @@ __device__ inline Slot make_slot(const DevPlan& P, float* base) {
   s.lenv = p; p += al64((long long)(P.d + 1) * P.ES);
   s.r2 = p; p += al64((long long)P.C * P.E2S);
   for (int i = 0; i < 2; ++i) { s.l2[i] = p; p += al64(P.E2S); }
-  s.arena = p; p += P.arena_in_smem ? 0 : al64(P.arena_floats);
+  s.arena = p; p += P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.nmax * (P.nmax | 1)))
+                                    : al64(P.arena_floats);
   for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
   return s;
 }
@@ -246,11 +226,16 @@ struct Arena {
   EigScratch eig;
 };
 
-__device__ inline Arena make_arena(const DevPlan& P, float* base) {
+__device__ inline Arena make_arena(const DevPlan& P, float* base, float* global_mat) {
   Arena a;
   const int nmax = P.nmax, ld = P.nmax | 1, kmax = P.kmax;
   float* p = base;
-  a.mat = p; p += al64((long long)nmax * ld);
+  if (P.mat_in_smem) {
+    a.mat = p;
+    p += al64((long long)nmax * ld);
+  } else {
+    a.mat = global_mat;
+  }
   a.G = p; p += al64((long long)nmax * ld);
   a.Y = p; p += al64((long long)nmax * (P.trunc_method == 1 ? ld : kmax));
   a.eig.S = p; p += al64((long long)kmax * kmax);
@@ -264,7 +249,7 @@ __device__ inline Arena make_arena(const DevPlan& P, float* base) {
   a.eig.p = p; p += al64(nmax);
   a.eig.lam = p; p += al64(nmax + 1);
   a.eig.cvec = p; p += al64(nmax);
-  a.eig.part = p; p += 64;
+  a.eig.part = p; p += al64(nmax + 64);
   a.eig.flag = reinterpret_cast<int*>(p); p += 64;
   return a;
 }
@@ -273,7 +258,7 @@ __host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_
   const int ld = nmax | 1;
   return 2 * al64((long long)nmax * ld) + al64((long long)nmax * (trunc_method == 1 ? ld : kmax)) +
          al64((long long)kmax * kmax) + al64(4LL * kmax * nmax) + al64(((long long)kmax * nmax + 3) / 4) +
-         7 * al64(nmax) + al64(nmax + 1) + 128;
+         7 * al64(nmax) + al64(nmax + 1) + al64(nmax + 64) + 64;
 }
 
 // Select the kout largest of sig[0..nv) into sh.sel (ties by index).
@@ -419,6 +404,7 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
       const bool rows_side = mrows <= ncols;
       const int nG = rows_side ? mrows : ncols;
       const int ldg = nG | 1;
+      VMC_TSTART(tg);
       if (rows_side) {
         // G = theta theta^T
         cta_gemm(make_gemm(mat, lin(ldm), 1, mat, lin(ldm), 1, ar.G, lin(ldg), lin(1), nG, nG, ncols));
@@ -426,6 +412,7 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
         // G = theta^T theta
         cta_gemm(make_gemm(mat, lin(1), ldm, mat, lin(1), ldm, ar.G, lin(ldg), lin(1), nG, nG, mrows));
       }
+      VMC_TSTOP(tg, PH_GRAM);
       cta_sym_topk(ar.G, nG, ldg, kout, ar.Y, kout, ar.eig, sh.red);
       if (threadIdx.x == 0 && kout < nG) {
         const float lk = ar.eig.lam[kout - 1], lk1 = ar.eig.lam[kout];
@@ -453,8 +440,10 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
         __syncthreads();
       }
       // carry'[k'][w][r'] = sum_i U[i][k'] theta[i][(r',w)]
+      VMC_TSTART(tc);
       cta_gemm(make_gemm(out, lin(1), kout, mat, lin(1), ldm, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols,
                          mrows));
+      VMC_TSTOP(tc, PH_CARRY);
       VMC_TSTOP(tj, PH_JACOBI);
     }
     // renormalise the new tensor
@@ -690,6 +679,7 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
                                                const int* bbond, int r, const int* sp0, const int* sp1,
                                                double vscale, float* const* vb) {
   const int C = P.C, d = P.d;
+  VMC_TSTART(tvr);
   // R2_{C-1} = [1]
   if (threadIdx.x == 0) S.r2[(size_t)(C - 1) * P.E2S] = 1.f;
   __syncthreads();
@@ -721,6 +711,8 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
                          lin(1), na * Lb * Lb1, ba, V1 * bb));
     }
   }
+  VMC_TSTOP(tvr, PH_V_RIGHT);
+  VMC_TSTART(tvl);
   float* Lc = S.l2[0];
   float* Ln = S.l2[1];
   if (threadIdx.x == 0) Lc[0] = 1.f;
@@ -789,6 +781,7 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
       Ln = t;
     }
   }
+  VMC_TSTOP(tvl, PH_V_LEFT);
   return energy;
 }
 
@@ -825,7 +818,7 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
 #else
   extern __shared__ float dyn_smem[];
 #endif
-  const Arena ar = make_arena(P, P.arena_in_smem ? dyn_smem : S.arena);
+  const Arena ar = make_arena(P, P.arena_in_smem ? dyn_smem : S.arena, S.arena);
   if (P.onerow_in_smem) {
     // the 1-row environment GEMM intermediates are never live during a truncation
     for (int i = 0; i < 4; ++i) S.scr[3 + i] = dyn_smem + (size_t)i * P.scr1;
@@ -1128,7 +1121,10 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
   if (phys_dim > kMaxD) return VMC_ERR_UNSUPPORTED;
   if (dtype != VMC_DTYPE_F32) return VMC_ERR_UNSUPPORTED;
-  if (strategy == VMC_STRATEGY_VARIATIONAL) return VMC_ERR_UNSUPPORTED;
+  // DensityMatrix (strategy.py:153-176) carries V_k^H without the singular
+  // values, so its next cut truncates an unweighted theta: not the ZipUp
+  // product, and ill-defined for rank-deficient theta.  Not implemented.
+  if (strategy == VMC_STRATEGY_VARIATIONAL || strategy == VMC_STRATEGY_DENSITY_MATRIX) return VMC_ERR_UNSUPPORTED;
   if (strategy < 0 || strategy > VMC_STRATEGY_VARIATIONAL) return VMC_ERR_INVALID;
   vmc_plan* pl = new (std::nothrow) vmc_plan();
   if (!pl) return VMC_ERR_INVALID;
@@ -1211,34 +1207,45 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
     const char* tm = std::getenv("VMC_TRUNCATION");
     P.trunc_method = (tm && std::strcmp(tm, "jacobi") == 0) ? 1 : 0;
   }
-  P.arena_floats = arena_floats(P.nmax, P.kmax, P.trunc_method);
-  P.arena_in_smem = P.arena_floats * 4 <= kMaxArenaSmemBytes ? 1 : 0;
+  {
+    const char* th = std::getenv("VMC_THREADS");
+    P.threads = th ? std::max(64, std::min(kThreads, std::atoi(th))) : kThreads;
+  }
+  long long budget = kMaxArenaSmemBytes;
+  if (const char* kb = std::getenv("VMC_SMEM_KB")) budget = std::max(0, std::atoi(kb)) * 1024LL;
+  const long long mat_floats = al64((long long)P.nmax * (P.nmax | 1));
+  const long long trunc_all = arena_floats(P.nmax, P.kmax, P.trunc_method);
+  P.arena_in_smem = 0;
+  P.mat_in_smem = 1;  // "theta lives inside the arena" (arena itself may be global)
+  P.arena_floats = trunc_all;
+  if (trunc_all * 4 <= budget) {
+    P.arena_in_smem = 1;
+    P.mat_in_smem = 1;
+  } else if ((trunc_all - mat_floats) * 4 <= budget && P.trunc_method == 0) {
+    P.arena_in_smem = 1;
+    P.mat_in_smem = 0;
+    P.arena_floats = trunc_all - mat_floats;
+  }
   P.scr1 = (int)al64(std::max(chimax * chimax * D * D, (long long)D * D * D * D));
   {
     // one bond value of a vertical-energy intermediate holds <= chimax * D^3 floats
     const long long unit = chimax * D * D * D;
     const long long nbuf = 1 + 2LL * d;
-    long long ch = (kMaxArenaSmemBytes / 4) / (nbuf * unit);
+    long long ch = (budget / 4) / (nbuf * unit);
     ch = std::max(1LL, std::min(ch, chimax));
     if (const char* vc = std::getenv("VMC_VCHUNK")) ch = std::max(1LL, std::min(ch, (long long)std::atoi(vc)));
     P.vchunk = (int)ch;
     P.vbuf = (int)al64(ch * unit);
-    P.vert_in_smem = nbuf * P.vbuf * 4 <= kMaxArenaSmemBytes ? 1 : 0;
-    if (!P.vert_in_smem) {
-      // global scratch buffers (SCR floats each) hold whole steps
-      P.vchunk = (int)chimax;
-      P.vbuf = (int)SCR;
-    }
+    P.vert_in_smem = (P.arena_in_smem && nbuf * P.vbuf * 4 <= budget) ? 1 : 0;
   }
   P.onerow_in_smem = 0;
-  if (P.arena_in_smem && std::max(P.arena_floats, 4LL * P.scr1) * 4 <= kMaxArenaSmemBytes) {
+  if (P.arena_in_smem && std::max(P.arena_floats, 4LL * P.scr1) * 4 <= budget) {
     P.onerow_in_smem = 1;
     P.arena_floats = std::max(P.arena_floats, 4LL * P.scr1);
   }
-  if (P.arena_in_smem && P.vert_in_smem) {
+  if (P.vert_in_smem) {
     P.arena_floats = std::max(P.arena_floats, (1 + 2LL * d) * P.vbuf);
   } else {
-    P.vert_in_smem = 0;
     P.vchunk = (int)chimax;
     P.vbuf = (int)SCR;
   }
@@ -1246,7 +1253,9 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   P.n_scr = 11 + 2 * kMaxD;
   P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + 3 * al64((long long)C * TS) +
                   al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
-                  2 * al64(E2S) + (P.arena_in_smem ? 0 : al64(P.arena_floats)) + (long long)P.n_scr * al64(SCR);
+                  2 * al64(E2S) +
+                  (P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.nmax * (P.nmax | 1))) : al64(P.arena_floats)) +
+                  (long long)P.n_scr * al64(SCR);
   P.cache_floats_per_chain = al64((long long)R * C * TS);
   if (chimax * D > kMaxVec) {
     delete pl;
@@ -1258,7 +1267,17 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
     vmc_plan_destroy(pl);
     return st;
   }
-  pl->slots_max = vmc_num_sms() * 4;
+  {
+    const size_t smem = P.arena_in_smem ? (size_t)P.arena_floats * 4 : 0;
+    int per_sm = 4;
+#ifndef VMC_HOST_EMULATION
+    if (smem > 48 * 1024) cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peps_kernel, P.threads, smem) == cudaSuccess && occ > 0)
+      per_sm = occ;
+#endif
+    pl->slots_max = vmc_num_sms() * per_sm;
+  }
   *out_plan = pl;
   return VMC_OK;
 }
@@ -1353,7 +1372,7 @@ static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float
       cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return VMC_ERR_CUDA;
 #endif
-  VMC_LAUNCH(peps_kernel, grid, kThreads, smem, stream, pl->dplan, mode, tensors, wsf, configs, uniforms, deltas, n,
+  VMC_LAUNCH(peps_kernel, grid, pl->hp.threads, smem, stream, pl->dplan, mode, tensors, wsf, configs, uniforms, deltas, n,
              static_cast<float*>(cache), full_gradient, out_O, out_p, out_E, logamp, sign, margin, gap, wsf, status);
   return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
 }

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "device_common.cuh"
+#include "phase_timers.cuh"
 
 namespace vmc {
 
@@ -101,8 +102,18 @@ __device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, fl
     float pv = 0.f;
     for (int i = rrow; i < m; i += nrow_thr) {
       const float* row = As + (size_t)i * lda;
-      float s = 0.f;
-      for (int l = rlane; l < m; l += rg) s = fmaf(row[l], v[l], s);
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+      int l = rlane;
+      for (; l + 3 * rg < m; l += 4 * rg) {
+        const float a0 = row[l], a1 = row[l + rg], a2 = row[l + 2 * rg], a3 = row[l + 3 * rg];
+        const float b0 = v[l], b1 = v[l + rg], b2 = v[l + 2 * rg], b3 = v[l + 3 * rg];
+        s0 = fmaf(a0, b0, s0);
+        s1 = fmaf(a1, b1, s1);
+        s2 = fmaf(a2, b2, s2);
+        s3 = fmaf(a3, b3, s3);
+      }
+      for (; l < m; l += rg) s0 = fmaf(row[l], v[l], s0);
+      float s = (s0 + s1) + (s2 + s3);
 #ifndef VMC_HOST_EMULATION
       for (int o = rg / 2; o > 0; o >>= 1) s += __shfl_xor_sync(rmask, s, o, rg);
 #endif
@@ -120,14 +131,31 @@ __device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, fl
     const float K = 0.5f * tj * ptv;
     // A_sub -= v w^T + w v^T, w = p - K v
     float s = 0.f;
-    for (int i = uy; i < m; i += gy) {
-      const float vi = v[i], wi = p[i] - K * vi;
-      float* arow = As + (size_t)i * lda;
-      for (int l = ux; l < m; l += gx) {
-        const float vl = v[l], wl = p[l] - K * vl;
-        const float nv = arow[l] - vi * wl - wi * vl;
-        arow[l] = nv;
-        if (l == 0 && i >= 2) s = fmaf(nv, nv, s);
+    // columns l = l0 + q*gx (q < 4) of this thread: v_l, w_l kept in registers
+    for (int l0 = ux; l0 < m; l0 += 4 * gx) {
+      float vl[4], wl[4];
+      int nl = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int l = l0 + q * gx;
+        vl[q] = l < m ? v[l] : 0.f;
+        wl[q] = l < m ? p[l] - K * vl[q] : 0.f;
+        nl += l < m;
+      }
+      for (int i = uy; i < m; i += gy) {
+        const float vi = v[i], wi = p[i] - K * vi;
+        float* arow = As + (size_t)i * lda;
+        float a[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = q < nl ? arow[l0 + q * gx] : 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (q < nl) {
+            const float nv = a[q] - vi * wl[q] - wi * vl[q];
+            arow[l0 + q * gx] = nv;
+            if (l0 + q * gx == 0 && i >= 2) s = fmaf(nv, nv, s);
+          }
+        }
       }
     }
     s = warp_sum_f(s);
@@ -148,6 +176,7 @@ __device__ __forceinline__ int sturm_count(const float* d, const float* e2, int 
   float q = d[0] - x;
   if (fabsf(q) < pivmin) q = -pivmin;
   int cnt = q < 0.f;
+#pragma unroll 4
   for (int i = 1; i < n; ++i) {
     q = (d[i] - x) - __fdividef(e2[i - 1], q);
     if (fabsf(q) < pivmin) q = -pivmin;
@@ -222,6 +251,7 @@ __device__ inline void tri_inverse_iteration(const float* d, const float* e, int
   const float tiny = 1.2e-7f * fmaxf(tnorm, 1e-30f);
   float al = d[0] - lam;
   float be = n > 1 ? e[0] : 0.f;
+#pragma unroll 4
   for (int i = 0; i < n - 1; ++i) {
     const float c = e[i];
     const float a1 = d[i + 1] - lam;
@@ -259,6 +289,7 @@ __device__ inline void tri_inverse_iteration(const float* d, const float* e, int
   for (int iter = 0; iter < 2; ++iter) {
     // forward: apply the row operations to the right-hand side (in x)
     float act = x[0];
+    #pragma unroll 4
     for (int i = 0; i < n - 1; ++i) {
       const float r1 = x[(size_t)(i + 1) * xs];
       if (!sw[i]) {
@@ -272,6 +303,7 @@ __device__ inline void tri_inverse_iteration(const float* d, const float* e, int
     x[(size_t)(n - 1) * xs] = act;
     // back substitution
     float xn1 = 0.f, xn2 = 0.f, amax = 0.f;
+    #pragma unroll 4
     for (int i = n - 1; i >= 0; --i) {
       const float xi = (x[(size_t)i * xs] - u1[i] * xn1 - u2[i] * xn2) / u0[i];
       x[(size_t)i * xs] = xi;
@@ -380,11 +412,20 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
     if (tj == 0.f) continue;
     const int m = n - j - 1;
     for (int t = grp; t < k; t += ngroups) {
-      float s = 0.f;
-      for (int i = lig; i < m; i += g) {
-        const float vi = (i == 0) ? 1.f : A[(size_t)(j + 1 + i) * lda + j];
-        s = fmaf(vi, Y[(size_t)(j + 1 + i) * ldy + t], s);
+      float s = 0.f, s1 = 0.f;
+      int i = lig;
+      if (i == 0) {
+        s = Y[(size_t)(j + 1) * ldy + t];
+        i += g;
       }
+      for (; i + g < m; i += 2 * g) {
+        const float a0 = A[(size_t)(j + 1 + i) * lda + j], a1 = A[(size_t)(j + 1 + i + g) * lda + j];
+        const float y0 = Y[(size_t)(j + 1 + i) * ldy + t], y1 = Y[(size_t)(j + 1 + i + g) * ldy + t];
+        s = fmaf(a0, y0, s);
+        s1 = fmaf(a1, y1, s1);
+      }
+      if (i < m) s = fmaf(A[(size_t)(j + 1 + i) * lda + j], Y[(size_t)(j + 1 + i) * ldy + t], s);
+      s += s1;
 #ifndef VMC_HOST_EMULATION
       for (int o = g / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, g);
 #endif
@@ -415,9 +456,14 @@ struct EigScratch {
 // receives the kk = min(k+1, n) largest eigenvalues.
 __device__ inline void cta_sym_topk(float* G, int n, int ldg, int k, float* Y, int ldy, const EigScratch& w,
                                     double* red) {
+  VMC_TSTART(t0);
   cta_tridiagonalize(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);
+  VMC_TSTOP(t0, PH_TRIDIAG);
+  VMC_TSTART(t1);
   const int kk = k + 1 <= n ? k + 1 : n;
   const float tnorm = cta_top_eigenvalues(w.d, w.e, w.e2, n, kk, w.lam);
+  VMC_TSTOP(t1, PH_BISECT);
+  VMC_TSTART(t2);
   for (int t = threadIdx.x; t < k; t += blockDim.x) {
     float* lu = w.lu + (size_t)t * 4 * n;
     tri_inverse_iteration(w.d, w.e, n, w.lam[t], tnorm, Y + t, ldy, lu, lu + n, lu + 2 * n, lu + 3 * n,
@@ -439,10 +485,16 @@ __device__ inline void cta_sym_topk(float* G, int n, int ldg, int k, float* Y, i
     }
   }
   __syncthreads();
-  bool ok = cta_cholqr(Y, n, k, ldy, w.S, w.flag);
-  if (ok) ok = cta_cholqr(Y, n, k, ldy, w.S, w.flag);
+  VMC_TSTOP(t2, PH_INVIT);
+  VMC_TSTART(t3);
+  // the vectors belong to distinct (or cluster-orthogonalised) eigenvalues and
+  // are already orthogonal to O(1e-4); one CholQR pass restores eps level
+  const bool ok = cta_cholqr(Y, n, k, ldy, w.S, w.flag);
   if (!ok) cta_mgs(Y, n, k, ldy, red);
+  VMC_TSTOP(t3, PH_CHOLQR);
+  VMC_TSTART(t4);
   cta_back_transform(G, n, ldg, w.tau, Y, k, ldy, w.cvec);
+  VMC_TSTOP(t4, PH_BACK);
 }
 
 }  // namespace vmc

@@ -45,9 +45,10 @@ class ZipUp(ContractionStrategy):
 
 
 class DensityMatrix(ContractionStrategy):
-    """strategy.py:64-71.  It keeps the top eigenvectors of theta^H theta, i.e.
-    the same truncated product U_k S_k V_k^H as ZipUp in a different bond gauge,
-    so the engine evaluates it with the ZipUp kernels."""
+    """strategy.py:64-71.  Keeps the top eigenvectors V_k of theta^H theta and
+    carries V_k^H (without the singular values) to the next site, so its
+    truncations differ from ZipUp's.  The engine does not implement it (the
+    plan returns VMC_ERR_UNSUPPORTED)."""
 
     name = "DensityMatrix"
 
@@ -63,8 +64,6 @@ class Variational(ContractionStrategy):
 
 
 def _engine_strategy(strategy):
-    if isinstance(strategy, DensityMatrix):
-        return "ZipUp", strategy.truncate_bond_dimension, 2
     if isinstance(strategy, Variational):
         return "Variational", strategy.truncate_bond_dimension, strategy.n_sweeps
     if isinstance(strategy, NoTruncation):
