@@ -1,0 +1,152 @@
+"""The FP64 SR layer (vmc_gb300.qgt / preconditioners, plain torch) against the oracle, and the
+multi-rank reductions with 2 gloo ranks on CPU."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+from oracle import peps as oracle
+from oracle import sr as osr
+from tests.helpers import uniform_init_tensors
+from vmc_gb300 import qgt as gq
+from vmc_gb300.distributed import gather_jacobian, global_energy, parameter_space_qgt, shard_chains
+from vmc_gb300.operators import LocalHamiltonian
+from vmc_gb300.preconditioners import DirectSolve, QRSolve, SRPreconditioner, reorder_updates
+
+
+class _Model:
+    """The attributes SRPreconditioner reads from a PEPS (shape, bond_dim, phys_dim, unpack)."""
+
+    def __init__(self, shape, D, d, tensors):
+        self.shape, self.bond_dim, self.phys_dim = shape, D, d
+        self.tensors = [[torch.as_tensor(t, dtype=torch.float32) for t in row] for row in tensors]
+
+    def unpack(self, flat):
+        out, off = [], 0
+        for row in self.tensors:
+            r = []
+            for t in row:
+                r.append(flat[off:off + t.numel()].reshape(t.shape))
+                off += t.numel()
+            out.append(r)
+        return out
+
+
+def _data(n=48, seed=0):
+    shape, D = (2, 3), 2
+    T = uniform_init_tensors(shape, D, seed=seed)
+    model = oracle.PEPS(T, shape, D, strategy=oracle.NoTruncation())
+    rng = np.random.default_rng(seed)
+    cfg = rng.integers(0, 2, size=(n, 6))
+    amps, grads, p = oracle.value_and_grad(model, cfg)
+    e = rng.standard_normal(n)
+    return shape, D, T, model, grads / amps[:, None], p, e
+
+
+@pytest.mark.parametrize("space", ["param", "sample"])
+def test_torch_sr_matches_oracle(space):
+    shape, D, T, om, o, p, e = _data()
+    sd = oracle.sliced_dims(om)
+    pps = oracle.params_per_site(om)
+    x_ref, m_ref = osr.sr_apply(o, p, e, pps=pps, sliced_dims=sd, n_samples=o.shape[0], diag_shift=1e-3,
+                            grad_factor=-1.0, space=osr.ParameterSpace() if space == "param" else osr.SampleSpace())
+    pre = SRPreconditioner(space=gq.ParameterSpace() if space == "param" else gq.SampleSpace(), diag_shift=1e-3)
+    model = _Model(shape, D, 2, T)
+    upd, metrics = pre.apply(model, model.tensors, torch.zeros((o.shape[0], 6)), torch.as_tensor(o),
+                             torch.as_tensor(p), torch.as_tensor(e), grad_factor=-1.0)
+    flat = torch.cat([u.reshape(-1) for row in upd for u in row]).double().numpy()
+    assert np.linalg.norm(flat - x_ref) / np.linalg.norm(x_ref) < 1e-5  # float32 output
+    assert abs(float(metrics["residual_error"]) - m_ref["residual_error"]) < 1e-8 * max(1.0, m_ref["residual_error"])
+
+
+def test_sample_space_gram_blocked_equals_dense():
+    shape, D, T, om, o, p, e = _data(64, 3)
+    sd = oracle.sliced_dims(om)
+    jac = gq.SlicedJacobian(torch.as_tensor(o), torch.as_tensor(p), sd, gq.SliceOrdering())
+    t16 = gq.QGT(jac, gq.SampleSpace(), n_blocks=16).to_dense()
+    ref = osr.to_dense(osr.SlicedJacobian(o, p, sd, osr.SliceOrdering()), osr.SampleSpace())
+    assert np.allclose(t16.numpy(), ref, rtol=1e-10, atol=1e-12)
+    s = gq.QGT(jac, gq.ParameterSpace()).to_dense()
+    ref_s = osr.to_dense(osr.SlicedJacobian(o, p, sd, osr.SliceOrdering()), osr.ParameterSpace())
+    assert np.allclose(s.numpy(), ref_s, rtol=1e-10, atol=1e-12)
+    v = np.random.default_rng(0).standard_normal(s.shape[0])
+    assert np.allclose((gq.QGT(jac, gq.ParameterSpace()) @ torch.as_tensor(v)).numpy(), ref_s @ v,
+                       rtol=1e-9, atol=1e-12)
+
+
+def test_reorder_and_qr_solve():
+    shape, D, T, om, o, p, e = _data(40, 5)
+    sd = oracle.sliced_dims(om)
+    pps = tuple(oracle.params_per_site(om))
+    x = np.arange(2 * sum(pps), dtype=np.float64)
+    assert np.array_equal(reorder_updates(gq.SliceOrdering(), torch.as_tensor(x), pps, sd).numpy(),
+                          osr.reorder_updates(osr.SliceOrdering(), x, pps, sd))
+    _, grads_full, _ = oracle.value_and_grad(om, np.random.default_rng(5).integers(0, 2, (40, 6)),
+                                             full_gradient=True)
+    dv = np.random.default_rng(6).standard_normal(40)
+    from vmc_gb300.preconditioners import _qr_solve
+
+    xq, mq = _qr_solve(gq.Jacobian(torch.as_tensor(grads_full)), torch.as_tensor(dv), None, True)
+    xr, mr = osr.qr_solve(osr.Jacobian(grads_full), dv)
+    assert mq["rank"] == mr["rank"]
+    assert np.allclose(xq.numpy(), xr, rtol=1e-8, atol=1e-10)
+
+
+def test_solvers_match():
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((20, 20))
+    a = a.T @ a + 0.3 * np.eye(20)
+    b = rng.standard_normal(20)
+    ref = np.linalg.solve(a, b)
+    A, B = torch.as_tensor(a), torch.as_tensor(b)
+    for f in (gq.solve_cholesky, gq.solve_svd, lambda m, r: gq.solve_cg(m, r, tol=1e-12)):
+        assert np.linalg.norm(f(A, B).numpy() - ref) / np.linalg.norm(ref) < 1e-8
+
+
+def test_shard_chains_cover_everything():
+    for n, ws in [(4096, 8), (100, 3), (5, 8)]:
+        spans = [shard_chains(n, ws, r) for r in range(ws)]
+        assert sum(c for _, c in spans) == n
+        assert all(spans[i][0] + spans[i][1] == spans[i + 1][0] for i in range(ws - 1))
+
+
+def _worker(rank, world, port, o, p, e, sd, out):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        start, count = shard_chains(o.shape[0], world, rank)
+        ol, pl, el = (torch.as_tensor(x[start:start + count]) for x in (o, p, e))
+        mean, var, n = global_energy(el)
+        jac = gq.SlicedJacobian(ol, pl, sd, gq.SliceOrdering())
+        S, m, n2 = parameter_space_qgt(jac)
+        go, gp = gather_jacobian(ol, pl)
+        if rank == 0:
+            out.put((float(mean), float(var), n, S.numpy(), go.numpy(), gp.numpy()))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_reduce_like_one_process():
+    shape, D, T, om, o, p, e = _data(50, 9)
+    sd = oracle.sliced_dims(om)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + (os.getpid() % 2000)
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, o, p, e, sd, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    res = q.get(timeout=120)
+    for pr in procs:
+        pr.join(timeout=60)
+        assert pr.exitcode == 0
+    mean, var, n, S, go, gp = res
+    assert n == 50 and abs(mean - e.mean()) < 1e-12 and abs(var - e.var()) < 1e-12
+    ref = osr.to_dense(osr.SlicedJacobian(o, p, sd, osr.SliceOrdering()), osr.ParameterSpace())
+    assert np.allclose(S, ref, rtol=1e-10, atol=1e-12)
+    assert np.array_equal(go, o) and np.array_equal(gp, p)

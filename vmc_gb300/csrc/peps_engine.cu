@@ -1271,7 +1271,7 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
     const size_t smem = P.arena_in_smem ? (size_t)P.arena_floats * 4 : 0;
     int per_sm = 4;
 #ifndef VMC_HOST_EMULATION
-    if (smem > 48 * 1024) cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 0) cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peps_kernel, P.threads, smem) == cudaSuccess && occ > 0)
       per_sm = occ;
@@ -1368,7 +1368,8 @@ static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float
   VMC_LAUNCH(permute_tensors_kernel, std::min(pl->hp.n_sites, 1024), kThreads, 0, stream, pl->dplan, tensors, wsf);
   const size_t smem = pl->hp.arena_in_smem ? (size_t)pl->hp.arena_floats * 4 : 0;
 #ifndef VMC_HOST_EMULATION
-  if (smem > 48 * 1024 &&
+  // static (~5 KB) + dynamic shared memory may exceed the 48 KB default: always opt in
+  if (smem > 0 &&
       cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return VMC_ERR_CUDA;
 #endif

@@ -1,0 +1,167 @@
+"""TDVP / VMC driver with Euler and RK4 integrators
+(API of src/vmc/drivers/tdvp.py:54-249 and integrators.py:45-144).
+
+State is the list-of-lists of site tensors; the derivative is the SR update
+computed from one engine sampling run (init_cache + n_steps fused sweeps).
+The engine evaluates real PEPS, so real-time evolution (grad factor -i, which
+makes the parameters complex) raises NotImplementedError.
+"""
+from __future__ import annotations
+
+import logging
+import math
+
+import torch
+
+from .kernels import build_mc_kernels
+from .preconditioners import SRPreconditioner
+from .sampling import _sample_counts, _trim_samples, make_mc_sampler
+
+logger = logging.getLogger(__name__)
+
+__all__ = ["TDVPDriver", "Integrator", "Euler", "RK4", "TimeUnit", "RealTimeUnit", "ImaginaryTimeUnit"]
+
+
+def _add_scaled(base, delta, scale):
+    """src/vmc/utils/utils.py:60-65."""
+    return [[b + scale * d for b, d in zip(rb, rd)] for rb, rd in zip(base, delta)]
+
+
+class Integrator:
+    """integrators.py:21-42."""
+
+    @staticmethod
+    def step(derivative_fn, state, t, dt, carry):  # pragma: no cover - abstract
+        raise NotImplementedError
+
+
+class Euler(Integrator):
+    """integrators.py:45-63."""
+
+    @staticmethod
+    def step(derivative_fn, state, t, dt, carry):
+        k, carry_next, aux = derivative_fn(state, t, carry)
+        return _add_scaled(state, k, dt), t + dt, carry_next, aux
+
+
+class RK4(Integrator):
+    """integrators.py:66-109."""
+
+    @staticmethod
+    def step(derivative_fn, state, t, dt, carry):
+        k1, c1, _ = derivative_fn(state, t, carry)
+        k2, c2, _ = derivative_fn(_add_scaled(state, k1, 0.5 * dt), t + 0.5 * dt, c1)
+        k3, c3, _ = derivative_fn(_add_scaled(state, k2, 0.5 * dt), t + 0.5 * dt, c2)
+        k4, c4, aux = derivative_fn(_add_scaled(state, k3, dt), t + dt, c3)
+        incr = [[(a + 2.0 * b + 2.0 * c + d) / 6.0 for a, b, c, d in zip(ra, rb, rc, rd)]
+                for ra, rb, rc, rd in zip(k1, k2, k3, k4)]
+        return _add_scaled(state, incr, dt), t + dt, c4, aux
+
+
+class TimeUnit:
+    """integrators.py:112-122."""
+
+    grad_factor = 1.0
+
+    def default_integrator(self):  # pragma: no cover - abstract
+        raise NotImplementedError
+
+
+class RealTimeUnit(TimeUnit):
+    """integrators.py:125-133: i d/dt psi = H psi."""
+
+    grad_factor = -1.0j
+
+    def default_integrator(self):
+        return RK4()
+
+
+class ImaginaryTimeUnit(TimeUnit):
+    """integrators.py:136-144: d/dt psi = -H psi."""
+
+    grad_factor = -1.0
+
+    def default_integrator(self):
+        return Euler()
+
+
+class TDVPDriver:
+    """tdvp.py:54-249 on the GB300 engine."""
+
+    def __init__(self, model, operator, *, preconditioner: SRPreconditioner, dt: float, t0: float = 0.0,
+                 time_unit: TimeUnit = RealTimeUnit(), integrator: Integrator | None = None, sampler_key=0,
+                 n_samples: int = 1, n_chains: int = 1, full_gradient: bool = False):
+        if isinstance(time_unit.grad_factor, complex):
+            raise NotImplementedError("real-time TDVP needs complex parameters; the engine evaluates real PEPS")
+        self._model = model
+        self.operator = operator
+        self.preconditioner = preconditioner
+        self.dt = float(dt)
+        self.t = float(t0)
+        self.step_count = 0
+        self.n_samples = int(n_samples)
+        self.n_chains = int(n_chains)
+        self.full_gradient = bool(full_gradient)
+        self.time_unit = time_unit
+        self.integrator = integrator or time_unit.default_integrator()
+        dev = model.device
+        self._gen = torch.Generator(device=dev)
+        self._gen.manual_seed(int(sampler_key))
+        self._tensors = [[t.clone() for t in row] for row in model.tensors]
+        self._sampler_configuration = torch.randint(0, model.phys_dim, (self.n_chains,) + model.shape,
+                                                    generator=self._gen, device=dev, dtype=torch.int32)
+        init_cache, transition, estimate = build_mc_kernels(model, operator, full_gradient=self.full_gradient)
+        self._init_cache = init_cache
+        self._mc_sampler = make_mc_sampler(transition, estimate)
+        self.residual_error = None
+        self.diag_shift_error = None
+        self.solve_time = None
+        self._loss_stats = None
+
+    def _time_derivative(self, tensors, t, carry):
+        """tdvp.py:113-163."""
+        gen, configs = carry
+        _, num_chains, chain_length, total = _sample_counts(self.n_samples, self.n_chains)
+        cache = self._init_cache(tensors, configs)
+        (configs, _, _), (hist, est) = self._mc_sampler(tensors, configs.reshape(num_chains, -1), gen, cache,
+                                                          n_steps=chain_length)
+        samples = _trim_samples(hist, total, self.n_samples)
+        o = _trim_samples(est.local_log_derivatives, total, self.n_samples)
+        e = _trim_samples(est.local_estimate, total, self.n_samples)
+        p = None if self.full_gradient else _trim_samples(est.active_slice_indices, total, self.n_samples)
+        self._model.tensors = tensors
+        updates, metrics = self.preconditioner.apply(self._model, tensors, samples, o, p, e,
+                                                     grad_factor=self.time_unit.grad_factor)
+        return updates, (gen, configs), (e, metrics)
+
+    def run(self, T: float) -> None:
+        """tdvp.py:205-237."""
+        duration = float(T)
+        assert duration > 0.0, f"T must be positive, got {duration}"
+        n_steps = int(round(duration / self.dt))
+        eps = 1e-12 * max(1.0, abs(duration), abs(self.dt))
+        assert abs(duration - n_steps * self.dt) <= eps, f"T={duration} must be an integer multiple of dt={self.dt}"
+        assert n_steps > 0
+        carry = (self._gen, self._sampler_configuration.reshape(self.n_chains, -1))
+        e = None
+        metrics = {}
+        for _ in range(n_steps):
+            self._tensors, self.t, carry, (e, metrics) = self.integrator.step(
+                self._time_derivative, self._tensors, self.t, self.dt, carry)
+            logger.debug("E_mean=%s", float(e.mean()))
+        self._sampler_configuration = carry[1]
+        self._model.tensors = self._tensors
+        self.step_count += n_steps
+        mean = e.mean()
+        var = e.var(unbiased=False)
+        self._loss_stats = {"mean": float(mean), "variance": float(var),
+                            "error_of_mean": float(math.sqrt(float(var) / e.numel()))}
+        self.residual_error = metrics.get("residual_error")
+
+    @property
+    def energy(self):
+        return self._loss_stats
+
+    @property
+    def model(self):
+        return self._model

@@ -1,0 +1,162 @@
+"""SR / TDVP preconditioner on the GPU in FP64
+(API of src/vmc/preconditioners/preconditioners.py:41-330)."""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import Callable
+
+import torch
+
+from .lowering import params_per_site
+from .qgt import (
+    QGT,
+    Jacobian,
+    ParameterSpace,
+    SampleSpace,
+    SiteOrdering,
+    SliceOrdering,
+    SlicedJacobian,
+    adjoint_matvec,
+    jacobian_mean,
+    solve_cg,
+    solve_cholesky,
+    solve_svd,
+)
+
+__all__ = ["DirectSolve", "QRSolve", "SRPreconditioner", "reorder_updates", "solve_cholesky", "solve_svd",
+           "solve_cg"]
+
+
+@dataclass(frozen=True)
+class DirectSolve:
+    """preconditioners.py:41-45."""
+
+    solver: Callable = solve_cholesky
+
+
+@dataclass(frozen=True)
+class QRSolve:
+    """preconditioners.py:48-53 (ParameterSpace and full Jacobian only, like the reference)."""
+
+    rcond: float | None = None
+    min_norm: bool = True
+
+
+def reorder_updates(ordering, updates, pps, sliced_dims):
+    """preconditioners.py:61-97: slice-major -> site-major parameter order."""
+    if isinstance(ordering, SiteOrdering):
+        return updates
+    total = sum(pps)
+    perm = []
+    off = 0
+    for site, n in enumerate(pps):
+        for k in range(sliced_dims[site]):
+            base = k * total + off
+            perm.extend(range(base, base + n))
+        off += n
+    return updates[torch.as_tensor(perm, device=updates.device)]
+
+
+def _direct_solve(space, jac, dv, diag_shift, solver):
+    """preconditioners.py:117-152."""
+    qgt = QGT(jac, space)
+    S = qgt.to_dense()
+    mat = S + diag_shift * torch.eye(S.shape[0], dtype=S.dtype, device=S.device)
+    if isinstance(space, ParameterSpace):
+        rhs = adjoint_matvec(jac, dv)
+        x = solver(mat, rhs)
+        res = torch.linalg.norm(S @ x - rhs) ** 2 / torch.linalg.norm(rhs) ** 2
+        return x, {"residual_error": res}
+    y = solver(mat, dv)
+    x = adjoint_matvec(jac, y)
+    res = torch.linalg.norm(S @ y - dv) ** 2 / torch.linalg.norm(dv) ** 2
+    return x, {"residual_error": res}
+
+
+def _qr_solve(jac: Jacobian, dv, rcond, min_norm):
+    """preconditioners.py:166-214: column-pivoted QR of the centred full Jacobian (diag shift unused)."""
+    import numpy as np
+    import scipy.linalg as sla
+
+    # torch has no column-pivoted QR; this branch runs LAPACK geqp3 on the host in FP64.
+    O = _to_np(jac.O)
+    oc = O - O.mean(axis=0)
+    q, r, piv = sla.qr(oc, mode="economic", pivoting=True)
+    dvn = _to_np(dv)
+    y = q.conj().T @ dvn
+    sv = np.linalg.svd(r, compute_uv=False)
+    tol = (max(r.shape) * np.finfo(r.dtype).eps if rcond is None else rcond) * (sv.max() if sv.size else 0)
+    rank = int(np.sum(sv > tol))
+    n_red = r.shape[1]
+    n2 = n_red - rank
+    x = np.zeros(n_red, dtype=np.result_type(oc.dtype, dvn.dtype))
+    if rank:
+        r11, r12, y1 = r[:rank, :rank], r[:rank, rank:], y[:rank]
+        if min_norm and n2 > 0:
+            a = sla.solve_triangular(r11, y1, lower=False)
+            b = sla.solve_triangular(r11, r12, lower=False)
+            x2 = sla.solve(b.conj().T @ b + np.eye(n2), b.conj().T @ a, assume_a="pos")
+            x1 = a - b @ x2
+        else:
+            x1 = sla.solve_triangular(r11, y1, lower=False)
+            x2 = np.zeros(n2, dtype=x.dtype)
+        x[piv] = np.concatenate([x1, x2])
+    rhs = oc.conj().T @ dvn
+    resid = oc.conj().T @ (oc @ x) - rhs
+    dev = jac.O.device
+    return torch.as_tensor(x, device=dev), {"residual_error": float(np.linalg.norm(resid) ** 2 /
+                                                                   np.linalg.norm(rhs) ** 2), "rank": rank}
+
+
+def _to_np(t):
+    return t.detach().to(torch.complex128 if t.is_complex() else torch.float64).cpu().numpy()
+
+
+class SRPreconditioner:
+    """preconditioners.py:244-330."""
+
+    def __init__(self, space=ParameterSpace(), strategy=DirectSolve(), diag_shift: float = 1e-2,
+                 gauge_config=None, ordering=SliceOrdering()):
+        self.space = space
+        self.strategy = strategy
+        self.diag_shift = float(diag_shift)
+        self.gauge_config = gauge_config
+        self.ordering = ordering
+        self.uses_local_energies = True
+        self._metrics = {}
+
+    @property
+    def residual_error(self):
+        return self._metrics.get("residual_error")
+
+    def apply(self, model, params, samples, o, p, local_energies, *, grad_factor=1.0):
+        """Returns (updates as a list of per-site tensors shaped like model.tensors, metrics)."""
+        if self.gauge_config is not None:
+            from .gauge import compute_gauge_projection
+
+            compute_gauge_projection(self.gauge_config, model, params)
+        e = local_energies.reshape(-1).to(torch.float64)
+        n_samples = samples.shape[0]
+        dv = (e - e.mean()) / n_samples
+        if isinstance(grad_factor, complex) and grad_factor.imag != 0:
+            dv = dv.to(torch.complex128) * grad_factor
+        else:
+            dv = dv * float(getattr(grad_factor, "real", grad_factor))
+        pps = tuple(params_per_site(model.shape, model.bond_dim))
+        sd = (model.phys_dim,) * (model.shape[0] * model.shape[1])
+        jac = Jacobian(o) if p is None else SlicedJacobian(o, p, sd, self.ordering)
+        if isinstance(self.strategy, DirectSolve):
+            x, metrics = _direct_solve(self.space, jac, dv, self.diag_shift, self.strategy.solver)
+        else:
+            if p is not None:
+                raise NotImplementedError("QRSolve not supported for SlicedJacobian")
+            if isinstance(self.space, SampleSpace):
+                raise NotImplementedError("QRSolve not supported for SampleSpace")
+            x, metrics = _qr_solve(jac, dv, self.strategy.rcond, self.strategy.min_norm)
+        if p is not None:
+            x = reorder_updates(self.ordering, x, pps, sd)
+        if not (isinstance(grad_factor, complex) and grad_factor.imag != 0):
+            x = 2.0 * x.real  # real parameters: preconditioners.py:322-329
+        self._metrics = metrics
+        return model.unpack(x.to(torch.float32)), metrics

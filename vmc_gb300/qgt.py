@@ -1,0 +1,198 @@
+"""Quantum geometric tensor and sliced Jacobian on the GPU in FP64
+(API of src/vmc/qgt/jacobian.py:21-139, qgt.py:36-223, solvers.py:16-37).
+
+The log-derivatives O come from the engine as FP32 (n_samples, n_params);
+every contraction here promotes to FP64 on the device.  The sliced ("small-o")
+Jacobian stores, per sample, only the active slice of each site; slice k of
+the expanded Jacobian is where(p == k, o, 0) (jacobian.py:56-93).
+
+The dense builds accumulate over column blocks (``n_blocks`` slices of the
+parameter axis) so the FP64 working set stays bounded.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import torch
+
+__all__ = [
+    "SliceOrdering", "SiteOrdering", "Jacobian", "SlicedJacobian", "ParameterSpace", "SampleSpace", "QGT",
+    "jacobian_mean", "solve_cholesky", "solve_svd", "solve_cg",
+]
+
+
+@dataclass(frozen=True)
+class SliceOrdering:
+    """jacobian.py:21-33: columns [k=0 all sites][k=1 all sites]..."""
+
+
+@dataclass(frozen=True)
+class SiteOrdering:
+    """jacobian.py:36-46: columns [site0 all k][site1 all k]..."""
+
+    params_per_site: tuple
+
+
+@dataclass
+class Jacobian:
+    """jacobian.py:49-53."""
+
+    O: torch.Tensor
+
+
+@dataclass
+class SlicedJacobian:
+    """jacobian.py:56-93."""
+
+    o: torch.Tensor
+    p: torch.Tensor
+    sliced_dims: tuple
+    ordering: object = SliceOrdering()
+
+    @property
+    def phys_dim(self) -> int:
+        return max(self.sliced_dims) if self.sliced_dims else 2
+
+
+@dataclass(frozen=True)
+class ParameterSpace:
+    """qgt.py:36-40: S = O^H O / N - mean^H mean."""
+
+
+@dataclass(frozen=True)
+class SampleSpace:
+    """qgt.py:43-47: T = O O^H / N with centring terms."""
+
+
+def _f64(x):
+    return x.to(torch.complex128 if x.is_complex() else torch.float64)
+
+
+def iter_sliced_blocks(jac: SlicedJacobian, n_blocks: int = 1):
+    """qgt.py:62-87, yielding FP64 blocks of the expanded Jacobian (optionally split column-wise)."""
+    o, p = jac.o, jac.p
+    if isinstance(jac.ordering, SliceOrdering):
+        for k in range(max(jac.sliced_dims)):
+            n = o.shape[1]
+            step = -(-n // max(1, n_blocks))
+            for c0 in range(0, n, step):
+                ob = o[:, c0:c0 + step]
+                yield torch.where(p[:, c0:c0 + step] == k, _f64(ob), torch.zeros((), dtype=torch.float64,
+                                                                                   device=o.device))
+    else:
+        i = 0
+        for site, n in enumerate(jac.ordering.params_per_site):
+            for k in range(jac.sliced_dims[site]):
+                yield torch.where(p[:, i:i + n] == k, _f64(o[:, i:i + n]),
+                                  torch.zeros((), dtype=torch.float64, device=o.device))
+            i += n
+
+
+def sliced_dense_blocks(jac: SlicedJacobian) -> torch.Tensor:
+    """qgt.py:106-108."""
+    return torch.cat(list(iter_sliced_blocks(jac)), dim=1)
+
+
+def _dense_O(jac):
+    return _f64(jac.O) if isinstance(jac, Jacobian) else sliced_dense_blocks(jac)
+
+
+def jacobian_mean(jac) -> torch.Tensor:
+    """jacobian.py:96-139."""
+    if isinstance(jac, Jacobian):
+        return _f64(jac.O).mean(dim=0)
+    return torch.cat([b.mean(dim=0) for b in iter_sliced_blocks(jac)])
+
+
+def _sample_space_dense(jac, n_blocks):
+    n = (jac.O if isinstance(jac, Jacobian) else jac.o).shape[0]
+    dev = (jac.O if isinstance(jac, Jacobian) else jac.o).device
+    G = torch.zeros((n, n), dtype=torch.float64, device=dev)
+    w = torch.zeros(n, dtype=torch.float64, device=dev)
+    msq = torch.zeros((), dtype=torch.float64, device=dev)
+    blocks = [_f64(jac.O)] if isinstance(jac, Jacobian) else iter_sliced_blocks(jac, n_blocks)
+    for ob in blocks:
+        G += ob @ ob.conj().T
+        mb = ob.mean(dim=0)
+        w += ob @ mb.conj()
+        msq += torch.vdot(mb, mb).real
+    G /= n
+    ones = torch.ones(n, dtype=torch.float64, device=dev)
+    G -= (w[:, None] * ones[None, :]) / n
+    G -= (ones[:, None] * w.conj()[None, :]) / n
+    G += (msq / n) * torch.ones((n, n), dtype=torch.float64, device=dev)
+    return G
+
+
+@dataclass
+class QGT:
+    """qgt.py:36-49: lazy QGT with S @ v and to_dense()."""
+
+    jac: object
+    space: object = ParameterSpace()
+    n_blocks: int = 16
+
+    def to_dense(self) -> torch.Tensor:
+        """qgt.py:173-223."""
+        if isinstance(self.space, SampleSpace):
+            return _sample_space_dense(self.jac, self.n_blocks)
+        O = _dense_O(self.jac)
+        m = O.mean(dim=0)
+        return (O.conj().T @ O) / O.shape[0] - m.conj()[:, None] * m[None, :]
+
+    def __matmul__(self, v):
+        """qgt.py:116-165."""
+        O = _dense_O(self.jac)
+        n = O.shape[0]
+        m = O.mean(dim=0)
+        v = _f64(v)
+        if isinstance(self.space, ParameterSpace):
+            return (O.conj().T @ (O @ v)) / n - m.conj() * torch.dot(m, v)
+        res = (O @ (O.conj().T @ v)) / n
+        vs = v.sum()
+        w = O @ m.conj()
+        res = res - w * (vs / n)
+        res = res - torch.vdot(w, v) / n
+        return res + torch.vdot(m, m) * vs / n
+
+
+def adjoint_matvec(jac, v) -> torch.Tensor:
+    """preconditioners.py:100-114: O^H v - mean^H sum(v), block by block."""
+    if isinstance(jac, Jacobian):
+        O = _f64(jac.O)
+        return O.conj().T @ v - O.mean(dim=0).conj() * v.sum()
+    parts = [ob.conj().T @ v - ob.mean(dim=0).conj() * v.sum() for ob in iter_sliced_blocks(jac)]
+    return torch.cat(parts)
+
+
+def solve_cholesky(mat, rhs):
+    """solvers.py:25-28 (cuSOLVER potrf/potrs in FP64)."""
+    L = torch.linalg.cholesky(mat)
+    return torch.cholesky_solve(rhs[:, None], L)[:, 0]
+
+
+def solve_svd(mat, rhs, rcond: float = 1e-12):
+    """solvers.py:31-37."""
+    U, S, Vh = torch.linalg.svd(mat, full_matrices=False)
+    s_inv = torch.where(S > rcond * S.max(), 1.0 / S, torch.zeros_like(S))
+    return Vh.conj().T @ (s_inv * (U.conj().T @ rhs))
+
+
+def solve_cg(mat, rhs, maxiter: int = 1000, tol: float = 1e-5):
+    """solvers.py:16-22 (stop when |r| <= tol |b|)."""
+    x = torch.zeros_like(rhs)
+    r = rhs - mat @ x
+    p = r.clone()
+    rs = torch.vdot(r, r).real
+    stop = (tol * torch.linalg.norm(rhs)) ** 2
+    for _ in range(maxiter):
+        if rs <= stop:
+            break
+        ap = mat @ p
+        alpha = rs / torch.vdot(p, ap)
+        x = x + alpha * p
+        r = r - alpha * ap
+        rs_new = torch.vdot(r, r).real
+        p = r + (rs_new / rs) * p
+        rs = rs_new
+    return x
