@@ -126,6 +126,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+NCU_DRAM_BYTES_PER_SAMPLE = {"heis8x8_D4_chi16": 2.826e9 / 608}
+
+
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -298,8 +301,14 @@ def run_ours(args, rank, world, local_rank):
     mean_launch_s = statistics.mean(launch_ms) / 1e3
     achieved = n * flops / mean_launch_s / 1e12 if flops else None
     peak = peaks.get("bf16_tflops")
+    # DRAM bytes per sample of peps_kernel from one ncu capture of this workload
+    # (608 chains, dram__bytes_read.sum + dram__bytes_write.sum = 2.826 GB, see
+    # profiles/peps_kernel_heis8x8_D4_chi16.md); each chain reuses its CTA slot,
+    # so traffic scales with the chains of a launch
+    traffic = NCU_DRAM_BYTES_PER_SAMPLE.get(w.name)
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                "frac": (achieved / peak) if achieved and peak else None,
+                "traffic": traffic * n if traffic else None, "traffic_unit": "bytes per launch",
                 "peak_kind": f"{peak_kind} bf16 burst (cuBLAS)", "kernel": "vmc::peps_kernel",
                 "flop_per_sample": flops, "units_per_launch": n}
     cpu = None
@@ -337,8 +346,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="heis8x8_D4_chi16")
     ap.add_argument("--chains", type=int, default=0)
-    ap.add_argument("--cpu-chains-per-core", type=int, default=2)
-    ap.add_argument("--ref-chains-per-core", type=int, default=1)
+    ap.add_argument("--cpu-chains-per-core", type=int, default=128)
+    ap.add_argument("--ref-chains-per-core", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -22,7 +22,8 @@ def fp32(tensors):
 
 def oracle_strategy(name, chi):
     return {"NoTruncation": lambda: oracle.NoTruncation(), "ZipUp": lambda: oracle.ZipUp(chi),
-            "DensityMatrix": lambda: oracle.DensityMatrix(chi)}[name]()
+            "DensityMatrix": lambda: oracle.DensityMatrix(chi),
+            "Variational": lambda: oracle.Variational(chi, 2)}[name]()
 
 
 def hamiltonian(kind, shape):

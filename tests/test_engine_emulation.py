@@ -39,6 +39,9 @@ CASES = [
     ((4, 4), 2, 4, "ZipUp", "tfim"),
     ((4, 4), 3, 6, "ZipUp", "heisenberg"),
     ((3, 4), 2, 3, "ZipUp", "heisenberg"),
+    ((3, 3), 2, 4, "Variational", "heisenberg"),
+    ((4, 4), 3, 6, "Variational", "tfim"),
+    ((3, 4), 2, 3, "Variational", "heisenberg"),
 ]
 
 

@@ -1,0 +1,99 @@
+// householder.cuh -- CTA-level Householder QR of a small matrix, for the
+// variational boundary-MPS compression (strategy.py:179-427, whose QR is
+// geqrf + orgqr through src/vmc/utils/factorizations.py:9-16).
+//
+// Only the orthogonal factor is formed.  The compression needs an orthonormal
+// basis of the span of the leading k columns; where the triangular factor is
+// needed the caller recomputes it as Q^T A with a GEMM.  Reflectors follow
+// LAPACK's xLARFG conventions: H = I - tau v v^T with v[0] = 1,
+// beta = -sign(alpha) * ||(alpha, x)||, and tau = 0 when x is exactly zero, so
+// rank-deficient panels give the same unit columns LAPACK gives.  The result
+// equals LAPACK's Q up to rounding; the boundary MPS it feeds is invariant
+// under the sign of each column.
+#pragma once
+
+#include "device_common.cuh"
+#include "truncation.cuh"
+
+namespace vmc {
+
+// Q (m x k; element (i, c) at Q[i*qrs + c*qcs]) := the first k columns of the
+// orthogonal factor of the QR factorisation of the m x k panel A[:, :k]
+// (element (i, j) at A[i*ars + j*acs]); requires k <= m.  H (m x k, leading
+// dimension ldh, odd for conflict-free column access) and tau (k floats) are
+// scratch; Q must alias neither A nor H.  One warp builds each reflector, the
+// warps share the trailing columns; 3 barriers per column.
+__device__ inline void cta_householder_q(const float* A, int m, int k, int ars, int acs, float* Q, int qrs, int qcs,
+                                         float* H, int ldh, float* tau) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int nl = nt < 32 ? nt : 32;
+  const int lane = tid % nl, warp = tid / nl, nwarps = nt / nl;
+  for (int e = tid; e < m * k; e += nt) {
+    const int i = e / k, j = e - i * k;
+    H[(size_t)i * ldh + j] = A[(size_t)i * ars + (size_t)j * acs];
+  }
+  __syncthreads();
+  for (int j = 0; j < k; ++j) {
+    if (warp == 0) {
+      float xn = 0.f;
+      for (int i = j + 1 + lane; i < m; i += nl) {
+        const float x = H[(size_t)i * ldh + j];
+        xn = fmaf(x, x, xn);
+      }
+      xn = warp_sum_f(xn);
+      const float alpha = H[(size_t)j * ldh + j];
+      float t = 0.f, beta = alpha, sc = 0.f;
+      if (xn > 0.f) {
+        beta = -copysignf(sqrtf(fmaf(alpha, alpha, xn)), alpha);
+        t = (beta - alpha) / beta;
+        sc = 1.f / (alpha - beta);
+      }
+      warp_sync();
+      if (t != 0.f)
+        for (int i = j + 1 + lane; i < m; i += nl) H[(size_t)i * ldh + j] *= sc;
+      if (lane == 0) {
+        H[(size_t)j * ldh + j] = beta;
+        tau[j] = t;
+      }
+    }
+    __syncthreads();
+    const float t = tau[j];
+    if (t != 0.f) {
+      for (int c = j + 1 + warp; c < k; c += nwarps) {
+        float w = 0.f;
+        for (int i = j + 1 + lane; i < m; i += nl) w = fmaf(H[(size_t)i * ldh + j], H[(size_t)i * ldh + c], w);
+        w = t * (warp_sum_f(w) + H[(size_t)j * ldh + c]);
+        warp_sync();
+        if (lane == 0) H[(size_t)j * ldh + c] -= w;
+        for (int i = j + 1 + lane; i < m; i += nl)
+          H[(size_t)i * ldh + c] = fmaf(-w, H[(size_t)i * ldh + j], H[(size_t)i * ldh + c]);
+      }
+    }
+    __syncthreads();
+  }
+  // Q = H_0 H_1 ... H_{k-1} [I_k; 0]; H_j leaves columns c < j at e_c
+  for (int e = tid; e < m * k; e += nt) {
+    const int i = e / k, c = e - i * k;
+    Q[(size_t)i * qrs + (size_t)c * qcs] = (i == c) ? 1.f : 0.f;
+  }
+  __syncthreads();
+  for (int j = k - 1; j >= 0; --j) {
+    const float t = tau[j];
+    if (t != 0.f) {
+      for (int c = j + warp; c < k; c += nwarps) {
+        float w = 0.f;
+        for (int i = j + 1 + lane; i < m; i += nl)
+          w = fmaf(H[(size_t)i * ldh + j], Q[(size_t)i * qrs + (size_t)c * qcs], w);
+        w = t * (warp_sum_f(w) + Q[(size_t)j * qrs + (size_t)c * qcs]);
+        warp_sync();
+        if (lane == 0) Q[(size_t)j * qrs + (size_t)c * qcs] -= w;
+        for (int i = j + 1 + lane; i < m; i += nl)
+          Q[(size_t)i * qrs + (size_t)c * qcs] =
+              fmaf(-w, H[(size_t)i * ldh + j], Q[(size_t)i * qrs + (size_t)c * qcs]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace vmc

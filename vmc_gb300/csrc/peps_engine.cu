@@ -24,6 +24,7 @@
 #include "device_common.cuh"
 #include "phase_timers.cuh"
 #include "truncation.cuh"
+#include "householder.cuh"
 #include "../../include/vmc_gb300.h"
 
 #ifdef VMC_HOST_EMULATION
@@ -32,15 +33,17 @@ thread_local vmc_dim3 threadIdx, blockIdx, blockDim, gridDim;
 
 namespace vmc {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;         // largest CTA the kernel is compiled for
+constexpr int kDefaultThreads = 128;  // one chain per 4 warps: more chains resident per SM
 constexpr int kMaxVec = 512;   // max vectors in one truncation (chi * D)
 constexpr int kMaxCols = 64;   // max lattice columns
 constexpr int kMaxD = 4;       // max physical dimension
-constexpr int kPermKinds = 5;  // permuted copies of every site tensor
+constexpr int kPermKinds = 6;  // permuted copies of every site tensor
 constexpr float kJacobiTol = 5e-7f;  // stop when every |a_p.a_q| <= tol |a_p||a_q|
 constexpr int kJacobiSweeps = 16;
-constexpr long long kMaxArenaSmemBytes = 96 * 1024;
-enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4 };
+// dynamic shared memory per chain; 52 KB keeps 4 chains of 128 threads on an SM
+constexpr long long kMaxArenaSmemBytes = 52 * 1024;
+enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4, P_VRB = 5 };
 enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3 };
 
 
@@ -60,6 +63,7 @@ struct DevPlan {
   int vert_in_smem;       // vertical-energy buffers live in the shared-memory arena
   int onerow_in_smem;     // 1-row intermediates share the shared-memory arena
   int n_scr;              // number of SCR scratch buffers per slot
+  int VS;                 // one variational environment (floats); 0 unless Variational
   long long slot_floats;  // floats per workspace slot
   long long perm_floats;  // floats of the permuted tensor pack
   long long cache_floats_per_chain;  // bottom env tensors per chain
@@ -97,10 +101,12 @@ struct Slot {
   float* r2;     // C*E2S
   float* l2[2];  // E2S
   float* arena;  // truncation arena when it does not fit shared memory
+  float* venv;   // Variational: left envs C*VS, then right envs C*VS
   float* scr[24];
 };
 
 __host__ __device__ inline long long al64(long long n) { return (n + 63) & ~63LL; }
+__host__ __device__ inline int min_i(int a, int b) { return a < b ? a : b; }
 
 __device__ inline Slot make_slot(const DevPlan& P, float* base) {
   Slot s;
@@ -115,6 +121,7 @@ __device__ inline Slot make_slot(const DevPlan& P, float* base) {
   s.arena = p; p += P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.nmax * (P.nmax | 1)))
                                     : al64(P.arena_floats);
   for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
+  s.venv = p; p += al64(2LL * P.C * P.VS);
   return s;
 }
 
@@ -124,6 +131,7 @@ struct Shared {
   int sel[kMaxVec];
   float sig[kMaxVec];
   int spins[2][kMaxCols];
+  int vb[kMaxCols + 1];  // Variational: current bond dimensions of the row being compressed
   double bcast[8];
 };
 
@@ -168,6 +176,8 @@ __global__ void permute_tensors_kernel(const DevPlan* __restrict__ Pp, const flo
       base[(size_t)(P_LENV * P.d + p) * sz + ((l * U + u) * Rr + r) * V + v] = x;
       // [u][r][v][l]
       base[(size_t)(P_R2 * P.d + p) * sz + ((u * Rr + r) * V + v) * L + l] = x;
+      // [v][r][l][u]
+      base[(size_t)(P_VRB * P.d + p) * sz + ((v * Rr + r) * L + l) * U + u] = x;
     }
   }
 }
@@ -275,6 +285,149 @@ __device__ inline void select_topk(Shared& sh, int nv, int kout) {
   __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// Variational compression sweeps (strategy.py:179-219 with the environments
+// of :257-289 and the sweeps of :292-427).  On entry dst holds the
+// QR-initialised result with the bond dimensions in sh.vb; on exit dst holds
+// the result of n_sweeps (left-to-right, right-to-left) pairs, every tensor
+// Frobenius-normalised, and the return value is the log of the scale taken
+// out.  The bonds end at bout (the right-to-left sweep's LQ clamps a bond to
+// phys * right).  Index names: src MPS m[d][p][r], row MPO W[l][p][q][w]
+// (p = pin, q = pout), result T[a][q][b]; left environments LE[d][l][a],
+// right environments RE[r][w][b].
+//   lr site i:  X[a][l][p][r] = LE.m,  Y[a][q][r][w] = X.W,
+//               optimal[a][q][b] = Y.RE,  T = Q of optimal,  LE' = Y.T
+//   rl site i:  Z1[d][p][w][b] = m.RE,  Z2[d][l][q][b] = Z1.W',
+//               optimal[a][(q,b)] = LE.Z2,  T = Q^T of optimal^T,  RE' = Z2.T
+// Only the final right-to-left sweep's scales reach the state: its site-0
+// tensor is the unnormalised optimum, built from right environments that
+// were renormalised on the way.
+// ---------------------------------------------------------------------------
+struct VSite {
+  int din, dn, pin, pout, Lb, Rb;
+  const float* m;
+  const float* W;   // [l][p][q][w]
+  const float* W2;  // [p][w][l][q]
+};
+
+__device__ inline VSite vsite(const DevPlan& P, const float* perm, const float* src, const int* bin, int row, int c,
+                              const int* spins, bool from_below) {
+  VSite v;
+  const int s = site_id(P, row, c);
+  const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1];
+  v.Lb = P.sdim[4 * s + 2];
+  v.Rb = P.sdim[4 * s + 3];
+  v.pin = from_below ? V : U;
+  v.pout = from_below ? U : V;
+  v.din = bin[c];
+  v.dn = bin[c + 1];
+  v.m = src + (size_t)c * P.TS;
+  v.W = perm_of(P, perm, s, from_below ? P_ZIPB : P_ZIPT, spins[c]);
+  v.W2 = perm_of(P, perm, s, from_below ? P_VRB : P_RENV, spins[c]);
+  return v;
+}
+
+// Z2[d][l][q][b] (via Z1) for site v and right environment RE of bond kb.
+__device__ inline void vright_z2(const VSite& v, const float* RE, int kb, float* Z1, float* Z2) {
+  cta_gemm(make_gemm(v.m, lin(v.dn), 1, RE, lin(1), v.Rb * kb, Z1, lin(v.Rb * kb), lin(1), v.din * v.pin, v.Rb * kb,
+                     v.dn));
+  cta_gemm(make_gemm(Z1, two(kb, v.pin * v.Rb * kb, 1), kb, v.W2, lin(1), v.Lb * v.pout, Z2,
+                     two(kb, v.Lb * v.pout * kb, 1), lin(kb), v.din * kb, v.Lb * v.pout, v.pin * v.Rb));
+}
+
+// RE'[d][l][c] = sum_{q,b} Z2[d][l][q][b] T[c][q][b], renormalised; returns log of its norm.
+__device__ inline double vright_env(const VSite& v, const float* Z2, const float* T, int kb, int kt, float* REn,
+                                    double* red) {
+  const int qb = v.pout * kb;
+  cta_gemm(make_gemm(Z2, lin(qb), 1, T, lin(qb), 1, REn, lin(kt), lin(1), v.din * v.Lb, kt, qb));
+  const int n = v.din * v.Lb * kt;
+  const double nrm = sqrt(cta_dot(REn, REn, n, red));
+  if (nrm > 0.0) {
+    cta_scale(REn, (float)(1.0 / nrm), n);
+    return log(nrm);
+  }
+  return 0.0;
+}
+
+__device__ __noinline__ double variational_sweeps(const DevPlan& P, const Slot& S, Shared& sh, const float* perm,
+                                                  const float* src, const int* bin, float* dst, int row,
+                                                  const int* spins, bool from_below, const Arena& ar) {
+  const int C = P.C;
+  const size_t VS = (size_t)P.VS;
+  float* LE = S.venv;
+  float* RE = S.venv + (size_t)C * VS;
+  float* X = S.scr[7];
+  float* Y = S.scr[8];
+  float* O = S.scr[9];
+  int* vb = sh.vb;
+  // right environments of the initial result
+  if (threadIdx.x == 0) RE[(size_t)(C - 1) * VS] = 1.f;
+  __syncthreads();
+  for (int i = C - 1; i >= 1; --i) {
+    const VSite v = vsite(P, perm, src, bin, row, i, spins, from_below);
+    vright_z2(v, RE + (size_t)i * VS, vb[i + 1], X, Y);
+    vright_env(v, Y, dst + (size_t)i * P.TS, vb[i + 1], vb[i], RE + (size_t)(i - 1) * VS, sh.red);
+  }
+  double logsum = 0.0;
+  for (int sweep = 0; sweep < P.n_sweeps; ++sweep) {
+    // ---- left to right (strategy.py:292-356); the last site is recomputed by the next sweep ----
+    if (threadIdx.x == 0) LE[0] = 1.f;
+    __syncthreads();
+    for (int i = 0; i + 1 < C; ++i) {
+      const VSite v = vsite(P, perm, src, bin, row, i, spins, from_below);
+      const int ka = vb[i], kb = vb[i + 1];
+      const float* LEi = LE + (size_t)i * VS;
+      cta_gemm(make_gemm(LEi, lin(1), v.Lb * ka, v.m, lin(1), v.pin * v.dn, X,
+                         two(ka, v.pin * v.dn, v.Lb * v.pin * v.dn), lin(1), v.Lb * ka, v.pin * v.dn, v.din));
+      cta_gemm(make_gemm(X, two(v.dn, v.Lb * v.pin * v.dn, 1), v.dn, v.W, lin(1), v.pout * v.Rb, Y,
+                         two(v.dn, v.pout * v.dn * v.Rb, v.Rb), two(v.Rb, v.dn * v.Rb, 1), ka * v.dn,
+                         v.pout * v.Rb, v.Lb * v.pin));
+      cta_gemm(make_gemm(Y, lin(v.dn * v.Rb), 1, RE + (size_t)i * VS, lin(1), kb, O, lin(kb), lin(1), ka * v.pout, kb,
+                         v.dn * v.Rb));
+      const int mr = ka * v.pout;
+      const int kt = kb < mr ? kb : mr;
+      float* T = dst + (size_t)i * P.TS;
+      cta_householder_q(O, mr, kt, kb, 1, T, kt, 1, ar.G, kt | 1, ar.eig.tau);
+      if (threadIdx.x == 0) vb[i + 1] = kt;
+      float* LEn = LE + (size_t)(i + 1) * VS;
+      cta_gemm(make_gemm(Y, lin(1), v.dn * v.Rb, T, lin(1), kt, LEn, lin(kt), lin(1), v.dn * v.Rb, kt, mr));
+      const int n = v.dn * v.Rb * kt;
+      const double nrm = sqrt(cta_dot(LEn, LEn, n, sh.red));
+      if (nrm > 0.0) cta_scale(LEn, (float)(1.0 / nrm), n);
+    }
+    // ---- right to left (strategy.py:359-427) ----
+    logsum = 0.0;
+    if (threadIdx.x == 0) RE[(size_t)(C - 1) * VS] = 1.f;
+    __syncthreads();
+    for (int i = C - 1; i >= 0; --i) {
+      const VSite v = vsite(P, perm, src, bin, row, i, spins, from_below);
+      const int ka = vb[i], kb = vb[i + 1];
+      vright_z2(v, RE + (size_t)i * VS, kb, X, Y);
+      const int qb = v.pout * kb;
+      float* T = dst + (size_t)i * P.TS;
+      float* opt = (i == 0) ? T : O;
+      cta_gemm(make_gemm(LE + (size_t)i * VS, lin(1), ka, Y, lin(1), qb, opt, lin(qb), lin(1), ka, qb, v.din * v.Lb));
+      if (i == 0) {
+        const int n = ka * qb;
+        const double nrm = sqrt(cta_dot(T, T, n, sh.red));
+        if (nrm > 0.0) {
+          cta_scale(T, (float)(1.0 / nrm), n);
+          logsum += log(nrm);
+        }
+        break;
+      }
+      // LQ through the QR of optimal^T: T[c][(q,b)] = Q[(q,b)][c]
+      const int kt = ka < qb ? ka : qb;
+      cta_householder_q(O, qb, kt, 1, qb, T, 1, qb, ar.G, kt | 1, ar.eig.tau);
+      if (threadIdx.x == 0) vb[i] = kt;
+      logsum += vright_env(v, Y, T, kb, kt, RE + (size_t)(i - 1) * VS, sh.red);
+      cta_scale(T, (float)(1.0 / sqrt((double)kt)), kt * qb);
+      logsum += 0.5 * log((double)kt);
+    }
+  }
+  return logsum;
+}
+
 __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared& sh, const float* perm,
                                          const float* src, const int* bin, float* dst, const int* bout, int row,
                                          const int* spins, bool from_below, const Arena& ar, float* min_gap) {
@@ -283,7 +436,11 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
   float* carry = S.scr[0];
   float* carry_next = S.scr[1];
   float* Z1 = S.scr[2];
-  if (threadIdx.x == 0) carry[0] = 1.f;
+  if (threadIdx.x == 0) {
+    carry[0] = 1.f;
+    sh.vb[0] = bout[0];
+    sh.vb[C] = bout[C];
+  }
   __syncthreads();
   int kc = 1;
   for (int c = 0; c < C; ++c) {
@@ -325,7 +482,9 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
       }
       break;
     }
-    const int kout = bout[c + 1];
+    // Variational: initialisation bonds min(chi, rows, cols) (strategy.py:244-246)
+    const int kout = (P.strategy == VMC_STRATEGY_VARIATIONAL) ? min_i(P.chi, min_i(mrows, ncols)) : bout[c + 1];
+    if (threadIdx.x == 0) sh.vb[c + 1] = kout;
     // theta as a row-major matrix: mat[(k,q)][(r',w)], odd leading dimension
     const int ldm = ncols | 1;
     float* mat = ar.mat;
@@ -339,6 +498,11 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
         carry_next[(size_t)i * ncols + (col % Rb) * dn + col / Rb] = mat[(size_t)i * ldm + col];
       }
       __syncthreads();
+    } else if (P.strategy == VMC_STRATEGY_VARIATIONAL) {
+      // ---- QR initialisation (strategy.py:222-254): Q of the leading kout columns, carry = Q^T theta ----
+      cta_householder_q(mat, mrows, kout, ldm, 1, out, kout, 1, ar.G, kout | 1, ar.eig.tau);
+      cta_gemm(make_gemm(out, lin(1), kout, mat, lin(1), ldm, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols,
+                         mrows));
     } else if (P.trunc_method == 1) {
       // ---- reference path: one-sided Jacobi on the smaller set of vectors ----
       if (mrows >= ncols) {
@@ -460,6 +624,8 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
     carry_next = t;
     kc = kout;
   }
+  if (P.strategy == VMC_STRATEGY_VARIATIONAL && P.n_sweeps > 0 && C > 1)
+    logsum = variational_sweeps(P, S, sh, perm, src, bin, dst, row, spins, from_below, ar);
   return logsum;
 }
 
@@ -992,7 +1158,7 @@ namespace vmc {
 // Bond dimensions produced by applying one row MPO to a boundary MPS
 // (strategy.py:118-150; dims depend on shapes only).
 static std::vector<int> apply_bonds(const std::vector<int>& bin, const std::vector<int>& wb, int pout, int chi,
-                                    int strategy) {
+                                    int strategy, int n_sweeps) {
   const int C = (int)bin.size() - 1;
   std::vector<int> out(C + 1, 1);
   if (strategy == VMC_STRATEGY_NO_TRUNCATION) {
@@ -1008,6 +1174,10 @@ static std::vector<int> apply_bonds(const std::vector<int>& bin, const std::vect
     left = k;
   }
   out[C] = bin[C] * wb[C];
+  if (strategy == VMC_STRATEGY_VARIATIONAL && n_sweeps > 0) {
+    // the right-to-left sweep's LQ keeps min(left, phys * right) (strategy.py:403-410)
+    for (int i = C - 1; i >= 1; --i) out[i] = std::min(out[i], pout * out[i + 1]);
+  }
   return out;
 }
 
@@ -1121,11 +1291,11 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
   if (phys_dim > kMaxD) return VMC_ERR_UNSUPPORTED;
   if (dtype != VMC_DTYPE_F32) return VMC_ERR_UNSUPPORTED;
+  if (strategy < 0 || strategy > VMC_STRATEGY_VARIATIONAL || n_sweeps < 0) return VMC_ERR_INVALID;
   // DensityMatrix (strategy.py:153-176) carries V_k^H without the singular
   // values, so its next cut truncates an unweighted theta: not the ZipUp
   // product, and ill-defined for rank-deficient theta.  Not implemented.
-  if (strategy == VMC_STRATEGY_VARIATIONAL || strategy == VMC_STRATEGY_DENSITY_MATRIX) return VMC_ERR_UNSUPPORTED;
-  if (strategy < 0 || strategy > VMC_STRATEGY_VARIATIONAL) return VMC_ERR_INVALID;
+  if (strategy == VMC_STRATEGY_DENSITY_MATRIX) return VMC_ERR_UNSUPPORTED;
   vmc_plan* pl = new (std::nothrow) vmc_plan();
   if (!pl) return VMC_ERR_INVALID;
   DevPlan& P = pl->hp;
@@ -1158,12 +1328,23 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   pl->bb.assign((size_t)R * (C + 1), 1);
   std::vector<int> wb(C + 1, 1);
   for (int i = 1; i < C; ++i) wb[i] = D;
+  // Variational rows pass through their QR-initialisation bonds (never
+  // clamped) before the sweeps: size the tensor buffers for those as well
+  long long TS_init = 1, chi_init = 1;
+  auto account_init = [&](const std::vector<int>& cur, int pout) {
+    const std::vector<int> init = apply_bonds(cur, wb, pout, chi, strategy, 0);
+    for (int c = 0; c < C; ++c) {
+      TS_init = std::max(TS_init, (long long)init[c] * pout * init[c + 1]);
+      chi_init = std::max(chi_init, (long long)std::max(init[c], init[c + 1]));
+    }
+  };
   {
     std::vector<int> cur(C + 1, 1);
     for (int r = 0; r < R; ++r) {
       for (int i = 0; i <= C; ++i) pl->tb[(size_t)r * (C + 1) + i] = cur[i];
       const int pout = r == R - 1 ? 1 : D;
-      cur = apply_bonds(cur, wb, pout, chi, strategy);
+      account_init(cur, pout);
+      cur = apply_bonds(cur, wb, pout, chi, strategy, n_sweeps);
     }
     for (int i = 0; i <= C; ++i) pl->tb[(size_t)R * (C + 1) + i] = cur[i];
   }
@@ -1172,7 +1353,8 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
     for (int r = R - 1; r >= 0; --r) {
       for (int i = 0; i <= C; ++i) pl->bb[(size_t)r * (C + 1) + i] = cur[i];
       const int pout = r == 0 ? 1 : D;
-      cur = apply_bonds(cur, wb, pout, chi, strategy);
+      account_init(cur, pout);
+      cur = apply_bonds(cur, wb, pout, chi, strategy, n_sweeps);
     }
   }
   // buffer sizes
@@ -1198,6 +1380,8 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
       ES = std::max(ES, t * D * b);
       if (r + 1 < R) E2S = std::max(E2S, t * D * D * (long long)pl->bb[(size_t)(r + 1) * (C + 1) + c]);
     }
+  TS = std::max(TS, TS_init);
+  chimax = std::max(chimax, chi_init);
   // truncation matrices: rows kc*pout <= chimax*D, cols <= chimax*D
   MM = (chimax * D + 1) * (chimax * D + 1);
   const long long SCR = std::max({chimax * chimax * D * D * D, TS * D * D, MM, 4LL * kMaxVec});
@@ -1209,7 +1393,7 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   }
   {
     const char* th = std::getenv("VMC_THREADS");
-    P.threads = th ? std::max(64, std::min(kThreads, std::atoi(th))) : kThreads;
+    P.threads = th ? std::max(64, std::min(kThreads, std::atoi(th))) : kDefaultThreads;
   }
   long long budget = kMaxArenaSmemBytes;
   if (const char* kb = std::getenv("VMC_SMEM_KB")) budget = std::max(0, std::atoi(kb)) * 1024LL;
@@ -1251,11 +1435,12 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   }
   P.TS = (int)TS; P.ES = (int)ES; P.E2S = (int)E2S; P.MM = (int)MM; P.SCR = (int)SCR;
   P.n_scr = 11 + 2 * kMaxD;
+  P.VS = strategy == VMC_STRATEGY_VARIATIONAL ? (int)(chimax * D * chimax) : 0;
   P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + 3 * al64((long long)C * TS) +
                   al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
                   2 * al64(E2S) +
                   (P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.nmax * (P.nmax | 1))) : al64(P.arena_floats)) +
-                  (long long)P.n_scr * al64(SCR);
+                  (long long)P.n_scr * al64(SCR) + al64(2LL * C * P.VS);
   P.cache_floats_per_chain = al64((long long)R * C * TS);
   if (chimax * D > kMaxVec) {
     delete pl;
