@@ -188,6 +188,35 @@ def test_config2_shape_within_fp32_tolerance(emu_lib):
         assert abs(res.E.numpy()[i] - le.local_estimate[i]) < tol * max(1.0, abs(le.local_estimate[i])) * 10
 
 
+@pytest.mark.parametrize("strategy,chi,env", [("ZipUp", 6, {}), ("ZipUp", 6, {"VMC_TRUNCATION": "jacobi"}),
+                                              ("ZipUp", 6, {"VMC_SMEM_KB": "0"}), ("Variational", 6, {}),
+                                              ("NoTruncation", 16, {})])
+def test_stale_memory_never_reaches_the_results(emu_lib, strategy, chi, env, monkeypatch):
+    """Workspace, cache and (in this build, always) shared memory start as NaN: every value the
+    kernel reads must have been written first, so the outputs equal those of a zeroed run."""
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    shape, D = (4, 4), 3
+    H = hamiltonian("heisenberg", shape)
+    T, cfg, u = make_case(shape, D, 4, seed=11)
+    tens = torch.from_numpy(pack_tensors(T))
+    outs = []
+    for fill in (0.0, float("nan")):
+        eng = _engine(emu_lib, shape, D, chi, strategy, H)
+        ws = eng.workspace(cfg.shape[0])
+        ws[: (ws.numel() // 4) * 4].view(torch.float32).fill_(fill)
+        cache = eng.new_cache(cfg.shape[0])
+        cache[: (cache.numel() // 4) * 4].view(torch.float32).fill_(fill)
+        c = torch.from_numpy(cfg.copy())
+        eng.init_cache(tens, c, cache)
+        res = eng.sweep(tens, c, torch.from_numpy(u), cache)
+        assert eng.status() == 0
+        outs.append(res)
+    a, b = outs
+    assert torch.equal(a.configs, b.configs) and torch.equal(a.E, b.E) and torch.equal(a.O, b.O)
+    assert torch.isfinite(b.E).all() and torch.isfinite(b.O).all()
+
+
 def test_invalid_arguments_return_status_codes(emu_lib):
     import ctypes as ct
 

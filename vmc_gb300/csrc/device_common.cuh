@@ -51,6 +51,10 @@ struct Gemm {
   int accumulate;  // 1: C += alpha*AB, 0: C = alpha*AB
 };
 
+// Each thread owns a TM x TN tile whose rows and columns are interleaved
+// with stride tiles_m / tiles_n, so consecutive lanes touch consecutive rows
+// and columns: unit-stride operands are read without shared-memory bank
+// conflicts and with coalesced global loads.
 template <int TM, int TN>
 __device__ __forceinline__ void gemm_tiles(const Gemm& g) {
   const int tiles_m = (g.M + TM - 1) / TM;
@@ -63,13 +67,13 @@ __device__ __forceinline__ void gemm_tiles(const Gemm& g) {
     bool mv[TM], nv[TN];
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
-      int m = tm * TM + i;
+      int m = tm + i * tiles_m;
       mv[i] = m < g.M;
       aoff[i] = imap(g.am, mv[i] ? m : 0);
     }
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
-      int n = tn * TN + j;
+      int n = tn + j * tiles_n;
       nv[j] = n < g.N;
       boff[j] = imap(g.bn, nv[j] ? n : 0);
     }
@@ -92,11 +96,11 @@ __device__ __forceinline__ void gemm_tiles(const Gemm& g) {
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
       if (!mv[i]) continue;
-      const int co = imap(g.cm, tm * TM + i);
+      const int co = imap(g.cm, tm + i * tiles_m);
 #pragma unroll
       for (int j = 0; j < TN; ++j) {
         if (!nv[j]) continue;
-        float* dst = g.C + co + imap(g.cn, tn * TN + j);
+        float* dst = g.C + co + imap(g.cn, tn + j * tiles_n);
         float v = g.alpha * acc[i][j];
         *dst = g.accumulate ? (*dst + v) : v;
       }
@@ -105,7 +109,11 @@ __device__ __forceinline__ void gemm_tiles(const Gemm& g) {
 }
 
 // CTA-wide GEMM; ends with a barrier so C is visible to the whole CTA.
+#ifdef VMC_GEMM_NOINLINE
+__device__ __noinline__ void cta_gemm(const Gemm& g) {
+#else
 __device__ inline void cta_gemm(const Gemm& g) {
+#endif
   const int work = g.M * g.N;
   const int nt = blockDim.x;
   if (g.M >= 4 && g.N >= 4 && work >= nt * 16) {

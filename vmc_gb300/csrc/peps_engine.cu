@@ -981,6 +981,10 @@ __global__ void __launch_bounds__(kThreads) peps_kernel(
     dyn_smem = static_cast<float*>(std::malloc(sizeof(float) * P.arena_floats));
     dyn_floats = P.arena_floats;
   }
+  // shared memory starts with whatever an earlier block left: poison it so a
+  // read before write shows up as NaN in the host tests
+  if (dyn_smem) std::memset(dyn_smem, 0xff, sizeof(float) * dyn_floats);
+  std::memset(&sh, 0xff, sizeof(sh));
 #else
   extern __shared__ float dyn_smem[];
 #endif

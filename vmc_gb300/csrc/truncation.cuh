@@ -280,6 +280,9 @@ __device__ inline void tri_inverse_iteration(const float* d, const float* e, int
   }
   if (fabsf(al) < tiny) al = copysignf(tiny, al == 0.f ? 1.f : al);
   u0[n - 1] = al;
+  // the back substitution reads these (times zero) at i = n-1: they must not hold stale data
+  u1[n - 1] = 0.f;
+  u2[n - 1] = 0.f;
   // start vector: deterministic pseudo-random entries in [0.5, 1.5)
   unsigned h = seed * 2654435761u + 12345u;
   for (int i = 0; i < n; ++i) {
