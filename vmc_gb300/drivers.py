@@ -158,6 +158,50 @@ class TDVPDriver:
                             "error_of_mean": float(math.sqrt(float(var) / e.numel()))}
         self.residual_error = metrics.get("residual_error")
 
+    # ------------------------------------------------------------ checkpoint
+    def state_dict(self) -> dict:
+        """Everything a run carries between ``run`` calls (the attributes tdvp.py:76-93 sets up):
+        parameters, time, step count, sampler configurations and the sampler's RNG state, so a
+        resumed run draws the same uniforms and reaches bit-identical parameters."""
+        return {
+            "format": "vmc_gb300.TDVPDriver/1",
+            "t": self.t,
+            "dt": self.dt,
+            "step_count": self.step_count,
+            "n_samples": self.n_samples,
+            "n_chains": self.n_chains,
+            "full_gradient": self.full_gradient,
+            "tensors": [[t.detach().to("cpu").clone() for t in row] for row in self._tensors],
+            "sampler_configuration": self._sampler_configuration.detach().to("cpu").clone(),
+            "generator_state": self._gen.get_state(),
+            "loss_stats": None if self._loss_stats is None else dict(self._loss_stats),
+        }
+
+    def load_state_dict(self, state: dict) -> None:
+        if state.get("format") != "vmc_gb300.TDVPDriver/1":
+            raise ValueError("not a TDVPDriver checkpoint")
+        for key in ("n_samples", "n_chains", "full_gradient"):
+            if state[key] != getattr(self, key):
+                raise ValueError(f"checkpoint {key}={state[key]} does not match this driver ({getattr(self, key)})")
+        shapes = [[tuple(t.shape) for t in row] for row in self._tensors]
+        if [[tuple(t.shape) for t in row] for row in state["tensors"]] != shapes:
+            raise ValueError("checkpoint tensors do not match the model's shapes")
+        dev = self._model.device
+        self.t = float(state["t"])
+        self.dt = float(state["dt"])
+        self.step_count = int(state["step_count"])
+        self._tensors = [[t.to(dev, torch.float32).clone() for t in row] for row in state["tensors"]]
+        self._model.tensors = self._tensors
+        self._sampler_configuration = state["sampler_configuration"].to(dev, torch.int32).clone()
+        self._gen.set_state(state["generator_state"])
+        self._loss_stats = None if state["loss_stats"] is None else dict(state["loss_stats"])
+
+    def save(self, path) -> None:
+        torch.save(self.state_dict(), path)
+
+    def load(self, path) -> None:
+        self.load_state_dict(torch.load(path, map_location="cpu", weights_only=True))
+
     @property
     def energy(self):
         return self._loss_stats

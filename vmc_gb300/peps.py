@@ -75,11 +75,14 @@ class PEPS:
     """Open-boundary PEPS on a rectangular lattice (model.py:22-98).
 
     ``rngs`` seeds the reference's initialiser (uniform [0, 1) entries,
-    src/vmc/utils/utils.py:22-47) when ``tensors`` is not given.
+    src/vmc/utils/utils.py:22-47) when ``tensors`` is not given.  ``lib``
+    selects an engine library other than the in-tree CUDA build (a ctypes
+    handle bound by ``vmc_gb300._abi.bind``); by default the CUDA build is
+    required.
     """
 
     def __init__(self, *, rngs=0, shape, bond_dim, phys_dim=2, contraction_strategy=None,
-                 dtype=torch.float32, device=None, tensors=None):
+                 dtype=torch.float32, device=None, tensors=None, lib=None):
         self.shape = (int(shape[0]), int(shape[1]))
         self.bond_dim = int(bond_dim)
         self.phys_dim = int(phys_dim)
@@ -103,6 +106,7 @@ class PEPS:
                 if tuple(self.tensors[r][c].shape) != want:
                     raise ValueError(f"tensor ({r},{c}) has shape {tuple(self.tensors[r][c].shape)}, want {want}")
         self._engines = {}
+        self._lib = lib
 
     site_dims = staticmethod(_site_dims)
 
@@ -136,7 +140,7 @@ class PEPS:
         if eng is None:
             sname, chi, n_sweeps = _engine_strategy(self.strategy)
             eng = PEPSEngine(self.shape, self.bond_dim, min(chi, 1 << 20), self.phys_dim, sname, n_sweeps,
-                             operator=operator, device=self.device)
+                             operator=operator, device=self.device, lib=self._lib)
             self._engines[key] = (eng, operator)
             return eng
         return eng[0]
