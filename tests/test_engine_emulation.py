@@ -217,6 +217,21 @@ def test_stale_memory_never_reaches_the_results(emu_lib, strategy, chi, env, mon
     assert torch.isfinite(b.E).all() and torch.isfinite(b.O).all()
 
 
+def test_wide_rows_keep_the_zipup_carry_in_range(emu_lib):
+    """4x8, D=5, chi=25: along an 8-column row the zip-up carry shrinks at every site; unnormalised,
+    its Gram matrix reaches 1e-22 and the squared off-diagonals underflow FP32.  The engine
+    renormalises the carry after every cut."""
+    shape, D, chi = (4, 8), 5, 25
+    T, cfg, _ = make_case(shape, D, 3, seed=7)
+    eng = _engine(emu_lib, shape, D, chi, "ZipUp", None)
+    la, sg, O = eng.amp_grad(torch.from_numpy(pack_tensors(T)), torch.from_numpy(cfg.copy()))
+    model = oracle.PEPS(fp32(T), shape, D, strategy=oracle.ZipUp(chi))
+    amp, grads, _ = oracle.value_and_grad(model, cfg)
+    assert_parity(np.abs((sg * torch.exp(la)).numpy() / amp - 1), True)
+    o_ref = grads / amp[:, None]
+    assert_parity(np.linalg.norm(O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
+
+
 def test_invalid_arguments_return_status_codes(emu_lib):
     import ctypes as ct
 

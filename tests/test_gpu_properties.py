@@ -6,7 +6,8 @@ checked through properties that hold exactly (or to truncation accuracy):
     sweep flips every site (bit-exact);
   * two runs on the same inputs are bitwise identical (determinism);
   * psi is linear in each site tensor, so sum(A[s] * O) per site equals the
-    row-r amplitude over the transition amplitude (1 up to truncation error);
+    row-r amplitude over the transition amplitude: the same value for every
+    site of a row, and exactly 1 on the last row;
   * every output is finite and the device status word stays clear.
 """
 from __future__ import annotations
@@ -62,21 +63,27 @@ def test_outputs_finite_and_linear_in_each_site(full_case):
     eng, T, tens, cfg, u = full_case
     res = _sweep(eng, tens, cfg, u)
     assert torch.isfinite(res.E).all() and torch.isfinite(res.O).all() and torch.isfinite(res.logamp).all()
-    # sum_{u,d,l,r} A[r][c][s] * O[r][c] = psi_row(r) / psi ~ 1
+    # psi is linear in each site tensor: sum_{u,d,l,r} A[r][c][s] * O[r][c] = psi_row(r) / psi, with
+    # psi_row(r) the amplitude contracted through row r's environments.  Truncation makes psi_row(r)
+    # differ between rows (by O(1) at chi=16), but it is one number for every site of a row, and for
+    # the last row it is the transition's psi itself.
     pps = params_per_site(SHAPE, D)
     cfg_new = res.configs
     off = 0
-    devs = []
+    vals = []
     for site in range(64):
         r, c = divmod(site, 8)
         A = torch.from_numpy(np.asarray(T[r][c], dtype=np.float32)).to(cfg.device).reshape(2, -1)
         o = res.O[:, off:off + pps[site]]
         a_sel = A[cfg_new[:, site].long()]
-        devs.append(((a_sel * o).sum(1).double() - 1).abs())
+        vals.append((a_sel * o).sum(1).double())
         off += pps[site]
-    dev = torch.stack(devs)
-    assert float(dev.median()) < 1e-3
-    assert float(dev.max()) < 0.2
+    v = torch.stack(vals, 1).reshape(N, 8, 8)
+    last = (v[:, 7, :] - 1).abs()
+    assert float(last.median()) < 1e-5 and float(last.max()) < 1e-3
+    mean = v.mean(dim=2, keepdim=True)
+    spread = ((v - mean).abs().amax(dim=2) / mean.abs().squeeze(2).clamp_min(1e-2))
+    assert float(spread.median()) < 1e-4 and float(torch.quantile(spread.flatten(), 0.99)) < 1e-2
     # configs changed on roughly half the sites (random uniforms, |psi'|^2/|psi|^2 ~ O(1))
     frac = (res.configs != cfg).double().mean().item()
     assert 0.2 < frac < 0.8

@@ -109,11 +109,7 @@ __device__ __forceinline__ void gemm_tiles(const Gemm& g) {
 }
 
 // CTA-wide GEMM; ends with a barrier so C is visible to the whole CTA.
-#ifdef VMC_GEMM_NOINLINE
-__device__ __noinline__ void cta_gemm(const Gemm& g) {
-#else
 __device__ inline void cta_gemm(const Gemm& g) {
-#endif
   const int work = g.M * g.N;
   const int nt = blockDim.x;
   if (g.M >= 4 && g.N >= 4 && work >= nt * 16) {

@@ -498,8 +498,11 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
         carry_next[(size_t)i * ncols + (col % Rb) * dn + col / Rb] = mat[(size_t)i * ldm + col];
       }
       __syncthreads();
-    } else if (P.strategy == VMC_STRATEGY_VARIATIONAL) {
-      // ---- QR initialisation (strategy.py:222-254): Q of the leading kout columns, carry = Q^T theta ----
+    } else if (P.strategy == VMC_STRATEGY_VARIATIONAL || (mrows > ncols && kout >= ncols)) {
+      // ---- QR: Variational initialisation (strategy.py:222-254), or a ZipUp cut that keeps every
+      // column (U S V^T = theta exactly; an orthonormal basis of the column space is all that is
+      // needed, and theta V / sigma would not be one for near-zero sigma).  U = Q of the leading
+      // kout columns, carry = Q^T theta ----
       cta_householder_q(mat, mrows, kout, ldm, 1, out, kout, 1, ar.G, kout | 1, ar.eig.tau);
       cta_gemm(make_gemm(out, lin(1), kout, mat, lin(1), ldm, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols,
                          mrows));
@@ -609,6 +612,16 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
                          mrows));
       VMC_TSTOP(tc, PH_CARRY);
       VMC_TSTOP(tj, PH_JACOBI);
+    }
+    // renormalise the carry: its norm shrinks by the contraction at every
+    // site, and a Gram matrix of a tiny theta underflows FP32 a few sites on
+    {
+      const int n_el = kout * ncols;
+      const double nrm = sqrt(cta_dot(carry_next, carry_next, n_el, sh.red));
+      if (nrm > 0.0) {
+        cta_scale(carry_next, (float)(1.0 / nrm), n_el);
+        logsum += log(nrm);
+      }
     }
     // renormalise the new tensor
     {
