@@ -232,6 +232,26 @@ def test_wide_rows_keep_the_zipup_carry_in_range(emu_lib):
     assert_parity(np.linalg.norm(O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
 
 
+@pytest.mark.parametrize("shape", [(3, 24), (2, 32)])
+def test_wide_lattice_environments_stay_in_range(emu_lib, shape):
+    """|psi| ~ 1e-63 here: row environments are renormalised at every column with their log-scales
+    carried in FP64, so nothing leaves the FP32 range (Metropolis ratios, O and E_loc all match)."""
+    D, chi = 4, 8
+    H = hamiltonian("heisenberg", shape)
+    T, cfg, u = make_case(shape, D, 4, seed=2)
+    eng = _engine(emu_lib, shape, D, chi, "ZipUp", H)
+    res, _, _ = _sweep(eng, T, cfg, u)
+    c2, ctx, le = oracle_sweep(fp32(T), shape, D, "ZipUp", chi, H, cfg, u)
+    assert np.array_equal(res.configs.numpy(), c2)
+    assert float(res.logamp.max()) < -100
+    amp = (res.sign * torch.exp(res.logamp)).numpy()
+    assert_parity(np.abs(amp / ctx.amp - 1), True)
+    e_ref = le.local_estimate
+    assert_parity(np.abs(res.E.numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
+    o_ref = le.local_log_derivatives
+    assert_parity(np.linalg.norm(res.O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
+
+
 def test_invalid_arguments_return_status_codes(emu_lib):
     import ctypes as ct
 

@@ -179,6 +179,18 @@ __device__ inline void cta_scale(float* dst, float s, int n) {
   __syncthreads();
 }
 
+// Frobenius-normalise x[0..n) in place; returns the log of the norm taken out
+// (0 for a zero vector).  Environments shrink by the contraction at every
+// column and would otherwise leave the FP32 range across a wide lattice.
+__device__ inline double cta_normalize(float* x, int n, double* red) {
+  const double nrm = sqrt(cta_dot(x, x, n, red));
+  if (nrm > 0.0) {
+    cta_scale(x, (float)(1.0 / nrm), n);
+    return log(nrm);
+  }
+  return 0.0;
+}
+
 // ---------------------------------------------------------------------------
 // Parallel one-sided (Hestenes) Jacobi: mutually orthogonalise `nv` vectors of
 // length `len` stored at V + j*ldv (contiguous elements).  Rotations use the

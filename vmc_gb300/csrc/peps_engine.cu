@@ -95,6 +95,8 @@ struct DevPlan {
 struct Slot {
   float* topc;   // (R+1)*C*TS
   double* lt;    // R+1
+  double* rl;    // [q][c] log-scale of right environment renv[q][c]
+  double* r2l;   // [c] log-scale of 2-row right environment r2[c]
   float* brow[3];
   float* renv;   // d*C*ES  [q][c]
   float* lenv;   // (d+1)*ES
@@ -113,6 +115,8 @@ __device__ inline Slot make_slot(const DevPlan& P, float* base) {
   float* p = base;
   s.topc = p; p += al64((long long)(P.R + 1) * P.C * P.TS);
   s.lt = reinterpret_cast<double*>(p); p += al64(2 * (P.R + 2));
+  s.rl = reinterpret_cast<double*>(p); p += al64(2LL * P.d * P.C);
+  s.r2l = reinterpret_cast<double*>(p); p += al64(2LL * P.C);
   for (int i = 0; i < 3; ++i) { s.brow[i] = p; p += al64((long long)P.C * P.TS); }
   s.renv = p; p += al64((long long)P.d * P.C * P.ES);
   s.lenv = p; p += al64((long long)(P.d + 1) * P.ES);
@@ -679,13 +683,17 @@ __device__ inline void fill_ones_row(const DevPlan& P, float* row) {
 // > c).  With open_q, R_c is produced for every spin q of site c+1
 // (renv[q][c]); otherwise only for its current spin (renv[spin][c] and also
 // stored at renv[0][c]... the caller reads renv_cur()).
-__device__ __noinline__ void right_envs(const DevPlan& P, const Slot& S, const float* perm, const float* top, const int* tbond,
-                           const float* bot, const int* bbond, int row, const int* spins, bool open_q) {
+__device__ __noinline__ void right_envs(const DevPlan& P, const Slot& S, Shared& sh, const float* perm,
+                                       const float* top, const int* tbond, const float* bot, const int* bbond, int row,
+                                       const int* spins, bool open_q) {
   const int C = P.C;
   float* X1 = S.scr[3];
   float* X2 = S.scr[4];
   // R_{C-1} = [1] for every q slot
-  for (int q = threadIdx.x; q < P.d; q += blockDim.x) S.renv[((size_t)q * C + (C - 1)) * P.ES] = 1.f;
+  for (int q = threadIdx.x; q < P.d; q += blockDim.x) {
+    S.renv[((size_t)q * C + (C - 1)) * P.ES] = 1.f;
+    S.rl[(size_t)q * C + (C - 1)] = 0.0;
+  }
   __syncthreads();
   for (int c = C - 1; c >= 1; --c) {
     // absorb site c into R_c -> R_{c-1}
@@ -697,11 +705,14 @@ __device__ __noinline__ void right_envs(const DevPlan& P, const Slot& S, const f
     // R_c (current spin of site c+1) lives in slot spin(c+1); for c = C-1 all slots hold [1]
     const int qin = (c == C - 1) ? 0 : spins[c + 1];
     const float* Rin = S.renv + ((size_t)qin * C + c) * P.ES;
+    const double lin_c = S.rl[(size_t)qin * C + c];
     renv_step1(T, Rin, X1, ta, U, tb, Rb, bb);
     for (int q = 0; q < P.d; ++q) {
       if (!open_q && q != spins[c]) continue;
       float* Rout = S.renv + ((size_t)q * C + (c - 1)) * P.ES;
       renv_step23(X1, perm_of(P, perm, s, P_RENV, q), B, X2, Rout, ta, U, Rb, bb, Lb, V, ba);
+      const double lg = cta_normalize(Rout, ta * Lb * ba, sh.red);
+      if (threadIdx.x == 0) S.rl[(size_t)q * C + (c - 1)] = lin_c + lg;
     }
   }
 }
@@ -710,6 +721,11 @@ __device__ inline const float* renv_cur(const DevPlan& P, const Slot& S, const i
   const int q = (c == P.C - 1) ? 0 : spins[c + 1];
   return S.renv + ((size_t)q * P.C + c) * P.ES;
 }
+__device__ inline double rlog_cur(const DevPlan& P, const Slot& S, const int* spins, int c) {
+  const int q = (c == P.C - 1) ? 0 : spins[c + 1];
+  return S.rl[(size_t)q * P.C + c];
+}
+
 
 // ---------------------------------------------------------------------------
 // Transition of one row (kernels.py:142-206): Metropolis along the row.
@@ -719,7 +735,7 @@ __device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Sha
                                const double* uniforms, const int32_t* deltas, float* min_margin) {
   const int C = P.C;
   VMC_TSTART(tr);
-  right_envs(P, S, perm, top, tbond, bot, bbond, row, spins, false);
+  right_envs(P, S, sh, perm, top, tbond, bot, bbond, row, spins, false);
   VMC_TSTOP(tr, PH_T_RENV);
   VMC_TSTART(tm);
   float* Lc = S.lenv;                  // current left env
@@ -744,7 +760,9 @@ __device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Sha
     lenv_step1(Lc, T, Y1, ta, Lb, ba, U, tb);
     lenv_step23(Y1, perm_of(P, perm, s, P_LENV, cur), B, Y2, Lp0, ba, tb, Lb, U, Rb, V, bb);
     const int n_env = tb * Rb * bb;
-    if (c == 0) amp_cur = cta_dot(Lp0, Rc, n_env, sh.red);
+    // L and R are renormalised per column, so psi is recomputed at every
+    // column in that column's scale; the ratio is scale-free
+    amp_cur = cta_dot(Lp0, Rc, n_env, sh.red);
     double amp_flip = amp_cur;
     if (flip != cur) {
       lenv_step23(Y1, perm_of(P, perm, s, P_LENV, flip), B, Y2, Lp1, ba, tb, Lb, U, Rb, V, bb);
@@ -767,6 +785,7 @@ __device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Sha
     __syncthreads();
     float* sel = accept ? Lp1 : Lp0;
     cta_copy(Lc, sel, n_env);
+    cta_normalize(Lc, n_env, sh.red);
   }
   VMC_TSTOP(tm, PH_T_METRO);
 }
@@ -782,7 +801,7 @@ __device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Sha
   const int C = P.C;
   const bool has_h = want_energy && P.row_has_h[row];
   VMC_TSTART(tr);
-  right_envs(P, S, perm, top, tbond, bot, bbond, row, spins, has_h);
+  right_envs(P, S, sh, perm, top, tbond, bot, bbond, row, spins, has_h);
   VMC_TSTOP(tr, PH_E_RENV);
   VMC_TSTART(tl);
   float* Lc = S.lenv;
@@ -793,6 +812,7 @@ __device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Sha
   if (threadIdx.x == 0) Lc[0] = 1.f;
   __syncthreads();
   double energy = 0.0;
+  double llog = 0.0;  // log-scale taken out of the left environment
   for (int c = 0; c < C; ++c) {
     const int s = site_id(P, row, c);
     const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1], Lb = P.sdim[4 * s + 2], Rb = P.sdim[4 * s + 3];
@@ -802,6 +822,8 @@ __device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Sha
     const float* Rc = renv_cur(P, S, spins, c);
     const int cur = spins[c];
     const int sz = U * V * Lb * Rb;
+    // column scale: psi-normalised amplitude factor times the environments' log-scales
+    const double cscale = oscale * exp(llog + rlog_cur(P, S, spins, c));
     lenv_step1(Lc, T, Y1, ta, Lb, ba, U, tb);
     const bool os = want_energy && P.onesite_mask[s];
     if (want_grad || os) {
@@ -809,7 +831,7 @@ __device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Sha
       if (want_grad && Orow != nullptr) {
         G = Orow + (full_gradient ? (size_t)P.d * P.site_osl[s] + (size_t)cur * sz : (size_t)P.site_osl[s]);
       }
-      grad_env(Y1, B, Rc, W, G, ba, V, bb, tb, Rb, Lb, U, (float)oscale);
+      grad_env(Y1, B, Rc, W, G, ba, V, bb, tb, Rb, Lb, U, (float)cscale);
       if (os) {
         // amps_site[p] = sum A[p] . G  (already divided by psi); E += sum_p op[p, s] amps[p]
         for (int p = 0; p < P.d; ++p) {
@@ -832,15 +854,18 @@ __device__ __noinline__ double estimate_row(const DevPlan& P, const Slot& S, Sha
         for (int q = 0; q < P.d; ++q) {
           const float* Rq = S.renv + ((size_t)q * C + c) * P.ES;
           const double psi = cta_dot(Lp, Rq, n_env, sh.red);
-          energy += (double)op[(size_t)(p * P.d + q) * P.d * P.d + col] * psi * oscale;
+          const double qscale = oscale * exp(llog + S.rl[(size_t)q * C + c]);
+          energy += (double)op[(size_t)(p * P.d + q) * P.d * P.d + col] * psi * qscale;
         }
       }
       (void)sn;
       cta_copy(Lc, S.lenv + (size_t)(1 + cur) * P.ES, n_env);
+      llog += cta_normalize(Lc, n_env, sh.red);
     } else if (c < C - 1) {
       float* Lp = S.lenv + P.ES;
       lenv_step23(Y1, perm_of(P, perm, s, P_LENV, cur), B, Y2, Lp, ba, tb, Lb, U, Rb, V, bb);
       cta_copy(Lc, Lp, n_env);
+      llog += cta_normalize(Lc, n_env, sh.red);
     }
   }
   VMC_TSTOP(tl, PH_E_LEFT);
@@ -860,7 +885,10 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
   const int C = P.C, d = P.d;
   VMC_TSTART(tvr);
   // R2_{C-1} = [1]
-  if (threadIdx.x == 0) S.r2[(size_t)(C - 1) * P.E2S] = 1.f;
+  if (threadIdx.x == 0) {
+    S.r2[(size_t)(C - 1) * P.E2S] = 1.f;
+    S.r2l[C - 1] = 0.0;
+  }
   __syncthreads();
   for (int c = C - 1; c >= 1; --c) {
     const int s0 = site_id(P, r, c), s1 = site_id(P, r + 1, c);
@@ -889,6 +917,8 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
       cta_gemm(make_gemm(vb[0], lin(V1 * bb), 1, B, lin(V1 * bb), 1, Rout + (size_t)a0 * Lb * Lb1 * ba, lin(ba),
                          lin(1), na * Lb * Lb1, ba, V1 * bb));
     }
+    const double lg = cta_normalize(Rout, ta * Lb * Lb1 * ba, sh.red);
+    if (threadIdx.x == 0) S.r2l[c - 1] = S.r2l[c] + lg;
   }
   VMC_TSTOP(tvr, PH_V_RIGHT);
   VMC_TSTART(tvl);
@@ -897,6 +927,7 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
   if (threadIdx.x == 0) Lc[0] = 1.f;
   __syncthreads();
   double energy = 0.0;
+  double l2log = 0.0;  // log-scale taken out of the 2-row left environment
   for (int c = 0; c < C; ++c) {
     const int s0 = site_id(P, r, c), s1 = site_id(P, r + 1, c);
     const int U = P.sdim[4 * s0], V = P.sdim[4 * s0 + 1], Lb = P.sdim[4 * s0 + 2], Rb = P.sdim[4 * s0 + 3];
@@ -952,9 +983,11 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
     if (vt) {
       const float* op = P.vert + (size_t)(r * C + c) * d * d * d * d;
       const int col = s_cur * d + sp1[c];
-      for (int j = 0; j < d * d; ++j) energy += (double)op[(size_t)j * d * d + col] * psi[j] * vscale;
+      const double cscale = vscale * exp(l2log + S.r2l[c]);
+      for (int j = 0; j < d * d; ++j) energy += (double)op[(size_t)j * d * d + col] * psi[j] * cscale;
     }
     if (!last) {
+      l2log += cta_normalize(Ln, tb * Rb * Rb1 * bb, sh.red);
       float* t = Lc;
       Lc = Ln;
       Ln = t;
@@ -1453,7 +1486,8 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   P.TS = (int)TS; P.ES = (int)ES; P.E2S = (int)E2S; P.MM = (int)MM; P.SCR = (int)SCR;
   P.n_scr = 11 + 2 * kMaxD;
   P.VS = strategy == VMC_STRATEGY_VARIATIONAL ? (int)(chimax * D * chimax) : 0;
-  P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + 3 * al64((long long)C * TS) +
+  P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + al64(2LL * d * C) + al64(2LL * C) +
+                  3 * al64((long long)C * TS) +
                   al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
                   2 * al64(E2S) +
                   (P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.nmax * (P.nmax | 1))) : al64(P.arena_floats)) +
