@@ -164,6 +164,40 @@ __device__ inline double cta_dot(const float* x, const float* y, int n, double* 
   return cta_sum(s, red);
 }
 
+// acc[p*d+q] += <x[p], y[q]> over n floats for all p, q < d, in one pass: each
+// thread keeps d*d partial sums, then one CTA reduction (one at a time when
+// d*d*warps exceeds the 32 doubles of `red`).
+__device__ inline void cta_dots_all(const float* const* x, const float* const* y, int d, int n, double* acc,
+                                    double* red) {
+  constexpr int kMax = 16;
+  double s[kMax];
+  const int dd = d * d;
+  for (int j = 0; j < dd; ++j) s[j] = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int p = 0; p < d; ++p) {
+      const double xp = (double)x[p][i];
+      for (int q = 0; q < d; ++q) s[p * d + q] += xp * (double)y[q][i];
+    }
+  }
+  const int nw = (blockDim.x + 31) >> 5;
+  if (dd * nw > 32) {
+    for (int j = 0; j < dd; ++j) acc[j] += cta_sum(s[j], red);
+    return;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = 0; j < dd; ++j) s[j] = warp_sum(s[j]);
+  __syncthreads();
+  if (lane == 0)
+    for (int j = 0; j < dd; ++j) red[j * nw + wid] = s[j];
+  __syncthreads();
+  for (int j = 0; j < dd; ++j) {
+    double r = 0.0;
+    for (int w = 0; w < nw; ++w) r += red[j * nw + w];
+    acc[j] += r;
+  }
+  __syncthreads();
+}
+
 __device__ inline void cta_copy(float* dst, const float* src, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
   __syncthreads();

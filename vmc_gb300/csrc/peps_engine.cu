@@ -942,16 +942,22 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
     double psi[kMaxD * kMaxD];
     for (int i = 0; i < d * d; ++i) psi[i] = 0.0;
     const int s_cur = sp0[c];
+    const int sz0 = ssize(P, s0), sz1 = ssize(P, s1);
+    const int vstride = (int)(vb[2] - vb[1]);
     for (int b0 = 0; b0 < tb; b0 += P.vchunk) {
       const int nb = P.vchunk < tb - b0 ? P.vchunk : tb - b0;
       float* Q1 = vb[0];
       // Q1[x][e][b][l][u] = sum_a L2[a][(l,x,e)] T[a][u][b0+b]
       cta_gemm(make_gemm(Lc, lin(1), Lb * Lb1 * ba, T + b0, two(nb, tb, 1), U * tb, Q1,
                          two(Lb1 * ba, U, nb * Lb * U), two(nb, 1, Lb * U), Lb * Lb1 * ba, U * nb, ta));
-      // Q2[p][e][b][rr][x][v] = sum_{l,u} Q1[x][e][b][l][u] A[p](u,v,l,rr)
-      for (int p = 0; p < d; ++p) {
-        if (!vt && p != s_cur) continue;
-        cta_gemm(make_gemm(Q1, lin(Lb * U), 1, perm_of(P, perm, s0, P_LENV, p), lin(1), Rb * V, vb[1 + p],
+      // Q2[p][e][b][rr][x][v] = sum_{l,u} Q1[x][e][b][l][u] A[p](u,v,l,rr); with a vertical term every
+      // p at once (the spin slices of A are contiguous, the buffers vb[1+p] equally spaced)
+      if (vt) {
+        cta_gemm(make_gemm(Q1, lin(Lb * U), 1, perm_of(P, perm, s0, P_LENV, 0), two(Rb * V, sz0, 1), Rb * V,
+                           vb[1], two(ba * nb, V, Rb * Lb1 * V), three(Rb, V, vstride, Lb1 * V, 1),
+                           Lb1 * ba * nb, d * Rb * V, Lb * U));
+      } else {
+        cta_gemm(make_gemm(Q1, lin(Lb * U), 1, perm_of(P, perm, s0, P_LENV, s_cur), lin(1), Rb * V, vb[1 + s_cur],
                            two(ba * nb, V, Rb * Lb1 * V), two(V, Lb1 * V, 1), Lb1 * ba * nb, Rb * V, Lb * U));
       }
       if (vt) {
@@ -961,13 +967,11 @@ __device__ __noinline__ double vertical_energy(const DevPlan& P, const Slot& S, 
                            two(V1, nb * Rb * V1 * Rb1, Rb1), three(Rb, Rb1, Rb * V1 * Rb1, V1 * Rb1, 1), ba * V1,
                            nb * Rb * Rb1, bb));
         const int q2n = Lb1 * ba * nb * Rb * V;
-        for (int q = 0; q < d; ++q) {
-          float* Vq = vb[1 + d + q];
-          // Vq[e][b][rr][x][v] = sum_{w,y} A'[q][x][v][w][y] W2[e][b][rr][w][y]
-          cta_gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, q), lin(V1 * Rb1), 1, W2, lin(V1 * Rb1), 1, Vq, lin(1),
-                             lin(Lb1 * V), Lb1 * V, ba * nb * Rb, V1 * Rb1));
-          for (int p = 0; p < d; ++p) psi[p * d + q] += cta_dot(vb[1 + p], Vq, q2n, sh.red);
-        }
+        // Vq[e][b][rr][x][v] = sum_{w,y} A'[q][x][v][w][y] W2[e][b][rr][w][y], every q in one GEMM
+        cta_gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, 0), two(Lb1 * V, sz1, V1 * Rb1), 1, W2, lin(V1 * Rb1), 1,
+                           vb[1 + d], two(Lb1 * V, vstride, 1), lin(Lb1 * V), d * Lb1 * V, ba * nb * Rb, V1 * Rb1));
+        // psi(p, q) += <Q2[p], Vq> for all d*d pairs in one pass and one reduction
+        cta_dots_all(vb + 1, vb + 1 + d, d, q2n, psi, sh.red);
       }
       if (!last) {
         float* Q3 = vb[0];
