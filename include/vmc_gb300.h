@@ -44,7 +44,8 @@ enum {
   VMC_ERR_WORKSPACE = 3,   /* workspace smaller than vmc_workspace_size() */
   VMC_ERR_CUDA = 4,        /* a CUDA runtime call failed */
   VMC_ERR_NONFINITE = 5,   /* device status word reported NaN/Inf */
-  VMC_ERR_TIMEOUT = 6      /* a bounded device wait gave up */
+  VMC_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+  VMC_ERR_SCRATCH = 7      /* plan needs more than the fixed scratch of vmc_peps_amp_grad_noalloc */
 };
 
 /* dtype of the site tensors (the engine computes in FP32 either way). */
@@ -166,6 +167,34 @@ vmc_status vmc_peps_amp_grad(const vmc_plan* plan, void* stream, const float* te
                              const int32_t* samples, int n, int full_gradient, float* out_O,
                              double* out_logamp, double* out_sign, float* out_gap, void* workspace,
                              size_t workspace_bytes, int32_t* status_dev);
+
+/*
+ * vmc_peps_amp_grad without a caller workspace.  No counterpart in the
+ * reference: it exists for callers that cannot hand the engine scratch memory,
+ * e.g. a framework that has reserved the device memory in a pool of its own
+ * and offers no scratch allocation where it calls out, or host code that must
+ * not trigger an allocation (allocations synchronise the device) at the call.
+ *
+ * Scratch is one fixed array of this library in device memory,
+ * VMC_NOALLOC_SCRATCH_BYTES (64 MiB) per device.  A plan needs the permuted
+ * tensors plus at least one CTA slot in it (vmc_workspace_size(plan, 1)
+ * bytes); larger plans are rejected with VMC_ERR_SCRATCH and nothing is
+ * launched.  Chains are then processed by as many CTAs as fit, so results are
+ * identical to vmc_peps_amp_grad's but throughput drops for large plans.
+ *
+ * The first call on a device looks up the array's address on the current
+ * device (cudaGetSymbolAddress) and caches it; make that first call before any
+ * stream capture begins.  Nothing in the scratch needs to start at zero: the
+ * kernels write every word before reading it.  All calls on a device share
+ * the one array, so calls that overlap in time (different streams or threads)
+ * race on it and corrupt each other's results: serialise them.  The call
+ * allocates no device or host memory.
+ */
+#define VMC_NOALLOC_SCRATCH_BYTES (64ull << 20)
+vmc_status vmc_peps_amp_grad_noalloc(const vmc_plan* plan, void* stream, const float* tensors,
+                                     const int32_t* samples, int n, int full_gradient, float* out_O,
+                                     double* out_logamp, double* out_sign, float* out_gap,
+                                     int32_t* status_dev);
 
 /*
  * local_estimate (compat.py:136-194): E_loc for samples[n][n_sites] with the

@@ -15,6 +15,7 @@ VMC_ERR_WORKSPACE = 3
 VMC_ERR_CUDA = 4
 VMC_ERR_NONFINITE = 5
 VMC_ERR_TIMEOUT = 6
+VMC_ERR_SCRATCH = 7
 
 VMC_DTYPE_F32 = 0
 VMC_DTYPE_C64 = 1
@@ -50,6 +51,7 @@ SIGNATURES = {
     "vmc_peps_init_cache": (_I, [_P, _P, _P, _P, _I, _P, _P, _SZ, _P]),
     "vmc_peps_sweep": (_I, [_P, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "vmc_peps_amp_grad": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P]),
+    "vmc_peps_amp_grad_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P]),
     "vmc_peps_local_energy": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _P]),
 }
 

@@ -20,6 +20,7 @@
 #include <vector>
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 
 #include "device_common.cuh"
 #include "phase_timers.cuh"
@@ -1333,6 +1334,7 @@ const char* vmc_status_string(vmc_status s) {
     case VMC_ERR_CUDA: return "CUDA runtime error";
     case VMC_ERR_NONFINITE: return "non-finite result";
     case VMC_ERR_TIMEOUT: return "device wait timed out";
+    case VMC_ERR_SCRATCH: return "plan needs more than the fixed 64 MiB no-alloc scratch";
     default: return "unknown status";
   }
 }
@@ -1657,6 +1659,64 @@ vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors
   return launch(pl, stream, MODE_SWEEP, tensors, configs_inout, uniforms, deltas, n_chains, cache_inout,
                 full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, out_gap, workspace,
                 workspace_bytes, status_dev);
+}
+
+// ---------------------------------------------------------------------------
+// vmc_peps_amp_grad_noalloc: the amp_grad launch with its workspace in a fixed
+// device array of this library (sized by VMC_NOALLOC_SCRATCH_BYTES).
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[VMC_NOALLOC_SCRATCH_BYTES];
+
+#ifndef VMC_HOST_EMULATION
+constexpr int kNoAllocMaxDevices = 64;
+static void* g_noalloc_ptr[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mutex;
+#endif
+
+// Address of the scratch array on the current device, looked up once per device.
+static vmc_status noalloc_scratch(void** out) {
+#ifdef VMC_HOST_EMULATION
+  *out = g_noalloc_scratch;
+  return VMC_OK;
+#else
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return VMC_ERR_CUDA;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return VMC_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return VMC_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return VMC_OK;
+#endif
+}
+
+vmc_status vmc_peps_amp_grad_noalloc(const vmc_plan* pl, void* stream, const float* tensors,
+                                     const int32_t* samples, int n, int full_gradient, float* out_O,
+                                     double* out_logamp, double* out_sign, float* out_gap, int32_t* status_dev) {
+  if (!pl || !tensors || !samples || n < 0 || !out_logamp || !out_sign || !status_dev) return VMC_ERR_INVALID;
+  const size_t perm_bytes = (size_t)pl->hp.perm_floats * 4, slot_bytes = (size_t)pl->hp.slot_floats * 4;
+  if (perm_bytes + slot_bytes > VMC_NOALLOC_SCRATCH_BYTES) return VMC_ERR_SCRATCH;
+  if (n == 0) return VMC_OK;
+  void* ws = nullptr;
+  const vmc_status st = noalloc_scratch(&ws);
+  if (st != VMC_OK) return st;
+  const size_t fit = (VMC_NOALLOC_SCRATCH_BYTES - perm_bytes) / slot_bytes;
+  const int grid = (int)std::min<size_t>({fit, (size_t)n, (size_t)pl->slots_max});
+  float* wsf = static_cast<float*>(ws);
+  VMC_LAUNCH(permute_tensors_kernel, std::min(pl->hp.n_sites, 1024), kThreads, 0, stream, pl->dplan, tensors, wsf);
+  const size_t smem = pl->hp.arena_in_smem ? (size_t)pl->hp.arena_floats * 4 : 0;
+#ifndef VMC_HOST_EMULATION
+  if (smem > 0 &&
+      cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return VMC_ERR_CUDA;
+#endif
+  VMC_LAUNCH(peps_kernel, grid, pl->hp.threads, smem, stream, pl->dplan, (int)MODE_AMPGRAD, tensors, wsf,
+             const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr, full_gradient, out_O, nullptr, nullptr,
+             out_logamp, out_sign, nullptr, out_gap, wsf, status_dev);
+  return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
 }
 
 vmc_status vmc_peps_amp_grad(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples, int n,
