@@ -106,7 +106,7 @@ def test_amp_grad_and_local_energy_match_oracle(emu_lib):
     assert_parity(np.abs(e - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
 
 
-@pytest.mark.parametrize("env", [{"VMC_VCHUNK": "1"}, {"VMC_TRUNCATION": "jacobi"}, {"VMC_SMEM_KB": "0"},
+@pytest.mark.parametrize("env", [{"VMC_VCHUNK": "1", "VMC_VERT_SMEM": "1"}, {"VMC_TRUNCATION": "jacobi"}, {"VMC_SMEM_KB": "0"},
                                  {"VMC_SMEM_KB": "24"}], ids=["chunk1", "jacobi", "all-global", "mat-global"])
 def test_alternative_engine_paths_match_oracle(emu_lib, env, monkeypatch):
     """Chunked vertical energy, the Jacobi truncation and the global-memory fallbacks agree with the oracle."""

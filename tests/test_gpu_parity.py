@@ -116,7 +116,7 @@ def test_amp_grad_and_local_energy_match_oracle(cuda_device):
     assert_parity(np.abs(e.cpu().numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
 
 
-@pytest.mark.parametrize("env", [{"VMC_VCHUNK": "1"}, {"VMC_TRUNCATION": "jacobi"}, {"VMC_SMEM_KB": "0"},
+@pytest.mark.parametrize("env", [{"VMC_VCHUNK": "1", "VMC_VERT_SMEM": "1"}, {"VMC_TRUNCATION": "jacobi"}, {"VMC_SMEM_KB": "0"},
                                  {"VMC_SMEM_KB": "24"}, {"VMC_THREADS": "256", "VMC_SMEM_KB": "96"}],
                          ids=["chunk1", "jacobi", "all-global", "mat-global", "256-threads"])
 def test_alternative_engine_paths(cuda_device, env, monkeypatch):

@@ -263,7 +263,7 @@ __device__ inline Arena make_arena(const DevPlan& P, float* base, float* global_
   a.eig.v = p; p += al64(nmax);
   a.eig.p = p; p += al64(nmax);
   a.eig.lam = p; p += al64(nmax + 1);
-  a.eig.cvec = p; p += al64(nmax);
+  a.eig.cvec = p; p += al64(2LL * nmax);
   a.eig.part = p; p += al64(nmax + 64);
   a.eig.flag = reinterpret_cast<int*>(p); p += 64;
   return a;
@@ -273,7 +273,7 @@ __host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_
   const int ld = nmax | 1;
   return 2 * al64((long long)nmax * ld) + al64((long long)nmax * (trunc_method == 1 ? ld : kmax)) +
          al64((long long)kmax * kmax) + al64(4LL * kmax * nmax) + al64(((long long)kmax * nmax + 3) / 4) +
-         7 * al64(nmax) + al64(nmax + 1) + al64(nmax + 64) + 64;
+         6 * al64(nmax) + al64(2LL * nmax) + al64(nmax + 1) + al64(nmax + 64) + 64;
 }
 
 // Select the kout largest of sig[0..nv) into sh.sel (ties by index).
@@ -346,12 +346,7 @@ __device__ inline double vright_env(const VSite& v, const float* Z2, const float
   const int qb = v.pout * kb;
   cta_gemm(make_gemm(Z2, lin(qb), 1, T, lin(qb), 1, REn, lin(kt), lin(1), v.din * v.Lb, kt, qb));
   const int n = v.din * v.Lb * kt;
-  const double nrm = sqrt(cta_dot(REn, REn, n, red));
-  if (nrm > 0.0) {
-    cta_scale(REn, (float)(1.0 / nrm), n);
-    return log(nrm);
-  }
-  return 0.0;
+  return cta_normalize(REn, n, red);
 }
 
 __device__ __noinline__ double variational_sweeps(const DevPlan& P, const Slot& S, Shared& sh, const float* perm,
@@ -397,8 +392,7 @@ __device__ __noinline__ double variational_sweeps(const DevPlan& P, const Slot& 
       float* LEn = LE + (size_t)(i + 1) * VS;
       cta_gemm(make_gemm(Y, lin(1), v.dn * v.Rb, T, lin(1), kt, LEn, lin(kt), lin(1), v.dn * v.Rb, kt, mr));
       const int n = v.dn * v.Rb * kt;
-      const double nrm = sqrt(cta_dot(LEn, LEn, n, sh.red));
-      if (nrm > 0.0) cta_scale(LEn, (float)(1.0 / nrm), n);
+      cta_normalize(LEn, n, sh.red);
     }
     // ---- right to left (strategy.py:359-427) ----
     logsum = 0.0;
@@ -414,11 +408,7 @@ __device__ __noinline__ double variational_sweeps(const DevPlan& P, const Slot& 
       cta_gemm(make_gemm(LE + (size_t)i * VS, lin(1), ka, Y, lin(1), qb, opt, lin(qb), lin(1), ka, qb, v.din * v.Lb));
       if (i == 0) {
         const int n = ka * qb;
-        const double nrm = sqrt(cta_dot(T, T, n, sh.red));
-        if (nrm > 0.0) {
-          cta_scale(T, (float)(1.0 / nrm), n);
-          logsum += log(nrm);
-        }
+        logsum += cta_normalize(T, n, sh.red);
         break;
       }
       // LQ through the QR of optimal^T: T[c][(q,b)] = Q[(q,b)][c]
@@ -426,8 +416,7 @@ __device__ __noinline__ double variational_sweeps(const DevPlan& P, const Slot& 
       cta_householder_q(O, qb, kt, 1, qb, T, 1, qb, ar.G, kt | 1, ar.eig.tau);
       if (threadIdx.x == 0) vb[i] = kt;
       logsum += vright_env(v, Y, T, kb, kt, RE + (size_t)(i - 1) * VS, sh.red);
-      cta_scale(T, (float)(1.0 / sqrt((double)kt)), kt * qb);
-      logsum += 0.5 * log((double)kt);
+      logsum += cta_normalize(T, kt * qb, sh.red);
     }
   }
   return logsum;
@@ -464,11 +453,7 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
                          two(dn, Lb * pout * ncol, Rb), three(pout, Rb, pout * ncol, ncol, 1), din * dn,
                          Lb * pout * Rb, pin));
       const int n_el = din * Lb * pout * ncol;
-      const double nrm = sqrt(cta_dot(out, out, n_el, sh.red));
-      if (nrm > 0.0) {
-        cta_scale(out, (float)(1.0 / nrm), n_el);
-        logsum += log(nrm);
-      }
+      logsum += cta_normalize(out, n_el, sh.red);
       continue;
     }
     // Z1[k][l][p][r'] = sum_d carry[k][l][d] m[d][p][r']
@@ -480,11 +465,7 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
       cta_gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, out, two(dn, pout * ncols, Rb),
                          two(Rb, ncols, 1), kc * dn, pout * Rb, Lb * pin));
       const int n_el = mrows * ncols;
-      const double nrm = sqrt(cta_dot(out, out, n_el, sh.red));
-      if (nrm > 0.0) {
-        cta_scale(out, (float)(1.0 / nrm), n_el);
-        logsum += log(nrm);
-      }
+      logsum += cta_normalize(out, n_el, sh.red);
       break;
     }
     // Variational: initialisation bonds min(chi, rows, cols) (strategy.py:244-246)
@@ -622,20 +603,12 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
     // site, and a Gram matrix of a tiny theta underflows FP32 a few sites on
     {
       const int n_el = kout * ncols;
-      const double nrm = sqrt(cta_dot(carry_next, carry_next, n_el, sh.red));
-      if (nrm > 0.0) {
-        cta_scale(carry_next, (float)(1.0 / nrm), n_el);
-        logsum += log(nrm);
-      }
+      logsum += cta_normalize(carry_next, n_el, sh.red);
     }
     // renormalise the new tensor
     {
       const int n_el = mrows * kout;
-      const double nrm = sqrt(cta_dot(out, out, n_el, sh.red));
-      if (nrm > 0.0) {
-        cta_scale(out, (float)(1.0 / nrm), n_el);
-        logsum += log(nrm);
-      }
+      logsum += cta_normalize(out, n_el, sh.red);
     }
     float* t = carry;
     carry = carry_next;
@@ -1016,7 +989,9 @@ __device__ inline double* cache_logs(const DevPlan& P, float* cache, int n_chain
 // ---------------------------------------------------------------------------
 // The fused kernel.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) peps_kernel(
+// At most 128 registers per thread (two 256-thread CTAs, or four of the default
+// 128 threads, per SM): left free, the compiler takes all 255 and halves occupancy.
+__global__ void __launch_bounds__(kThreads, 2) peps_kernel(
     const DevPlan* __restrict__ Pp, int mode, const float* __restrict__ tensors, const float* __restrict__ perm,
     int32_t* configs, const double* __restrict__ uniforms, const int32_t* __restrict__ deltas, int n_chains,
     float* cache, int full_gradient, float* out_O, int8_t* out_p, double* out_E, double* logamp_io,
@@ -1476,7 +1451,13 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
     if (const char* vc = std::getenv("VMC_VCHUNK")) ch = std::max(1LL, std::min(ch, (long long)std::atoi(vc)));
     P.vchunk = (int)ch;
     P.vbuf = (int)al64(ch * unit);
-    P.vert_in_smem = (P.arena_in_smem && nbuf * P.vbuf * 4 <= budget) ? 1 : 0;
+    // The vertical-energy buffers live in (L1-cached) global scratch with the
+    // whole bond range in one chunk: fewer, larger GEMMs beat shared-memory
+    // chunks of a few bond values (measured +5 % at 8x8, D=4, chi=16).
+    // VMC_VERT_SMEM=1 puts them in the shared-memory arena, chunked.
+    P.vert_in_smem = 0;
+    if (const char* vs = std::getenv("VMC_VERT_SMEM"))
+      if (std::atoi(vs) != 0 && P.arena_in_smem && nbuf * P.vbuf * 4 <= budget) P.vert_in_smem = 1;
   }
   P.onerow_in_smem = 0;
   if (P.arena_in_smem && std::max(P.arena_floats, 4LL * P.scr1) * 4 <= budget) {

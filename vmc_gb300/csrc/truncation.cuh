@@ -78,19 +78,18 @@ __device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, fl
       tj = (beta - alpha) / beta;
       scal = 1.f / (alpha - beta);
     }
-    for (int i = tid; i < m; i += nt) {
-      const float vi = (i == 0) ? 1.f : A[(size_t)(j + 1 + i) * lda + j] * scal;
-      v[i] = vi;
-      if (i > 0) A[(size_t)(j + 1 + i) * lda + j] = vi;
-    }
+    // column j stays unscaled until barrier (2): the matrix-vector product
+    // below rebuilds v from it, so v needs no barrier of its own
+    const float* colj = A + (size_t)(j + 1) * lda + j;
+    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? 1.f : colj[(size_t)i * lda] * scal;
     if (tid == 0) {
       d[j] = A[(size_t)j * lda + j];
       e[j] = beta;
       tau[j] = tj;
     }
-    __syncthreads();  // (1) v visible
     float* As = A + (size_t)(j + 1) * lda + (j + 1);
     if (tj == 0.f) {
+      __syncthreads();  // v visible
       float s = 0.f;
       for (int i = 2 + tid; i < m; i += nt) s = fmaf(As[(size_t)i * lda], As[(size_t)i * lda], s);
       s = warp_sum_f(s);
@@ -106,13 +105,16 @@ __device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, fl
       int l = rlane;
       for (; l + 3 * rg < m; l += 4 * rg) {
         const float a0 = row[l], a1 = row[l + rg], a2 = row[l + 2 * rg], a3 = row[l + 3 * rg];
-        const float b0 = v[l], b1 = v[l + rg], b2 = v[l + 2 * rg], b3 = v[l + 3 * rg];
+        const float b0 = l == 0 ? 1.f : colj[(size_t)l * lda] * scal;
+        const float b1 = colj[(size_t)(l + rg) * lda] * scal;
+        const float b2 = colj[(size_t)(l + 2 * rg) * lda] * scal;
+        const float b3 = colj[(size_t)(l + 3 * rg) * lda] * scal;
         s0 = fmaf(a0, b0, s0);
         s1 = fmaf(a1, b1, s1);
         s2 = fmaf(a2, b2, s2);
         s3 = fmaf(a3, b3, s3);
       }
-      for (; l < m; l += rg) s0 = fmaf(row[l], v[l], s0);
+      for (; l < m; l += rg) s0 = fmaf(row[l], l == 0 ? 1.f : colj[(size_t)l * lda] * scal, s0);
       float s = (s0 + s1) + (s2 + s3);
 #ifndef VMC_HOST_EMULATION
       for (int o = rg / 2; o > 0; o >>= 1) s += __shfl_xor_sync(rmask, s, o, rg);
@@ -120,12 +122,14 @@ __device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, fl
       const float pi = tj * s;
       if (rlane == 0) {
         p[i] = pi;
-        pv = fmaf(pi, v[i], pv);
+        pv = fmaf(pi, i == 0 ? 1.f : colj[(size_t)i * lda] * scal, pv);
       }
     }
     pv = warp_sum_f(pv);
     if (lane == 0) part[32 + warp] = pv;
-    __syncthreads();  // (2) p visible
+    __syncthreads();  // (2) p and v visible
+    // store the reflector in column j (nothing reads column j any more)
+    for (int i = 1 + tid; i < m; i += nt) A[(size_t)(j + 1 + i) * lda + j] = v[i];
     float ptv = 0.f;
     for (int w = 0; w < nwarps; ++w) ptv += part[32 + w];
     const float K = 0.5f * tj * ptv;
@@ -203,11 +207,15 @@ __device__ inline float cta_top_eigenvalues(const float* d, const float* e, floa
   const float span = hi - lo;
   lo -= 1e-6f * span + 1e-30f;
   hi += 1e-6f * span + 1e-30f;
+  // lanes per eigenvalue: 8 (9-way multisection) unless fewer lanes let every
+  // wanted eigenvalue run in one round
   int G = nt >= 8 ? 8 : 1;
+  while (G > 2 && nt / G < kk) G >>= 1;
   const int ngroups = nt / G;
   const int l = tid % G;
   const int base = (tid & 31) & ~(G - 1);
-  const unsigned gmask = (G == 1) ? 1u : (0xffu << base);
+  // exactly this group's lanes: groups leave the loop independently
+  const unsigned gmask = (((1u << G) - 1u) << base);
   const int npts = G > 1 ? G - 1 : 1;
   const int rounds = (kk + ngroups - 1) / ngroups;
   for (int rd = 0; rd < rounds; ++rd) {
@@ -215,7 +223,7 @@ __device__ inline float cta_top_eigenvalues(const float* d, const float* e, floa
     const bool valid = t < kk && tid / G < ngroups;
     const int idx = n - 1 - (valid ? t : 0);
     float a = lo, b = hi;
-    const int max_it = npts > 1 ? 14 : 64;
+    const int max_it = npts >= 7 ? 14 : (npts >= 3 ? 20 : (npts >= 2 ? 26 : 64));
     for (int it = 0; it < max_it; ++it) {
       const float step = (b - a) / (float)(npts + 1);
       int pred = 0;
@@ -410,25 +418,60 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
   while (gx * 2 <= k && gx * 2 <= nt) gx *= 2;
   const int gy = nt / gx;
   const int ux = tid % gx, uy = tid / gx;
-  for (int j = n - 3; j >= 0; --j) {
+  float* cv2 = cvec + k;
+  int j = n - 3;
+  // pairs: Y <- H_{j-1} H_j Y in one reduction and one update.  With
+  // a = v_j^T Y, b = v_{j-1}^T Y and sg = v_{j-1}^T v_j:
+  //   c_j = tau_j a,  c_{j-1} = tau_{j-1} (b - sg c_j),
+  //   Y -= v_j c_j^T + v_{j-1} c_{j-1}^T.
+  // Rows are indexed from j (v_{j-1}[j] = 1, v_j[j] = 0, v_j[j+1] = 1).
+  for (; j >= 1; j -= 2) {
+    const float t1 = tau[j], t0 = tau[j - 1];
+    if (t1 == 0.f && t0 == 0.f) continue;
+    const int m = n - j;
+    for (int t = grp; t < k; t += ngroups) {
+      float a = 0.f, b = 0.f, sg = 0.f;
+      for (int i = lig; i < m; i += g) {
+        const int row = j + i;
+        const float y = Y[(size_t)row * ldy + t];
+        const float vb = (i == 0) ? 1.f : A[(size_t)row * lda + (j - 1)];
+        const float va = (i == 0) ? 0.f : ((i == 1) ? 1.f : A[(size_t)row * lda + j]);
+        a = fmaf(va, y, a);
+        b = fmaf(vb, y, b);
+        sg = fmaf(va, vb, sg);
+      }
+#ifndef VMC_HOST_EMULATION
+      for (int o = g / 2; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(gmask, a, o, g);
+        b += __shfl_xor_sync(gmask, b, o, g);
+        sg += __shfl_xor_sync(gmask, sg, o, g);
+      }
+#endif
+      if (lig == 0) {
+        const float cj = t1 * a;
+        cvec[t] = cj;
+        cv2[t] = t0 * (b - sg * cj);
+      }
+    }
+    __syncthreads();
+    for (int i = uy; i < m; i += gy) {
+      const int row = j + i;
+      const float vb = (i == 0) ? 1.f : A[(size_t)row * lda + (j - 1)];
+      const float va = (i == 0) ? 0.f : ((i == 1) ? 1.f : A[(size_t)row * lda + j]);
+      float* yrow = Y + (size_t)row * ldy;
+      for (int t = ux; t < k; t += gx) yrow[t] -= va * cvec[t] + vb * cv2[t];
+    }
+    __syncthreads();
+  }
+  // a last unpaired reflector (j == 0)
+  for (; j >= 0; --j) {
     const float tj = tau[j];
     if (tj == 0.f) continue;
     const int m = n - j - 1;
     for (int t = grp; t < k; t += ngroups) {
-      float s = 0.f, s1 = 0.f;
-      int i = lig;
-      if (i == 0) {
-        s = Y[(size_t)(j + 1) * ldy + t];
-        i += g;
-      }
-      for (; i + g < m; i += 2 * g) {
-        const float a0 = A[(size_t)(j + 1 + i) * lda + j], a1 = A[(size_t)(j + 1 + i + g) * lda + j];
-        const float y0 = Y[(size_t)(j + 1 + i) * ldy + t], y1 = Y[(size_t)(j + 1 + i + g) * ldy + t];
-        s = fmaf(a0, y0, s);
-        s1 = fmaf(a1, y1, s1);
-      }
-      if (i < m) s = fmaf(A[(size_t)(j + 1 + i) * lda + j], Y[(size_t)(j + 1 + i) * ldy + t], s);
-      s += s1;
+      float s = 0.f;
+      for (int i = lig; i < m; i += g)
+        s = fmaf(i == 0 ? 1.f : A[(size_t)(j + 1 + i) * lda + j], Y[(size_t)(j + 1 + i) * ldy + t], s);
 #ifndef VMC_HOST_EMULATION
       for (int o = g / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, g);
 #endif
