@@ -18,6 +18,12 @@ inline unsigned long long jacobi_sweep_hist[32];
 #endif
 
 // offset(i) with i = (i1 * n2 + i2) * n3 + i3  ->  i1*s1 + i2*s2 + i3*s3
+#ifndef VMC_GEMM_TENSOR_CORES
+#define VMC_GEMM_TENSOR_CORES 0
+#endif
+// CTA GEMMs of at least 16 x 8 x 8 run on the tensor cores (3xTF32)
+constexpr bool kGemmTensorCores = VMC_GEMM_TENSOR_CORES != 0;
+
 struct IMap {
   int n2, n3, s1, s2, s3;
 };
@@ -108,10 +114,93 @@ __device__ __forceinline__ void gemm_tiles(const Gemm& g) {
   }
 }
 
+#ifndef VMC_HOST_EMULATION
+// ---------------------------------------------------------------------------
+// Tensor-core path: warp-level mma.sync m16n8k8 with TF32 operands and FP32
+// accumulation.  Each operand is split x = hi + lo (hi = x rounded to TF32,
+// lo = the TF32 rounding of the remainder) and hi*hi + hi*lo + lo*hi is
+// accumulated, which keeps products to about 2^-22 relative: FP32 accuracy
+// for these contractions.  Operands are read in place through the index maps,
+// with rows, columns and k beyond the matrix read as zero.
+// Fragment layout (PTX ISA, m16n8k8 .tf32): lane = 4*g + t;
+//   A: a0 (g, t), a1 (g+8, t), a2 (g, t+4), a3 (g+8, t+4)
+//   B: b0 (k=t, n=g), b1 (k=t+4, n=g)
+//   D: d0 (g, 2t), d1 (g, 2t+1), d2 (g+8, 2t), d3 (g+8, 2t+1)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_m16n8k8_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_bits(x);
+  lo = tf32_bits(x - __uint_as_float(hi));
+}
+
+__device__ inline void gemm_mma(const Gemm& g) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int gr = lane >> 2, tg = lane & 3;
+  const int tiles_m = (g.M + 15) >> 4, tiles_n = (g.N + 7) >> 3;
+  for (int t = warp; t < tiles_m * tiles_n; t += nwarps) {
+    const int m0 = (t / tiles_n) << 4, n0 = (t % tiles_n) << 3;
+    const int r0 = m0 + gr, r1 = r0 + 8, c0 = n0 + gr;
+    const bool v0 = r0 < g.M, v1 = r1 < g.M, vc = c0 < g.N;
+    const float* a0p = g.A + imap(g.am, v0 ? r0 : 0);
+    const float* a1p = g.A + imap(g.am, v1 ? r1 : 0);
+    const float* bp = g.B + imap(g.bn, vc ? c0 : 0);
+    float d[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k0 = 0; k0 < g.K; k0 += 8) {
+      const int ka = k0 + tg, kb = ka + 4;
+      const bool ka_ok = ka < g.K, kb_ok = kb < g.K;
+      const float x0 = (v0 && ka_ok) ? a0p[(size_t)ka * g.sak] : 0.f;
+      const float x1 = (v1 && ka_ok) ? a1p[(size_t)ka * g.sak] : 0.f;
+      const float x2 = (v0 && kb_ok) ? a0p[(size_t)kb * g.sak] : 0.f;
+      const float x3 = (v1 && kb_ok) ? a1p[(size_t)kb * g.sak] : 0.f;
+      const float y0 = (vc && ka_ok) ? bp[(size_t)ka * g.sbk] : 0.f;
+      const float y1 = (vc && kb_ok) ? bp[(size_t)kb * g.sbk] : 0.f;
+      uint32_t ah[4], al[4], bh[2], bl[2];
+      split_tf32(x0, ah[0], al[0]);
+      split_tf32(x1, ah[1], al[1]);
+      split_tf32(x2, ah[2], al[2]);
+      split_tf32(x3, ah[3], al[3]);
+      split_tf32(y0, bh[0], bl[0]);
+      split_tf32(y1, bh[1], bl[1]);
+      mma_m16n8k8_tf32(d, al, bh);
+      mma_m16n8k8_tf32(d, ah, bl);
+      mma_m16n8k8_tf32(d, ah, bh);
+    }
+    const int cc0 = n0 + 2 * tg, cc1 = cc0 + 1;
+    const bool w00 = v0 && cc0 < g.N, w01 = v0 && cc1 < g.N, w10 = v1 && cc0 < g.N, w11 = v1 && cc1 < g.N;
+    const int o0 = w00 || w01 ? imap(g.cm, r0) : 0, o1 = w10 || w11 ? imap(g.cm, r1) : 0;
+    const int q0 = cc0 < g.N ? imap(g.cn, cc0) : 0, q1 = cc1 < g.N ? imap(g.cn, cc1) : 0;
+    if (w00) { float* p = g.C + o0 + q0; const float v = g.alpha * d[0]; *p = g.accumulate ? (*p + v) : v; }
+    if (w01) { float* p = g.C + o0 + q1; const float v = g.alpha * d[1]; *p = g.accumulate ? (*p + v) : v; }
+    if (w10) { float* p = g.C + o1 + q0; const float v = g.alpha * d[2]; *p = g.accumulate ? (*p + v) : v; }
+    if (w11) { float* p = g.C + o1 + q1; const float v = g.alpha * d[3]; *p = g.accumulate ? (*p + v) : v; }
+  }
+}
+#endif
+
 // CTA-wide GEMM; ends with a barrier so C is visible to the whole CTA.
 __device__ inline void cta_gemm(const Gemm& g) {
   const int work = g.M * g.N;
   const int nt = blockDim.x;
+#ifndef VMC_HOST_EMULATION
+  if (kGemmTensorCores && g.M >= 16 && g.N >= 8 && g.K >= 8 && work >= nt * 32) {
+    gemm_mma(g);
+    __syncthreads();
+    return;
+  }
+#endif
   if (g.M >= 4 && g.N >= 4 && work >= nt * 16) {
     gemm_tiles<4, 4>(g);
   } else if (g.M >= 2 && g.N >= 2 && work >= nt * 4) {
@@ -157,40 +246,57 @@ __device__ inline double cta_sum(double v, double* red) {
   return r;
 }
 
-// dot(x, y) over n contiguous floats, accumulated in double.
+// dot(x, y) over n contiguous floats: FP32 partial sums per thread (two
+// chains), combined across the CTA in double.  FP64 arithmetic runs at a
+// small fraction of the FP32 rate on this part, so it is kept out of the loop.
 __device__ inline double cta_dot(const float* x, const float* y, int n, double* red) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += (double)x[i] * (double)y[i];
-  return cta_sum(s, red);
+  float s0 = 0.f, s1 = 0.f;
+  int i = threadIdx.x;
+  const int st = blockDim.x;
+  for (; i + st < n; i += 2 * st) {
+    s0 = fmaf(x[i], y[i], s0);
+    s1 = fmaf(x[i + st], y[i + st], s1);
+  }
+  if (i < n) s0 = fmaf(x[i], y[i], s0);
+  return cta_sum((double)s0 + (double)s1, red);
 }
 
-// acc[p*d+q] += <x[p], y[q]> over n floats for all p, q < d, in one pass: each
-// thread keeps d*d partial sums, then one CTA reduction (one at a time when
-// d*d*warps exceeds the 32 doubles of `red`).
+// acc[p*d+q] += <x[p], y[q]> over n floats for all p, q < d.  For d = 2 the
+// four products share one pass and one CTA reduction (register accumulators,
+// FP32 per thread, double across threads); other d fall back to one cta_dot
+// per pair.
 __device__ inline void cta_dots_all(const float* const* x, const float* const* y, int d, int n, double* acc,
                                     double* red) {
-  constexpr int kMax = 16;
-  double s[kMax];
-  const int dd = d * d;
-  for (int j = 0; j < dd; ++j) s[j] = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    for (int p = 0; p < d; ++p) {
-      const double xp = (double)x[p][i];
-      for (int q = 0; q < d; ++q) s[p * d + q] += xp * (double)y[q][i];
-    }
-  }
   const int nw = (blockDim.x + 31) >> 5;
-  if (dd * nw > 32) {
-    for (int j = 0; j < dd; ++j) acc[j] += cta_sum(s[j], red);
+  if (d != 2 || 4 * nw > 32) {
+    for (int p = 0; p < d; ++p)
+      for (int q = 0; q < d; ++q) acc[p * d + q] += cta_dot(x[p], y[q], n, red);
     return;
   }
+  const float* x0 = x[0];
+  const float* x1 = x[1];
+  const float* y0 = y[0];
+  const float* y1 = y[1];
+  float f00 = 0.f, f01 = 0.f, f10 = 0.f, f11 = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float a = x0[i], b = x1[i], u = y0[i], v = y1[i];
+    f00 = fmaf(a, u, f00);
+    f01 = fmaf(a, v, f01);
+    f10 = fmaf(b, u, f10);
+    f11 = fmaf(b, v, f11);
+  }
+  double s[4] = {(double)f00, (double)f01, (double)f10, (double)f11};
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int j = 0; j < dd; ++j) s[j] = warp_sum(s[j]);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s[j] = warp_sum(s[j]);
   __syncthreads();
-  if (lane == 0)
-    for (int j = 0; j < dd; ++j) red[j * nw + wid] = s[j];
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) red[j * nw + wid] = s[j];
+  }
   __syncthreads();
-  for (int j = 0; j < dd; ++j) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
     double r = 0.0;
     for (int w = 0; w < nw; ++w) r += red[j * nw + w];
     acc[j] += r;
@@ -213,16 +319,37 @@ __device__ inline void cta_scale(float* dst, float s, int n) {
   __syncthreads();
 }
 
-// Frobenius-normalise x[0..n) in place; returns the log of the norm taken out
-// (0 for a zero vector).  Environments shrink by the contraction at every
-// column and would otherwise leave the FP32 range across a wide lattice.
+// Rescale x[0..n) in place by the power of two that brings max|x| into
+// [0.5, 1); returns the log of the factor taken out (0 for a zero or
+// non-finite vector).  Power-of-two scaling is exact, so the returned log
+// matches the applied scale bit for bit.  Environments shrink by the
+// contraction at every column and would otherwise leave the FP32 range across
+// a wide lattice.
 __device__ inline double cta_normalize(float* x, int n, double* red) {
-  const double nrm = sqrt(cta_dot(x, x, n, red));
-  if (nrm > 0.0) {
-    cta_scale(x, (float)(1.0 / nrm), n);
-    return log(nrm);
-  }
-  return 0.0;
+  float m = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, fabsf(x[i]));
+#ifndef VMC_HOST_EMULATION
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+#endif
+  float* fred = reinterpret_cast<float*>(red);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) fred[wid] = m;
+  __syncthreads();
+  m = 0.f;
+  for (int w = 0; w < nw; ++w) m = fmaxf(m, fred[w]);
+  __syncthreads();
+  if (!(m > 0.f) || !isfinite(m)) return 0.0;
+  int e = 0;
+  frexpf(m, &e);  // m = f * 2^e, f in [0.5, 1)
+  e = e < -120 ? -120 : (e > 120 ? 120 : e);  // keep 2^-e a normal float
+  if (e == 0) return 0.0;
+  const float sc = ldexpf(1.f, -e);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= sc;
+  __syncthreads();
+  return (double)e * 0.69314718055994530942;
 }
 
 // ---------------------------------------------------------------------------
