@@ -50,7 +50,8 @@ def _oracle_chunk(args):
     n_sites = w.shape[0] * w.shape[1]
     cfg = initial_configs(n, n_sites, w.phys_dim, seed=seed).astype(np.int64)
     u = next(uniform_stream(n, n_sites, seed=seed))
-    strat = oracle.ZipUp(w.chi) if w.strategy == "ZipUp" else oracle.NoTruncation()
+    strat = {"ZipUp": lambda: oracle.ZipUp(w.chi), "Variational": lambda: oracle.Variational(w.chi, 2)}.get(
+        w.strategy, oracle.NoTruncation)()
     model = oracle.PEPS(T, w.shape, w.bond_dim, w.phys_dim, strategy=strat)
     init, trans, est = oracle.build_mc_kernels(model, w.operator())
     cache = init(T, cfg)
@@ -181,12 +182,13 @@ def e2e_public_api(w, n, rank, dev, ustream, args, barrier):
     import torch
 
     from vmc_gb300.kernels import build_mc_kernels
-    from vmc_gb300.peps import PEPS, ZipUp
+    from vmc_gb300.peps import PEPS, NoTruncation, Variational, ZipUp
     from vmc_gb300.sampling import make_mc_sampler
     from vmc_gb300.synthetic import initial_configs, random_tensors
 
     n_sites = w.shape[0] * w.shape[1]
-    model = PEPS(shape=w.shape, bond_dim=w.bond_dim, phys_dim=w.phys_dim, contraction_strategy=ZipUp(w.chi),
+    strategy = {"ZipUp": ZipUp, "Variational": Variational}.get(w.strategy, lambda _: NoTruncation())(w.chi)
+    model = PEPS(shape=w.shape, bond_dim=w.bond_dim, phys_dim=w.phys_dim, contraction_strategy=strategy,
                  device=dev, tensors=random_tensors(w.shape, w.bond_dim, w.phys_dim, seed=0))
     init_cache, transition, estimate = build_mc_kernels(model, w.operator())
     sampler = make_mc_sampler(transition, estimate)
