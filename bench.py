@@ -27,7 +27,8 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "PEPS samples/s (amp+grad log psi+E_loc), D=4 chi=16"
+def metric_name(w) -> str:
+    return f"PEPS samples/s (amp+grad log psi+E_loc), D={w.bond_dim} chi={w.chi}"
 UNIT = "samples/s"
 
 
@@ -127,7 +128,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-NCU_DRAM_BYTES_PER_SAMPLE = {"heis8x8_D4_chi16": 2.826e9 / 608}
+NCU_DRAM_BYTES_PER_SAMPLE = {"heis8x8_D4_chi16": 13.179e9 / 608}
 
 
 def _peaks():
@@ -161,7 +162,7 @@ def run_reference(args, rank, world):
         wall = time.perf_counter() - t0
     value = n_total / wall
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "impl": "reference", "metric": metric_name(w), "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
@@ -304,7 +305,7 @@ def run_ours(args, rank, world, local_rank):
     achieved = n * flops / mean_launch_s / 1e12 if flops else None
     peak = peaks.get("bf16_tflops")
     # DRAM bytes per sample of peps_kernel from one ncu capture of this workload
-    # (608 chains, dram__bytes_read.sum + dram__bytes_write.sum = 2.826 GB, see
+    # (608 chains, dram__bytes_read.sum + dram__bytes_write.sum = 13.18 GB, see
     # profiles/peps_kernel_heis8x8_D4_chi16.md); each chain reuses its CTA slot,
     # so traffic scales with the chains of a launch
     traffic = NCU_DRAM_BYTES_PER_SAMPLE.get(w.name)
@@ -322,7 +323,7 @@ def run_ours(args, rank, world, local_rank):
                "sample": f"{ns} chains x 1 sweep ({wall:.1f} s), FP64 NumPy oracle restatement over {cores} processes"}
     clk = clocks.summary()
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric_name(w), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
