@@ -124,7 +124,7 @@ __device__ inline Slot make_slot(const DevPlan& P, float* base) {
   s.lenv = p; p += al64((long long)(P.d + 1) * P.ES);
   s.r2 = p; p += al64((long long)P.C * P.E2S);
   for (int i = 0; i < 2; ++i) { s.l2[i] = p; p += al64(P.E2S); }
-  s.arena = p; p += P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.nmax * (P.nmax | 1)))
+  s.arena = p; p += P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.es * P.nmax * (P.nmax | 1)))
                                     : al64(P.arena_floats);
   for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
   s.venv = p; p += al64(2LL * P.C * P.VS);
@@ -144,11 +144,13 @@ struct Shared {
 // ---------------------------------------------------------------------------
 // Device code, compiled once per element type.
 // ---------------------------------------------------------------------------
-__host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_method) {
+// Floats of the truncation arena (layout: make_arena); es = floats per element.
+__host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_method, int es) {
   const int ld = nmax | 1;
-  return 2 * al64((long long)nmax * ld) + al64((long long)nmax * (trunc_method == 1 ? ld : kmax)) +
+  return 2 * al64((long long)es * nmax * ld) + al64((long long)es * nmax * (trunc_method == 1 ? ld : kmax)) +
          al64((long long)kmax * kmax) + al64(4LL * kmax * nmax) + al64(((long long)kmax * nmax + 3) / 4) +
-         6 * al64(nmax) + al64(2LL * nmax) + al64(nmax + 1) + al64(nmax + 64) + 64;
+         3 * al64(nmax) + 3 * al64((long long)es * nmax) + al64(nmax + 1) + al64(2LL * es * nmax) +
+         al64(nmax + 64) + 64 + (es == 2 ? al64((long long)nmax * kmax) : 0);
 }
 
 namespace rk {
@@ -286,11 +288,11 @@ static void default_operator(vmc_plan* pl) {
   DevPlan& P = pl->hp;
   HostOp& op = pl->op;
   const int d2 = P.d * P.d;
-  op.onesite.assign((size_t)P.n_sites * P.d * P.d, 0.f);
+  op.onesite.assign((size_t)P.es * P.n_sites * P.d * P.d, 0.f);
   op.onesite_mask.assign(P.n_sites, 0);
-  op.horiz.assign((size_t)std::max(P.R * (P.C - 1), 1) * d2 * d2, 0.f);
+  op.horiz.assign((size_t)P.es * std::max(P.R * (P.C - 1), 1) * d2 * d2, 0.f);
   op.horiz_mask.assign(std::max(P.R * (P.C - 1), 1), 0);
-  op.vert.assign((size_t)std::max((P.R - 1) * P.C, 1) * d2 * d2, 0.f);
+  op.vert.assign((size_t)P.es * std::max((P.R - 1) * P.C, 1) * d2 * d2, 0.f);
   op.vert_mask.assign(std::max((P.R - 1) * P.C, 1), 0);
   op.row_has_h.assign(P.R, 0);
   op.row_has_v.assign(P.R, 0);
@@ -331,7 +333,7 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   const int R = shape->n_rows, C = shape->n_cols;
   if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
   if (phys_dim > kMaxD) return VMC_ERR_UNSUPPORTED;
-  if (dtype != VMC_DTYPE_F32) return VMC_ERR_UNSUPPORTED;
+  if (dtype != VMC_DTYPE_F32 && dtype != VMC_DTYPE_C64) return VMC_ERR_UNSUPPORTED;
   if (strategy < 0 || strategy > VMC_STRATEGY_VARIATIONAL || n_sweeps < 0) return VMC_ERR_INVALID;
   // DensityMatrix (strategy.py:153-176) carries V_k^H without the singular
   // values, so its next cut truncates an unweighted theta: not the ZipUp
@@ -342,7 +344,7 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   DevPlan& P = pl->hp;
   std::memset(&P, 0, sizeof(P));
   P.R = R; P.C = C; P.D = bond_dim; P.d = phys_dim; P.chi = chi; P.strategy = strategy;
-  P.es = 1;
+  P.es = dtype == VMC_DTYPE_C64 ? 2 : 1;
   P.n_sweeps = n_sweeps; P.n_sites = R * C;
   const int D = bond_dim, d = phys_dim;
   pl->sdim.resize(4 * R * C);
@@ -364,7 +366,7 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
       poff += (long long)kPermKinds * d * sz;
     }
   P.np_sliced = (int)osl;
-  P.perm_floats = (poff + 63) & ~63LL;
+  P.perm_floats = (poff * P.es + 63) & ~63LL;
   // bond dims
   pl->tb.assign((size_t)(R + 1) * (C + 1), 1);
   pl->bb.assign((size_t)R * (C + 1), 1);
@@ -426,12 +428,19 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   chimax = std::max(chimax, chi_init);
   // truncation matrices: rows kc*pout <= chimax*D, cols <= chimax*D
   MM = (chimax * D + 1) * (chimax * D + 1);
-  const long long SCR = std::max({chimax * chimax * D * D * D, TS * D * D, MM, 4LL * kMaxVec});
+  // element counts above; every DevPlan buffer size below counts floats (es per element)
+  const long long es = P.es;
+  // (>= 8 * kMaxVec floats: contract_bottom keeps 2 x kMaxVec complex doubles in scr[0])
+  const long long SCR = std::max(es * std::max({chimax * chimax * D * D * D, TS * D * D, MM}), 8LL * kMaxVec);
+  TS *= es;
+  ES *= es;
+  E2S *= es;
   P.nmax = (int)(chimax * D);
   P.kmax = (int)std::min<long long>(chi, chimax * D);
   {
     const char* tm = std::getenv("VMC_TRUNCATION");
-    P.trunc_method = (tm && std::strcmp(tm, "jacobi") == 0) ? 1 : 0;
+    // the one-sided Jacobi cross-check exists for real elements only
+    P.trunc_method = (tm && std::strcmp(tm, "jacobi") == 0 && es == 1) ? 1 : 0;
   }
   {
     const char* th = std::getenv("VMC_THREADS");
@@ -439,8 +448,8 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   }
   long long budget = kMaxArenaSmemBytes;
   if (const char* kb = std::getenv("VMC_SMEM_KB")) budget = std::max(0, std::atoi(kb)) * 1024LL;
-  const long long mat_floats = al64((long long)P.nmax * (P.nmax | 1));
-  const long long trunc_all = arena_floats(P.nmax, P.kmax, P.trunc_method);
+  const long long mat_floats = al64(es * P.nmax * (P.nmax | 1));
+  const long long trunc_all = arena_floats(P.nmax, P.kmax, P.trunc_method, P.es);
   P.arena_in_smem = 0;
   P.mat_in_smem = 1;  // "theta lives inside the arena" (arena itself may be global)
   P.arena_floats = trunc_all;
@@ -452,10 +461,10 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
     P.mat_in_smem = 0;
     P.arena_floats = trunc_all - mat_floats;
   }
-  P.scr1 = (int)al64(std::max(chimax * chimax * D * D, (long long)D * D * D * D));
+  P.scr1 = (int)al64(es * std::max(chimax * chimax * D * D, (long long)D * D * D * D));
   {
     // one bond value of a vertical-energy intermediate holds <= chimax * D^3 floats
-    const long long unit = chimax * D * D * D;
+    const long long unit = es * chimax * D * D * D;
     const long long nbuf = 1 + 2LL * d;
     long long ch = (budget / 4) / (nbuf * unit);
     ch = std::max(1LL, std::min(ch, chimax));
@@ -483,12 +492,12 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   }
   P.TS = (int)TS; P.ES = (int)ES; P.E2S = (int)E2S; P.MM = (int)MM; P.SCR = (int)SCR;
   P.n_scr = 11 + 2 * kMaxD;
-  P.VS = strategy == VMC_STRATEGY_VARIATIONAL ? (int)(chimax * D * chimax) : 0;
+  P.VS = strategy == VMC_STRATEGY_VARIATIONAL ? (int)(es * chimax * D * chimax) : 0;
   P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + al64(2LL * d * C) + al64(2LL * C) +
                   3 * al64((long long)C * TS) +
                   al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
                   2 * al64(E2S) +
-                  (P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.nmax * (P.nmax | 1))) : al64(P.arena_floats)) +
+                  (P.arena_in_smem ? (P.mat_in_smem ? 0 : mat_floats) : al64(P.arena_floats)) +
                   (long long)P.n_scr * al64(SCR) + al64(2LL * C * P.VS);
   P.cache_floats_per_chain = al64((long long)R * C * TS);
   if (chimax * D > kMaxVec) {
@@ -527,24 +536,26 @@ vmc_status vmc_peps_plan_set_operator(vmc_plan* pl, const double* onesite, const
   HostOp& op = pl->op;
   default_operator(pl);
   const int d = P.d, d2 = d * d, R = P.R, C = P.C;
+  // complex plans read (re, im) pairs for every matrix element
+  const size_t es = (size_t)P.es;
   if (onesite && onesite_mask) {
     for (int s = 0; s < P.n_sites; ++s) {
       op.onesite_mask[s] = onesite_mask[s] != 0;
-      for (int i = 0; i < d * d; ++i) op.onesite[(size_t)s * d * d + i] = (float)onesite[(size_t)s * d * d + i];
+      for (size_t i = 0; i < es * d * d; ++i) op.onesite[es * s * d * d + i] = (float)onesite[es * s * d * d + i];
     }
   }
   if (horiz && horiz_mask && C > 1) {
     for (int t = 0; t < R * (C - 1); ++t) {
       op.horiz_mask[t] = horiz_mask[t] != 0;
       if (op.horiz_mask[t]) op.row_has_h[t / (C - 1)] = 1;
-      for (int i = 0; i < d2 * d2; ++i) op.horiz[(size_t)t * d2 * d2 + i] = (float)horiz[(size_t)t * d2 * d2 + i];
+      for (size_t i = 0; i < es * d2 * d2; ++i) op.horiz[es * t * d2 * d2 + i] = (float)horiz[es * t * d2 * d2 + i];
     }
   }
   if (vert && vert_mask && R > 1) {
     for (int t = 0; t < (R - 1) * C; ++t) {
       op.vert_mask[t] = vert_mask[t] != 0;
       if (op.vert_mask[t]) op.row_has_v[t / C] = 1;
-      for (int i = 0; i < d2 * d2; ++i) op.vert[(size_t)t * d2 * d2 + i] = (float)vert[(size_t)t * d2 * d2 + i];
+      for (size_t i = 0; i < es * d2 * d2; ++i) op.vert[es * t * d2 * d2 + i] = (float)vert[es * t * d2 * d2 + i];
     }
   }
   if (n_diag > 0) {
