@@ -152,6 +152,21 @@ class PEPSEngine:
         if v & _abi.VMC_DEV_TIMEOUT:
             raise TimeoutError("engine reported a device-side timeout")
 
+    def amplitude(self, logamp, sign):
+        """psi from (log|psi|, sign) -- or (log|psi|, phase) for a complex engine."""
+        if self.complex:
+            return torch.exp(torch.complex(logamp, sign))
+        return sign * torch.exp(logamp)
+
+    def log_sign(self, amps):
+        """(log|psi|, sign or phase) of given amplitudes, the inverse of ``amplitude``."""
+        a = torch.as_tensor(amps, device=self.device)
+        if self.complex:
+            a = a.to(torch.complex128)
+            return torch.log(torch.abs(a)), torch.angle(a)
+        a = a.to(torch.float64)
+        return torch.log(torch.abs(a)), torch.sign(a)
+
     # ------------------------------------------------------------------ calls
     def init_cache(self, tensors, configs, cache=None):
         self._check_tensors(tensors)
