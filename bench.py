@@ -47,7 +47,7 @@ def _oracle_chunk(args):
 
     wname, n, seed = args
     w = WORKLOADS[wname]
-    T = random_tensors(w.shape, w.bond_dim, w.phys_dim, seed=0)
+    T = w.tensors(seed=0)
     n_sites = w.shape[0] * w.shape[1]
     cfg = initial_configs(n, n_sites, w.phys_dim, seed=seed).astype(np.int64)
     u = next(uniform_stream(n, n_sites, seed=seed))
@@ -164,7 +164,7 @@ def run_reference(args, rank, world):
     line = {
         "impl": "reference", "metric": metric_name(w), "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128" if w.dtype == "complex64" else "f64", "data": "synthetic",
         "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
                    "strategy": f"{w.strategy}({w.chi})", "model": w.model,
                    "chains_per_step": per * cores, "parallelism": "host processes"},
@@ -190,7 +190,8 @@ def e2e_public_api(w, n, rank, dev, ustream, args, barrier):
     n_sites = w.shape[0] * w.shape[1]
     strategy = {"ZipUp": ZipUp, "Variational": Variational}.get(w.strategy, lambda _: NoTruncation())(w.chi)
     model = PEPS(shape=w.shape, bond_dim=w.bond_dim, phys_dim=w.phys_dim, contraction_strategy=strategy,
-                 device=dev, tensors=random_tensors(w.shape, w.bond_dim, w.phys_dim, seed=0))
+                 device=dev, tensors=w.tensors(seed=0),
+                 dtype=torch.complex64 if w.dtype == "complex64" else torch.float32)
     init_cache, transition, estimate = build_mc_kernels(model, w.operator())
     sampler = make_mc_sampler(transition, estimate)
     cfg = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
@@ -248,8 +249,9 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device(f"cuda:{local_rank}")
     torch.cuda.set_device(dev)
     n_sites = w.shape[0] * w.shape[1]
-    eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev)
-    tens = torch.from_numpy(pack_tensors(random_tensors(w.shape, w.bond_dim, w.phys_dim, seed=0))).to(dev)
+    eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev,
+                     dtype=w.dtype)
+    tens = torch.from_numpy(pack_tensors(w.tensors(seed=0))).to(dev)
     cfg0 = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
     ustream = uniform_stream(n, n_sites, seed=1000 * rank)
     total = args.warmup + args.steps
@@ -325,7 +327,8 @@ def run_ours(args, rank, world, local_rank):
     line = {
         "metric": metric_name(w), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64" if w.dtype == "complex64" else "f32",
+        "data": "synthetic",
         "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
                    "phys_dim": w.phys_dim, "strategy": f"{w.strategy}({w.chi})", "model": w.model,
                    "chains_per_gpu": n, "global_chains": n * world, "parallelism": f"replicas x{world}",

@@ -24,6 +24,12 @@
  * Numerics: FP32 contractions with FP64 log-scales and FP64 energy
  * accumulation.  Amplitudes are returned as (log|psi|, sign); log-derivatives
  * O_k = dpsi/dA / psi are returned directly, so nothing underflows.
+ *
+ * Complex plans (VMC_DTYPE_C64, complex64 site tensors as in the reference's
+ * complex PEPS): every complex array is interleaved (re, im) -- the packed
+ * tensors and out_O as float pairs, out_E as double pairs, the operator
+ * tables of vmc_peps_plan_set_operator as double pairs -- and the "sign"
+ * arrays hold the phase of psi in radians (psi = exp(logamp + i phase)).
  */
 #ifndef VMC_GB300_H_
 #define VMC_GB300_H_
@@ -48,7 +54,7 @@ enum {
   VMC_ERR_SCRATCH = 7      /* plan needs more than the fixed scratch of vmc_peps_amp_grad_noalloc */
 };
 
-/* dtype of the site tensors (the engine computes in FP32 either way). */
+/* dtype of the site tensors: real FP32, or complex64 (FP32 real and imaginary parts). */
 enum { VMC_DTYPE_F32 = 0, VMC_DTYPE_C64 = 1 };
 
 /* Boundary-MPS strategy: strategy.py:44-92. */
@@ -94,7 +100,9 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
  *   (row-major site ids) in diag_sites[diag_site_off[t] ...] and its table of
  *   d^diag_nsites[t] values starts at diag_values[diag_value_off[t]].
  * The local-energy convention is the reference's: an off-diagonal term adds
- * sum_j op[j, s] psi(j) / psi (energy.py:176-200).
+ * sum_j op[j, s] psi(j) / psi (energy.py:176-200).  For a complex plan the
+ * onesite / horiz / vert tables hold (re, im) double pairs per element;
+ * diagonal tables stay real.
  */
 vmc_status vmc_peps_plan_set_operator(vmc_plan* plan,
                                       const double* onesite, const int* onesite_mask,

@@ -43,6 +43,21 @@ def oracle_sweep(tensors, shape, bond_dim, strategy, chi, operator, configs, uni
     return c2, ctx, le
 
 
+def complex_tensors(shape, bond_dim, seed=0, phys_dim=2):
+    """Complex PEPS: re and im i.i.d. N(0,1)/sqrt(2 d D^4), rounded to complex64 (the engine's input)."""
+    rng = np.random.default_rng(seed)
+    n_rows, n_cols = shape
+    out = []
+    for r in range(n_rows):
+        row = []
+        for c in range(n_cols):
+            sh = (phys_dim,) + oracle.PEPS.site_dims(r, c, n_rows, n_cols, bond_dim)
+            t = (rng.standard_normal(sh) + 1j * rng.standard_normal(sh)) / np.sqrt(2 * phys_dim * bond_dim ** 4)
+            row.append(t.astype(np.complex64).astype(np.complex128))
+        out.append(row)
+    return out
+
+
 def make_case(shape, bond_dim, n_chains, seed=0, phys_dim=2):
     T = random_tensors(shape, bond_dim, phys_dim, seed=seed)
     n_sites = shape[0] * shape[1]

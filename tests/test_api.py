@@ -214,3 +214,54 @@ def test_tdvp_checkpoint_resumes_bit_identically(emu_lib, tmp_path):
     assert a.energy == b.energy
     with pytest.raises(ValueError):
         _checkpoint_driver(emu_lib, n_chains=4).load(tmp_path / "driver.pt")
+
+
+def test_complex_peps_apply_autograd_and_log_value(emu_lib):
+    """Complex PEPS through the public surface (host-emulation engine): amplitudes and log psi, and
+    torch's convention for the holomorphic amplitude, grad of Re(sum w psi) = conj(sum w dpsi/dA)."""
+    from tests.helpers import complex_tensors
+    from vmc_gb300 import NoTruncation, PEPS
+    from vmc_gb300.compat import peps_apply
+
+    shape, D = (2, 3), 2
+    T = complex_tensors(shape, D, seed=6)
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=NoTruncation(), tensors=T, device="cpu",
+                 lib=emu_lib, dtype=torch.complex64)
+    samples = exact.all_configs(6)[::5]
+    packed = model.packed().clone().requires_grad_(True)
+    amp = peps_apply(packed, torch.from_numpy(samples), shape, model.strategy, model=model)
+    om = oracle.PEPS(T, shape, D, strategy=oracle.NoTruncation())
+    a_ref, g_ref, _ = oracle.value_and_grad(om, samples, full_gradient=True)
+    assert amp.dtype == torch.complex128
+    assert np.max(np.abs(amp.detach().numpy() / a_ref - 1)) < 2e-5
+    w = torch.linspace(-1, 1, amp.shape[0], dtype=torch.float64)
+    (amp * w).real.sum().backward()
+    expect = np.conj((w.numpy()[:, None] * g_ref).sum(0))
+    assert np.linalg.norm(packed.grad.numpy() - expect) / np.linalg.norm(expect) < 1e-4
+    logpsi = model(torch.from_numpy(samples))
+    assert torch.allclose(torch.exp(logpsi), amp.detach(), rtol=1e-5)
+
+
+def test_real_time_tdvp_on_a_complex_peps(emu_lib):
+    """tdvp.py with RealTimeUnit (grad factor -i) needs complex parameters: one RK4 step runs on a
+    complex PEPS and keeps the parameters complex; a real PEPS is refused."""
+    from vmc_gb300 import PEPS, ZipUp
+    from vmc_gb300.drivers import RealTimeUnit, TDVPDriver
+    from vmc_gb300.preconditioners import SRPreconditioner
+    from vmc_gb300.qgt import SampleSpace
+
+    shape, D = (2, 3), 2
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(4), device="cpu", lib=emu_lib,
+                 dtype=torch.complex64, rngs=1)
+    drv = TDVPDriver(model, transverse_field_ising(shape), dt=0.01, time_unit=RealTimeUnit(),
+                     preconditioner=SRPreconditioner(space=SampleSpace(), diag_shift=1e-2), n_samples=16,
+                     n_chains=8)
+    before = [[t.clone() for t in row] for row in drv._tensors]
+    drv.run(0.01)
+    assert drv.step_count == 1 and drv._tensors[0][0].dtype == torch.complex64
+    delta = sum(float((a - b).abs().sum()) for ra, rb in zip(drv._tensors, before) for a, b in zip(ra, rb))
+    assert np.isfinite(delta) and delta > 0
+    real_model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(4), device="cpu", lib=emu_lib)
+    with pytest.raises(NotImplementedError):
+        TDVPDriver(real_model, transverse_field_ising(shape), dt=0.01, time_unit=RealTimeUnit(),
+                   preconditioner=SRPreconditioner())

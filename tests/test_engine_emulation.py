@@ -12,7 +12,7 @@ import pytest
 import torch
 
 from oracle import peps as oracle
-from tests.helpers import assert_parity, fp32, hamiltonian, make_case, oracle_sweep
+from tests.helpers import assert_parity, complex_tensors, fp32, hamiltonian, make_case, oracle_sweep
 from vmc_gb300 import _abi
 from vmc_gb300.engine import PEPSEngine
 from vmc_gb300.lowering import pack_tensors
@@ -252,6 +252,61 @@ def test_wide_lattice_environments_stay_in_range(emu_lib, shape):
     assert_parity(np.linalg.norm(res.O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
 
 
+COMPLEX_CASES = [
+    ((3, 3), 2, 16, "NoTruncation", "heisenberg"),
+    ((3, 3), 3, 4, "ZipUp", "tfim"),
+    ((4, 4), 2, 4, "ZipUp", "heisenberg"),
+    ((3, 4), 2, 3, "Variational", "heisenberg"),
+]
+
+
+@pytest.mark.parametrize("shape,D,chi,strategy,model", COMPLEX_CASES)
+@pytest.mark.parametrize("full", [False, True])
+def test_complex_sweep_matches_oracle(emu_lib, shape, D, chi, strategy, model, full):
+    """complex64 PEPS (interleaved (re, im) elements): complex Gram / Householder truncation, bilinear
+    amplitudes, complex O_k and E_loc against the complex128 oracle."""
+    H = hamiltonian(model, shape)
+    T = complex_tensors(shape, D, seed=D + chi)
+    rng = np.random.default_rng(3)
+    n_sites = shape[0] * shape[1]
+    cfg = rng.integers(0, 2, (5, n_sites)).astype(np.int32)
+    u = rng.random((5, n_sites))
+    eng = PEPSEngine(shape, D, chi, 2, strategy, operator=H, device="cpu", lib=emu_lib, dtype="complex64")
+    tens = torch.from_numpy(pack_tensors(T))
+    c = torch.from_numpy(cfg.copy())
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, torch.from_numpy(u), cache, full_gradient=full)
+    c2, ctx, le = oracle_sweep(T, shape, D, strategy, chi, H, cfg, u, full_gradient=full)
+    assert np.array_equal(res.configs.numpy(), c2)
+    trunc = strategy != "NoTruncation"
+    amp = np.exp(res.logamp.numpy() + 1j * res.sign.numpy())
+    assert_parity(np.abs(amp / ctx.amp - 1), trunc)
+    e_ref = le.local_estimate
+    assert res.E.dtype == torch.complex128
+    assert_parity(np.abs(res.E.numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), trunc)
+    o_ref = le.local_log_derivatives
+    assert_parity(np.linalg.norm(res.O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), trunc)
+    assert eng.status() == 0
+
+
+def test_complex_amp_grad_and_local_energy(emu_lib):
+    shape, D, chi = (4, 4), 2, 4
+    H = hamiltonian("heisenberg", shape)
+    T = complex_tensors(shape, D, seed=9)
+    cfg = np.random.default_rng(4).integers(0, 2, (6, 16)).astype(np.int32)
+    eng = PEPSEngine(shape, D, chi, 2, "ZipUp", operator=H, device="cpu", lib=emu_lib, dtype="complex64")
+    tens = torch.from_numpy(pack_tensors(T))
+    la, ph, O = eng.amp_grad(tens, torch.from_numpy(cfg))
+    E = eng.local_energy(tens, torch.from_numpy(cfg), la, ph)
+    model = oracle.PEPS(T, shape, D, strategy=oracle.ZipUp(chi))
+    amp, grads, _ = oracle.value_and_grad(model, cfg)
+    assert_parity(np.abs(np.exp(la.numpy() + 1j * ph.numpy()) / amp - 1), True)
+    o_ref = grads / amp[:, None]
+    assert_parity(np.linalg.norm(O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
+    e_ref = oracle.local_estimate(model, cfg, H, amp)
+    assert_parity(np.abs(E.numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
+
+
 def test_invalid_arguments_return_status_codes(emu_lib):
     import ctypes as ct
 
@@ -259,7 +314,7 @@ def test_invalid_arguments_return_status_codes(emu_lib):
     bad = _abi.VmcShape(0, 3)
     assert emu_lib.vmc_peps_plan(ct.byref(bad), 2, 4, 2, 0, 1, 2, ct.byref(plan)) == _abi.VMC_ERR_INVALID
     ok = _abi.VmcShape(3, 3)
-    assert emu_lib.vmc_peps_plan(ct.byref(ok), 2, 4, 2, 1, 1, 2, ct.byref(plan)) == _abi.VMC_ERR_UNSUPPORTED
+    assert emu_lib.vmc_peps_plan(ct.byref(ok), 2, 4, 2, 7, 1, 2, ct.byref(plan)) == _abi.VMC_ERR_UNSUPPORTED
     assert emu_lib.vmc_peps_plan(ct.byref(ok), 2, 4, 9, 0, 1, 2, ct.byref(plan)) == _abi.VMC_ERR_UNSUPPORTED
     assert emu_lib.vmc_peps_plan(ct.byref(ok), 2, 4, 2, 0, 1, 2, ct.byref(plan)) == _abi.VMC_OK
     cfg = np.zeros((2, 9), np.int32)

@@ -14,7 +14,7 @@ import torch
 
 from oracle import peps as oracle
 from tests.helpers import (CONFIG2_MAX_TOL, CONFIG2_MEDIAN_TOL, TRUNC_MAX_TOL, TRUNC_MEDIAN_TOL, assert_parity,
-                           fp32, hamiltonian, make_case, oracle_sweep)
+                           complex_tensors, fp32, hamiltonian, make_case, oracle_sweep)
 from vmc_gb300.engine import PEPSEngine
 from vmc_gb300.lowering import pack_tensors
 
@@ -150,3 +150,40 @@ def test_two_sweeps_match_oracle_sampler(cuda_device):
     assert same.mean() > 0.9
     e_ref = le.local_estimate[1][same]
     assert_parity(np.abs(res.E.cpu().numpy()[same] - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
+
+
+COMPLEX_CASES = [
+    ((3, 3), 2, 16, "NoTruncation", "heisenberg"),
+    ((4, 4), 3, 6, "ZipUp", "tfim"),
+    ((4, 4), 3, 6, "ZipUp", "heisenberg"),
+    ((3, 4), 2, 3, "Variational", "heisenberg"),
+]
+
+
+@pytest.mark.parametrize("shape,D,chi,strategy,model", COMPLEX_CASES)
+@pytest.mark.parametrize("full", [False, True])
+def test_complex_sweep_matches_oracle(cuda_device, shape, D, chi, strategy, model, full):
+    """complex64 PEPS against the complex128 oracle (amplitude log|psi| + i phase, complex O_k, E_loc)."""
+    H = hamiltonian(model, shape)
+    T = complex_tensors(shape, D, seed=D + chi)
+    n_sites = shape[0] * shape[1]
+    rng = np.random.default_rng(3)
+    cfg = rng.integers(0, 2, (32, n_sites)).astype(np.int32)
+    u = rng.random((32, n_sites))
+    eng = PEPSEngine(shape, D, chi, 2, strategy, operator=H, device=cuda_device, dtype="complex64")
+    tens = torch.from_numpy(pack_tensors(T)).to(cuda_device)
+    c = torch.from_numpy(cfg.copy()).to(cuda_device)
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, torch.from_numpy(u).to(cuda_device), cache, full_gradient=full)
+    torch.cuda.synchronize()
+    eng.raise_on_status()
+    c2, ctx, le = oracle_sweep(T, shape, D, strategy, chi, H, cfg, u, full_gradient=full)
+    same = np.all(res.configs.cpu().numpy() == c2, axis=1)
+    assert np.all(same | (res.margin.cpu().numpy() < 1e-4)) and same.mean() > 0.9
+    trunc = strategy != "NoTruncation"
+    amp = np.exp(res.logamp.cpu().numpy() + 1j * res.sign.cpu().numpy())
+    assert_parity(np.abs(amp[same] / ctx.amp[same] - 1), trunc)
+    e, e_ref = res.E.cpu().numpy()[same], le.local_estimate[same]
+    assert_parity(np.abs(e - e_ref) / np.maximum(1.0, np.abs(e_ref)), trunc)
+    o, o_ref = res.O.cpu().numpy()[same], le.local_log_derivatives[same]
+    assert_parity(np.linalg.norm(o - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), trunc)

@@ -64,6 +64,40 @@ def test_torch_sr_matches_oracle(space):
     assert abs(float(metrics["residual_error"]) - m_ref["residual_error"]) < 1e-8 * max(1.0, m_ref["residual_error"])
 
 
+class _ComplexModel(_Model):
+    def __init__(self, shape, D, d, tensors):
+        self.shape, self.bond_dim, self.phys_dim = shape, D, d
+        self.dtype = torch.complex64
+        self.tensors = [[torch.as_tensor(t, dtype=torch.complex64) for t in row] for row in tensors]
+
+
+@pytest.mark.parametrize("space", ["param", "sample"])
+@pytest.mark.parametrize("grad_factor", [-1.0, -1.0j])
+def test_complex_sr_matches_oracle(space, grad_factor):
+    """Complex parameters: complex O, complex E_loc, imaginary (-1) and real (-i) time; no 2 Re(x)."""
+    from tests.helpers import complex_tensors
+
+    shape, D = (2, 3), 2
+    T = complex_tensors(shape, D, seed=4)
+    model = oracle.PEPS(T, shape, D, strategy=oracle.NoTruncation())
+    rng = np.random.default_rng(7)
+    cfg = rng.integers(0, 2, size=(40, 6))
+    amps, grads, p = oracle.value_and_grad(model, cfg)
+    o = grads / amps[:, None]
+    e = rng.standard_normal(40) + 1j * rng.standard_normal(40)
+    sd = oracle.sliced_dims(model)
+    x_ref, _ = osr.sr_apply(o, p, e, pps=oracle.params_per_site(model), sliced_dims=sd, n_samples=40,
+                            diag_shift=1e-3, grad_factor=grad_factor, real_params=False,
+                            space=osr.ParameterSpace() if space == "param" else osr.SampleSpace())
+    pre = SRPreconditioner(space=gq.ParameterSpace() if space == "param" else gq.SampleSpace(), diag_shift=1e-3)
+    m = _ComplexModel(shape, D, 2, T)
+    upd, _ = pre.apply(m, m.tensors, torch.zeros((40, 6)), torch.as_tensor(o), torch.as_tensor(p),
+                       torch.as_tensor(e), grad_factor=grad_factor)
+    flat = torch.cat([u.reshape(-1) for row in upd for u in row]).to(torch.complex128).numpy()
+    assert upd[0][0].dtype == torch.complex64
+    assert np.linalg.norm(flat - x_ref) / np.linalg.norm(x_ref) < 1e-5
+
+
 def test_sample_space_gram_blocked_equals_dense():
     shape, D, T, om, o, p, e = _data(64, 3)
     sd = oracle.sliced_dims(om)

@@ -47,17 +47,22 @@ class _PepsAmplitude(torch.autograd.Function):
     def forward(ctx, packed, samples, engine):
         logamp, sign, O = engine.amp_grad(packed.detach().contiguous(), samples, full_gradient=True,
                                           want_O=packed.requires_grad)
-        amp = sign * torch.exp(logamp)
+        amp = engine.amplitude(logamp, sign)
         if O is not None:
             ctx.save_for_backward(O, amp)
+        ctx.param_dtype = packed.dtype
         return amp
 
     @staticmethod
     def backward(ctx, g):
         O, amp = ctx.saved_tensors
-        # d amp_i / d theta = amp_i * O_i  (O = dpsi/dtheta / psi, full layout)
-        grad = ((g * amp)[:, None] * O.to(torch.float64)).sum(0)
-        return grad.to(torch.float32), None, None
+        # d amp_i / d theta = amp_i * O_i  (O = dpsi/dtheta / psi, full layout); psi is holomorphic in
+        # theta, so in torch's convention grad_theta = sum_i g_i * conj(amp_i O_i)
+        if amp.is_complex():
+            grad = (g[:, None] * torch.conj(amp[:, None] * O.to(torch.complex128))).sum(0)
+        else:
+            grad = ((g * amp)[:, None] * O.to(torch.float64)).sum(0)
+        return grad.to(ctx.param_dtype), None, None
 
 
 def peps_apply(tensors, sample, shape, strategy, model=None):
@@ -76,16 +81,16 @@ def peps_apply(tensors, sample, shape, strategy, model=None):
 
 
 def log_value(model, samples, tensors=None):
-    """(log|psi|, sign) for a batch; never underflows."""
+    """(log|psi|, sign) for a batch -- (log|psi|, phase) for a complex model; never underflows."""
     eng = model.engine()
     logamp, sign, _ = eng.amp_grad(model.packed(tensors), _samples(model, samples), want_O=False)
     return logamp, sign
 
 
 def _value(model, sample):
-    """compat.py:67-78 (float64 amplitudes)."""
+    """compat.py:67-78 (float64 / complex128 amplitudes)."""
     la, sg = log_value(model, sample)
-    amp = sg * torch.exp(la)
+    amp = model.engine().amplitude(la, sg)
     return amp if torch.as_tensor(sample).ndim > 1 else amp[0]
 
 
@@ -94,8 +99,8 @@ def _value_and_grad(model, sample, *, full_gradient=False):
     eng = model.engine()
     s = _samples(model, sample)
     logamp, sign, O = eng.amp_grad(model.packed(), s, full_gradient=full_gradient, want_O=True)
-    amp = sign * torch.exp(logamp)
-    grads = O.to(torch.float64) * amp[:, None]
+    amp = eng.amplitude(logamp, sign)
+    grads = O.to(amp.dtype) * amp[:, None]
     p = None
     if not full_gradient:
         pps = torch.as_tensor(params_per_site(model.shape, model.bond_dim), device=s.device)
@@ -114,12 +119,11 @@ def _grad(model, sample, *, full_gradient=False):
 def local_estimate(model, samples, operator, amps):
     """compat.py:136-194: E_loc with the caller's amplitudes as denominators.
 
-    ``amps`` is a tensor of amplitudes or a (log|psi|, sign) pair."""
+    ``amps`` is a tensor of amplitudes or a (log|psi|, sign-or-phase) pair."""
     eng = model.engine(operator)
     s = _samples(model, samples)
     if isinstance(amps, tuple):
         logamp, sign = amps
     else:
-        a = torch.as_tensor(amps, device=s.device, dtype=torch.float64)
-        logamp, sign = torch.log(torch.abs(a)), torch.sign(a)
+        logamp, sign = eng.log_sign(amps)
     return eng.local_energy(model.packed(), s, logamp, sign)

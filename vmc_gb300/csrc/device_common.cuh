@@ -55,7 +55,87 @@ struct Gemm {
   IMap cm, cn;
   float alpha;
   int accumulate;  // 1: C += alpha*AB, 0: C = alpha*AB
+  // complex elements: every index map and stride counts elements of two
+  // floats (re, im); conja / conjb conjugate the operand, alpha_im is the
+  // imaginary part of alpha
+  int cplx;
+  int conja, conjb;
+  float alpha_im;
 };
+
+// Complex variant of gemm_tiles: interleaved (re, im) elements.
+template <int TM, int TN>
+__device__ __forceinline__ void gemm_tiles_c(const Gemm& g) {
+  const int tiles_m = (g.M + TM - 1) / TM;
+  const int tiles_n = (g.N + TN - 1) / TN;
+  const int n_tiles = tiles_m * tiles_n;
+  const float sa = g.conja ? -1.f : 1.f, sb = g.conjb ? -1.f : 1.f;
+  for (int t = threadIdx.x; t < n_tiles; t += blockDim.x) {
+    const int tn = t % tiles_n;
+    const int tm = t / tiles_n;
+    int aoff[TM], boff[TN];
+    bool mv[TM], nv[TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      int m = tm + i * tiles_m;
+      mv[i] = m < g.M;
+      aoff[i] = 2 * imap(g.am, mv[i] ? m : 0);
+    }
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      int n = tn + j * tiles_n;
+      nv[j] = n < g.N;
+      boff[j] = 2 * imap(g.bn, nv[j] ? n : 0);
+    }
+    float cr[TM][TN], ci[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) cr[i][j] = ci[i][j] = 0.f;
+    const int ska = 2 * g.sak, skb = 2 * g.sbk;
+    for (int k = 0; k < g.K; ++k) {
+      float ar[TM], ai[TM], br[TN], bi[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) {
+        const float* pa = g.A + aoff[i] + k * ska;
+        ar[i] = pa[0];
+        ai[i] = sa * pa[1];
+      }
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const float* pb = g.B + boff[j] + k * skb;
+        br[j] = pb[0];
+        bi[j] = sb * pb[1];
+      }
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+          cr[i][j] = fmaf(ar[i], br[j], fmaf(-ai[i], bi[j], cr[i][j]));
+          ci[i][j] = fmaf(ar[i], bi[j], fmaf(ai[i], br[j], ci[i][j]));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      if (!mv[i]) continue;
+      const int co = imap(g.cm, tm + i * tiles_m);
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        if (!nv[j]) continue;
+        float* dst = g.C + 2 * (co + imap(g.cn, tn + j * tiles_n));
+        const float vr = g.alpha * cr[i][j] - g.alpha_im * ci[i][j];
+        const float vi = g.alpha * ci[i][j] + g.alpha_im * cr[i][j];
+        if (g.accumulate) {
+          dst[0] += vr;
+          dst[1] += vi;
+        } else {
+          dst[0] = vr;
+          dst[1] = vi;
+        }
+      }
+    }
+  }
+}
 
 // Each thread owns a TM x TN tile whose rows and columns are interleaved
 // with stride tiles_m / tiles_n, so consecutive lanes touch consecutive rows
@@ -194,6 +274,17 @@ __device__ inline void gemm_mma(const Gemm& g) {
 __device__ inline void cta_gemm(const Gemm& g) {
   const int work = g.M * g.N;
   const int nt = blockDim.x;
+  if (g.cplx) {
+    if (g.M >= 4 && g.N >= 2 && work >= nt * 8) {
+      gemm_tiles_c<4, 2>(g);
+    } else if (g.M >= 2 && g.N >= 2 && work >= nt * 4) {
+      gemm_tiles_c<2, 2>(g);
+    } else {
+      gemm_tiles_c<1, 1>(g);
+    }
+    __syncthreads();
+    return;
+  }
 #ifndef VMC_HOST_EMULATION
   if (kGemmTensorCores && g.M >= 16 && g.N >= 8 && g.K >= 8 && work >= nt * 32) {
     gemm_mma(g);
@@ -218,6 +309,7 @@ __device__ inline Gemm make_gemm(const float* A, IMap am, int sak, const float* 
   g.A = A; g.B = B; g.C = C; g.M = M; g.N = N; g.K = K;
   g.am = am; g.sak = sak; g.bn = bn; g.sbk = sbk; g.cm = cm; g.cn = cn;
   g.alpha = alpha; g.accumulate = accumulate;
+  g.cplx = 0; g.conja = 0; g.conjb = 0; g.alpha_im = 0.f;
   return g;
 }
 
@@ -302,6 +394,21 @@ __device__ inline void cta_dots_all(const float* const* x, const float* const* y
     acc[j] += r;
   }
   __syncthreads();
+}
+
+// Bilinear complex dot sum_i x_i y_i over n interleaved (re, im) elements;
+// returns the real part, *im the imaginary part.  FP32 partials per thread,
+// double across the CTA.
+__device__ inline double cta_cdot(const float* x, const float* y, int n, double* red, double* im) {
+  float sr = 0.f, si = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float xr = x[2 * i], xi = x[2 * i + 1], yr = y[2 * i], yi = y[2 * i + 1];
+    sr = fmaf(xr, yr, fmaf(-xi, yi, sr));
+    si = fmaf(xr, yi, fmaf(xi, yr, si));
+  }
+  const double re = cta_sum((double)sr, red);
+  *im = cta_sum((double)si, red);
+  return re;
 }
 
 __device__ inline void cta_copy(float* dst, const float* src, int n) {

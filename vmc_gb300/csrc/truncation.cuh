@@ -491,6 +491,7 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
 // Scratch for cta_sym_topk (all pointers into shared or global memory).
 struct EigScratch {
   float *d, *e, *e2, *tau, *v, *p, *lam, *cvec, *part;
+  float* yr;               // complex solves: real n*k eigenvectors of T before the back-transform
   float* S;                // k*k
   float* lu;               // k * 4 * n
   unsigned char* sw;       // k * n
@@ -500,11 +501,10 @@ struct EigScratch {
 // Y (n x k, row stride ldy) <- orthonormal basis of the dominant k-dimensional
 // invariant subspace of the symmetric matrix G (destroyed).  lam[0..kk-1]
 // receives the kk = min(k+1, n) largest eigenvalues.
-__device__ inline void cta_sym_topk(float* G, int n, int ldg, int k, float* Y, int ldy, const EigScratch& w,
-                                    double* red) {
-  VMC_TSTART(t0);
-  cta_tridiagonalize(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);
-  VMC_TSTOP(t0, PH_TRIDIAG);
+// Y (n x k, real, row stride ldy) <- orthonormal eigenvectors of the k
+// largest eigenvalues of the tridiagonal (w.d, w.e); w.lam receives the
+// min(k+1, n) largest eigenvalues.
+__device__ inline void tri_topk_vectors(int n, int k, float* Y, int ldy, const EigScratch& w, double* red) {
   VMC_TSTART(t1);
   const int kk = k + 1 <= n ? k + 1 : n;
   const float tnorm = cta_top_eigenvalues(w.d, w.e, w.e2, n, kk, w.lam);
@@ -538,8 +538,179 @@ __device__ inline void cta_sym_topk(float* G, int n, int ldg, int k, float* Y, i
   const bool ok = cta_cholqr(Y, n, k, ldy, w.S, w.flag);
   if (!ok) cta_mgs(Y, n, k, ldy, red);
   VMC_TSTOP(t3, PH_CHOLQR);
+}
+
+__device__ inline void cta_sym_topk(float* G, int n, int ldg, int k, float* Y, int ldy, const EigScratch& w,
+                                    double* red) {
+  VMC_TSTART(t0);
+  cta_tridiagonalize(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);
+  VMC_TSTOP(t0, PH_TRIDIAG);
+  tri_topk_vectors(n, k, Y, ldy, w, red);
   VMC_TSTART(t4);
   cta_back_transform(G, n, ldg, w.tau, Y, k, ldy, w.cvec);
+  VMC_TSTOP(t4, PH_BACK);
+}
+
+// ---------------------------------------------------------------------------
+// Complex Hermitian variants.  Complex elements are interleaved (re, im)
+// floats; leading dimensions count elements.
+// ---------------------------------------------------------------------------
+
+// Householder tridiagonalisation of the Hermitian n x n matrix A (full storage,
+// both triangles kept current), as LAPACK's zhetd2 does it: each reflector
+// H_j = I - tau_j v_j v_j^H has a real beta, so T = Q^H A Q is real symmetric
+// tridiagonal (d, e) with Q = H_0 ... H_{n-2}; the last step only rotates a
+// phase.  tau (complex) and A[j+1+i][j] (i >= 1; v_j[0] = 1 implicit) hold the
+// reflectors.  v, p: n complex scratch; part: >= 64 floats.  For one column:
+//   p = tau A v,   w = p - (tau/2) (p^H v) v,   A -= v w^H + w v^H.
+__device__ inline void cta_tridiagonalize_c(float* A, int n, int lda, float* d, float* e, float* tau, float* v,
+                                            float* p, float* part) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int nl = nt < 32 ? nt : 32;
+  const int lane = tid % nl, warp = tid / nl, nwarps = nt / nl;
+  auto re = [&](int i, int j) -> float& { return A[2 * ((size_t)i * lda + j)]; };
+  auto im = [&](int i, int j) -> float& { return A[2 * ((size_t)i * lda + j) + 1]; };
+  if (n == 1) {
+    if (tid == 0) d[0] = A[0];
+    __syncthreads();
+    return;
+  }
+  for (int j = 0; j < n - 1; ++j) {
+    const int m = n - j - 1;  // length of the reflected vector (rows j+1..n-1)
+    // |x|^2 of A[j+2.., j], one warp
+    if (warp == 0) {
+      float s = 0.f;
+      for (int i = j + 2 + lane; i < n; i += nl) s = fmaf(re(i, j), re(i, j), fmaf(im(i, j), im(i, j), s));
+      s = warp_sum_f(s);
+      if (lane == 0) part[0] = s;
+    }
+    __syncthreads();
+    const float xn2 = part[0];
+    const float ar = re(j + 1, j), ai = im(j + 1, j);
+    float tr = 0.f, ti = 0.f, beta = ar, sr = 0.f, si = 0.f;
+    if (xn2 > 0.f || ai != 0.f) {
+      beta = -copysignf(sqrtf(ar * ar + ai * ai + xn2), ar);
+      tr = (beta - ar) / beta;
+      ti = -ai / beta;
+      // scal = 1 / (alpha - beta)
+      const float dr = ar - beta, di = ai, den = dr * dr + di * di;
+      sr = dr / den;
+      si = -di / den;
+    }
+    // v (rows j+1..): v_0 = 1, v_i = x_i * scal; column j keeps x until barrier (2)
+    for (int i = tid; i < m; i += nt) {
+      if (i == 0) {
+        v[0] = 1.f;
+        v[1] = 0.f;
+      } else {
+        const float xr = re(j + 1 + i, j), xi = im(j + 1 + i, j);
+        v[2 * i] = xr * sr - xi * si;
+        v[2 * i + 1] = xr * si + xi * sr;
+      }
+    }
+    if (tid == 0) {
+      d[j] = re(j, j);
+      e[j] = beta;
+      tau[2 * j] = tr;
+      tau[2 * j + 1] = ti;
+    }
+    __syncthreads();  // (1) v visible
+    if (tr == 0.f && ti == 0.f) continue;
+    // p = tau * A_sub v (one thread per row)
+    for (int i = tid; i < m; i += nt) {
+      float yr = 0.f, yi = 0.f;
+      for (int l = 0; l < m; ++l) {
+        const float a_r = re(j + 1 + i, j + 1 + l), a_i = im(j + 1 + i, j + 1 + l);
+        const float vr = v[2 * l], vi = v[2 * l + 1];
+        yr = fmaf(a_r, vr, fmaf(-a_i, vi, yr));
+        yi = fmaf(a_r, vi, fmaf(a_i, vr, yi));
+      }
+      p[2 * i] = tr * yr - ti * yi;
+      p[2 * i + 1] = tr * yi + ti * yr;
+    }
+    __syncthreads();  // (2) p visible
+    // c = p^H v; K = (tau / 2) c
+    float cr = 0.f, ci = 0.f;
+    for (int i = 0; i < m; ++i) {
+      const float pr = p[2 * i], pi = -p[2 * i + 1], vr = v[2 * i], vi = v[2 * i + 1];
+      cr = fmaf(pr, vr, fmaf(-pi, vi, cr));
+      ci = fmaf(pr, vi, fmaf(pi, vr, ci));
+    }
+    const float kr = 0.5f * (tr * cr - ti * ci), ki = 0.5f * (tr * ci + ti * cr);
+    // reflector into column j, rank-2 update of the trailing matrix:
+    // A[i][l] -= v_i conj(w_l) + w_i conj(v_l),  w = p - K v
+    for (int i = 1 + tid; i < m; i += nt) {
+      re(j + 1 + i, j) = v[2 * i];
+      im(j + 1 + i, j) = v[2 * i + 1];
+    }
+    for (int e2 = tid; e2 < m * m; e2 += nt) {
+      const int i = e2 / m, l = e2 - i * m;
+      const float vir = v[2 * i], vii = v[2 * i + 1], vlr = v[2 * l], vli = v[2 * l + 1];
+      const float wir = p[2 * i] - (kr * vir - ki * vii), wii = p[2 * i + 1] - (kr * vii + ki * vir);
+      const float wlr = p[2 * l] - (kr * vlr - ki * vli), wli = p[2 * l + 1] - (kr * vli + ki * vlr);
+      // v_i conj(w_l) + w_i conj(v_l)
+      const float ur = (vir * wlr + vii * wli) + (wir * vlr + wii * vli);
+      const float ui = (vii * wlr - vir * wli) + (wii * vlr - wir * vli);
+      re(j + 1 + i, j + 1 + l) -= ur;
+      im(j + 1 + i, j + 1 + l) -= ui;
+    }
+    __syncthreads();  // (3) trailing matrix updated
+  }
+  if (tid == 0) d[n - 1] = re(n - 1, n - 1);
+  __syncthreads();
+}
+
+// Y (n x k complex, row stride ldy) <- Q Y with Q = H_0 ... H_{n-2} from
+// cta_tridiagonalize_c (H_j = I - tau_j v_j v_j^H applied for j descending).
+__device__ inline void cta_back_transform_c(const float* A, int n, int lda, const float* tau, float* Y, int k,
+                                            int ldy, float* cvec) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int j = n - 2; j >= 0; --j) {
+    const float tr = tau[2 * j], ti = tau[2 * j + 1];
+    if (tr == 0.f && ti == 0.f) continue;
+    const int m = n - j - 1;
+    // c_t = tau * sum_i conj(v_i) Y[j+1+i][t]
+    for (int t = tid; t < k; t += nt) {
+      float sr = 0.f, si = 0.f;
+      for (int i = 0; i < m; ++i) {
+        const float vr = i == 0 ? 1.f : A[2 * ((size_t)(j + 1 + i) * lda + j)];
+        const float vi = i == 0 ? 0.f : -A[2 * ((size_t)(j + 1 + i) * lda + j) + 1];
+        const float yr = Y[2 * ((size_t)(j + 1 + i) * ldy + t)], yi = Y[2 * ((size_t)(j + 1 + i) * ldy + t) + 1];
+        sr = fmaf(vr, yr, fmaf(-vi, yi, sr));
+        si = fmaf(vr, yi, fmaf(vi, yr, si));
+      }
+      cvec[2 * t] = tr * sr - ti * si;
+      cvec[2 * t + 1] = tr * si + ti * sr;
+    }
+    __syncthreads();
+    for (int e2 = tid; e2 < m * k; e2 += nt) {
+      const int i = e2 / k, t = e2 - i * k;
+      const float vr = i == 0 ? 1.f : A[2 * ((size_t)(j + 1 + i) * lda + j)];
+      const float vi = i == 0 ? 0.f : A[2 * ((size_t)(j + 1 + i) * lda + j) + 1];
+      float* y = Y + 2 * ((size_t)(j + 1 + i) * ldy + t);
+      y[0] -= vr * cvec[2 * t] - vi * cvec[2 * t + 1];
+      y[1] -= vr * cvec[2 * t + 1] + vi * cvec[2 * t];
+    }
+    __syncthreads();
+  }
+}
+
+// Y (n x k complex, ldy) <- orthonormal basis of the dominant k-dimensional
+// invariant subspace of the Hermitian matrix G (complex, destroyed).
+__device__ inline void cta_herm_topk(float* G, int n, int ldg, int k, float* Y, int ldy, const EigScratch& w,
+                                     double* red) {
+  VMC_TSTART(t0);
+  cta_tridiagonalize_c(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);
+  VMC_TSTOP(t0, PH_TRIDIAG);
+  tri_topk_vectors(n, k, w.yr, k, w, red);
+  for (int e2 = threadIdx.x; e2 < n * k; e2 += blockDim.x) {
+    const int i = e2 / k, t = e2 - i * k;
+    Y[2 * ((size_t)i * ldy + t)] = w.yr[e2];
+    Y[2 * ((size_t)i * ldy + t) + 1] = 0.f;
+  }
+  __syncthreads();
+  VMC_TSTART(t4);
+  cta_back_transform_c(G, n, ldg, w.tau, Y, k, ldy, w.cvec);
   VMC_TSTOP(t4, PH_BACK);
 }
 

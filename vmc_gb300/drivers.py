@@ -3,8 +3,8 @@
 
 State is the list-of-lists of site tensors; the derivative is the SR update
 computed from one engine sampling run (init_cache + n_steps fused sweeps).
-The engine evaluates real PEPS, so real-time evolution (grad factor -i, which
-makes the parameters complex) raises NotImplementedError.
+Real-time evolution (grad factor -i) needs complex parameters: it runs on a
+complex PEPS and raises NotImplementedError for a real one.
 """
 from __future__ import annotations
 
@@ -91,8 +91,8 @@ class TDVPDriver:
     def __init__(self, model, operator, *, preconditioner: SRPreconditioner, dt: float, t0: float = 0.0,
                  time_unit: TimeUnit = RealTimeUnit(), integrator: Integrator | None = None, sampler_key=0,
                  n_samples: int = 1, n_chains: int = 1, full_gradient: bool = False):
-        if isinstance(time_unit.grad_factor, complex):
-            raise NotImplementedError("real-time TDVP needs complex parameters; the engine evaluates real PEPS")
+        if isinstance(time_unit.grad_factor, complex) and not getattr(model, "is_complex", False):
+            raise NotImplementedError("real-time TDVP needs complex parameters: use a complex PEPS")
         self._model = model
         self.operator = operator
         self.preconditioner = preconditioner
@@ -148,14 +148,14 @@ class TDVPDriver:
         for _ in range(n_steps):
             self._tensors, self.t, carry, (e, metrics) = self.integrator.step(
                 self._time_derivative, self._tensors, self.t, self.dt, carry)
-            logger.debug("E_mean=%s", float(e.mean()))
+            logger.debug("E_mean=%s", e.mean().item())
         self._sampler_configuration = carry[1]
         self._model.tensors = self._tensors
         self.step_count += n_steps
         mean = e.mean()
-        var = e.var(unbiased=False)
-        self._loss_stats = {"mean": float(mean), "variance": float(var),
-                            "error_of_mean": float(math.sqrt(float(var) / e.numel()))}
+        var = float((e - mean).abs().pow(2).mean())
+        self._loss_stats = {"mean": mean.item(), "variance": var,
+                            "error_of_mean": math.sqrt(var / e.numel())}
         self.residual_error = metrics.get("residual_error")
 
     # ------------------------------------------------------------ checkpoint
@@ -190,7 +190,7 @@ class TDVPDriver:
         self.t = float(state["t"])
         self.dt = float(state["dt"])
         self.step_count = int(state["step_count"])
-        self._tensors = [[t.to(dev, torch.float32).clone() for t in row] for row in state["tensors"]]
+        self._tensors = [[t.to(dev, self._model.dtype).clone() for t in row] for row in state["tensors"]]
         self._model.tensors = self._tensors
         self._sampler_configuration = state["sampler_configuration"].to(dev, torch.int32).clone()
         self._gen.set_state(state["generator_state"])

@@ -42,9 +42,9 @@ class SweepResult:
     configs: torch.Tensor        # (n, n_sites) int32, updated in place
     O: torch.Tensor | None       # (n, n_params) float32
     p: torch.Tensor | None       # (n, n_params_sliced) int8
-    E: torch.Tensor              # (n,) float64
-    logamp: torch.Tensor         # (n,) float64
-    sign: torch.Tensor           # (n,) float64
+    E: torch.Tensor              # (n,) float64, complex128 for a complex engine
+    logamp: torch.Tensor         # (n,) float64 log|psi|
+    sign: torch.Tensor           # (n,) float64 sign of psi, or its phase in radians for a complex engine
     margin: torch.Tensor | None  # (n,) float32
     gap: torch.Tensor | None = None  # (n,) float32 smallest relative eigen-gap at a cut
 
@@ -53,8 +53,12 @@ class PEPSEngine:
     """Plan + workspace for one (shape, D, chi, d, strategy, operator)."""
 
     def __init__(self, shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, operator=None,
-                 device=None, lib=None):
+                 device=None, lib=None, dtype="float32"):
         self.shape = (int(shape[0]), int(shape[1]))
+        self.complex = str(dtype).replace("torch.", "") in ("complex64", "complex128")
+        # dtypes of this engine's parameters / O_k and of E_loc
+        self.param_dtype = torch.complex64 if self.complex else torch.float32
+        self.energy_dtype = torch.complex128 if self.complex else torch.float64
         self.bond_dim, self.chi, self.phys_dim = int(bond_dim), int(chi), int(phys_dim)
         self.strategy = strategy
         self.n_sites = self.shape[0] * self.shape[1]
@@ -73,7 +77,8 @@ class PEPSEngine:
         sid = STRATEGY_IDS[strategy] if isinstance(strategy, str) else int(strategy)
         with torch.cuda.device(self.device) if self.device.type == "cuda" else _null():
             st = lib.vmc_peps_plan(ct.byref(_abi.VmcShape(*self.shape)), self.bond_dim, self.chi,
-                                   self.phys_dim, _abi.VMC_DTYPE_F32, sid, int(n_sweeps), ct.byref(plan))
+                                   self.phys_dim, _abi.VMC_DTYPE_C64 if self.complex else _abi.VMC_DTYPE_F32,
+                                   sid, int(n_sweeps), ct.byref(plan))
         _abi.check(lib, st, "vmc_peps_plan")
         self._plan = plan
         self.n_params_sliced = int(lib.vmc_peps_n_params_sliced(plan))
@@ -95,10 +100,11 @@ class PEPSEngine:
 
     # ------------------------------------------------------------------ setup
     def set_operator(self, operator):
-        lo = lower_operator(operator, self.shape, self.phys_dim)
+        lo = lower_operator(operator, self.shape, self.phys_dim, complex_elements=self.complex)
+        onesite, horiz, vert = (np.ascontiguousarray(a) for a in (lo.onesite, lo.horiz, lo.vert))
         st = self.lib.vmc_peps_plan_set_operator(
-            self._plan, _np_vp(lo.onesite), _np_vp(lo.onesite_mask), _np_vp(lo.horiz), _np_vp(lo.horiz_mask),
-            _np_vp(lo.vert), _np_vp(lo.vert_mask), lo.n_diag,
+            self._plan, _np_vp(onesite), _np_vp(lo.onesite_mask), _np_vp(horiz), _np_vp(lo.horiz_mask),
+            _np_vp(vert), _np_vp(lo.vert_mask), lo.n_diag,
             _np_vp(lo.diag_nsites) if lo.n_diag else None, _np_vp(lo.diag_site_off) if lo.n_diag else None,
             _np_vp(lo.diag_sites) if lo.n_diag else None, _np_vp(lo.diag_value_off) if lo.n_diag else None,
             _np_vp(lo.diag_values) if lo.n_diag else None)
@@ -122,8 +128,8 @@ class PEPSEngine:
         return None
 
     def _check_tensors(self, tensors):
-        if tensors.dtype != torch.float32 or tensors.device != self.device or not tensors.is_contiguous():
-            raise ValueError("packed tensors must be a contiguous float32 vector on the engine device")
+        if tensors.dtype != self.param_dtype or tensors.device != self.device or not tensors.is_contiguous():
+            raise ValueError(f"packed tensors must be a contiguous {self.param_dtype} vector on the engine device")
         if tensors.numel() != self.n_params_full:
             raise ValueError(f"expected {self.n_params_full} packed parameters, got {tensors.numel()}")
 
@@ -145,6 +151,21 @@ class PEPSEngine:
             raise FloatingPointError("engine reported a non-finite amplitude or energy")
         if v & _abi.VMC_DEV_TIMEOUT:
             raise TimeoutError("engine reported a device-side timeout")
+
+    def amplitude(self, logamp, sign):
+        """psi from (log|psi|, sign) -- or (log|psi|, phase) for a complex engine."""
+        if self.complex:
+            return torch.exp(torch.complex(logamp, sign))
+        return sign * torch.exp(logamp)
+
+    def log_sign(self, amps):
+        """(log|psi|, sign or phase) of given amplitudes, the inverse of ``amplitude``."""
+        a = torch.as_tensor(amps, device=self.device)
+        if self.complex:
+            a = a.to(torch.complex128)
+            return torch.log(torch.abs(a)), torch.angle(a)
+        a = a.to(torch.float64)
+        return torch.log(torch.abs(a)), torch.sign(a)
 
     # ------------------------------------------------------------------ calls
     def init_cache(self, tensors, configs, cache=None):
@@ -178,9 +199,9 @@ class PEPSEngine:
         if out is None:
             out = SweepResult(
                 configs=c,
-                O=torch.empty((n, np_), dtype=torch.float32, device=dev) if want_O else None,
+                O=torch.empty((n, np_), dtype=self.param_dtype, device=dev) if want_O else None,
                 p=torch.empty((n, self.n_params_sliced), dtype=torch.int8, device=dev) if want_p else None,
-                E=torch.empty(n, dtype=torch.float64, device=dev),
+                E=torch.empty(n, dtype=self.energy_dtype, device=dev),
                 logamp=torch.empty(n, dtype=torch.float64, device=dev),
                 sign=torch.empty(n, dtype=torch.float64, device=dev),
                 margin=torch.empty(n, dtype=torch.float32, device=dev) if want_margin else None,
@@ -200,7 +221,7 @@ class PEPSEngine:
         n = c.shape[0]
         dev = self.device
         np_ = self.n_params_full if full_gradient else self.n_params_sliced
-        O = torch.empty((n, np_), dtype=torch.float32, device=dev) if want_O else None
+        O = torch.empty((n, np_), dtype=self.param_dtype, device=dev) if want_O else None
         logamp = torch.empty(n, dtype=torch.float64, device=dev)
         sign = torch.empty(n, dtype=torch.float64, device=dev)
         gap = torch.empty(n, dtype=torch.float32, device=dev) if want_gap else None
@@ -217,7 +238,7 @@ class PEPSEngine:
         self._check_tensors(tensors)
         c = self._configs(samples)
         n = c.shape[0]
-        E = torch.empty(n, dtype=torch.float64, device=self.device)
+        E = torch.empty(n, dtype=self.energy_dtype, device=self.device)
         ws = self.workspace(n)
         la = logamp.to(torch.float64).contiguous()
         sg = sign.to(torch.float64).contiguous()

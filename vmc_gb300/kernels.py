@@ -73,7 +73,7 @@ def build_mc_kernels(model, operator, *, full_gradient: bool = False):
             deltas = torch.randint(1, d, (n, n_sites), generator=gen, device=engine.device, dtype=torch.int32)
         res = engine.sweep(model.packed(tensors), cfg, u, cache.bottom_envs, deltas=deltas,
                            full_gradient=full_gradient)
-        amp = res.sign * torch.exp(res.logamp)
+        amp = engine.amplitude(res.logamp, res.sign)
         est = LocalEstimates(
             local_log_derivatives=res.O,
             local_estimate=res.E,

@@ -35,9 +35,13 @@ def params_per_site(shape, bond_dim):
             for r in range(n_rows) for c in range(n_cols)]
 
 
-def pack_tensors(tensors) -> np.ndarray:
-    return np.concatenate([np.asarray(t, dtype=np.float32).reshape(-1)
-                           for row in tensors for t in row])
+def pack_tensors(tensors, complex_elements: bool | None = None) -> np.ndarray:
+    """ravel_pytree order of tensors[r][c].  Complex tensors (or complex_elements=True) pack as
+    complex64; real ones as float32."""
+    if complex_elements is None:
+        complex_elements = any(np.iscomplexobj(t) for row in tensors for t in row)
+    dt = np.complex64 if complex_elements else np.float32
+    return np.concatenate([np.asarray(t).astype(dt).reshape(-1) for row in tensors for t in row])
 
 
 @dataclass
@@ -59,6 +63,10 @@ class LoweredOperator:
         return int(self.diag_nsites.shape[0])
 
 
+def _as_complex(op, what):
+    return np.asarray(op, dtype=np.complex128)
+
+
 def _real(op, what):
     op = np.asarray(op)
     if np.iscomplexobj(op):
@@ -68,35 +76,41 @@ def _real(op, what):
     return np.asarray(op, dtype=np.float64)
 
 
-def lower_operator(operator, shape, phys_dim: int) -> LoweredOperator:
+def lower_operator(operator, shape, phys_dim: int, complex_elements: bool = False) -> LoweredOperator:
+    """Dense per-location tables of the operator's terms.  For a complex engine
+    (complex_elements=True) the one-site, horizontal and vertical tables are
+    complex128, handed to the C ABI as interleaved (re, im) doubles; diagonal
+    tables stay real."""
     n_rows, n_cols = shape
     d, d2 = phys_dim, phys_dim * phys_dim
+    _mat = _as_complex if complex_elements else _real
+    mdt = np.complex128 if complex_elements else np.float64
     diagonal, one_site, horizontal, vertical, plaquette = bucket_terms(operator.terms, shape)
     if any(t for row in plaquette for t in row):
         raise NotImplementedError("PlaquetteTerm belongs to the gauge-invariant PEPS model")
     n_sites = n_rows * n_cols
-    onesite = np.zeros((n_sites, d, d))
+    onesite = np.zeros((n_sites, d, d), dtype=mdt)
     onesite_mask = np.zeros(n_sites, dtype=np.int32)
     for r in range(n_rows):
         for c in range(n_cols):
             for term in one_site[r][c]:
-                onesite[r * n_cols + c] += _real(term.op, "one-site").reshape(d, d)
+                onesite[r * n_cols + c] += _mat(term.op, "one-site").reshape(d, d)
                 onesite_mask[r * n_cols + c] = 1
     nh = max(n_rows * (n_cols - 1), 1)
-    horiz = np.zeros((nh, d2, d2))
+    horiz = np.zeros((nh, d2, d2), dtype=mdt)
     horiz_mask = np.zeros(nh, dtype=np.int32)
     for r in range(n_rows):
         for c in range(n_cols - 1):
             for term in horizontal[r][c]:
-                horiz[r * (n_cols - 1) + c] += _real(term.op, "horizontal").reshape(d2, d2)
+                horiz[r * (n_cols - 1) + c] += _mat(term.op, "horizontal").reshape(d2, d2)
                 horiz_mask[r * (n_cols - 1) + c] = 1
     nv = max((n_rows - 1) * n_cols, 1)
-    vert = np.zeros((nv, d2, d2))
+    vert = np.zeros((nv, d2, d2), dtype=mdt)
     vert_mask = np.zeros(nv, dtype=np.int32)
     for r in range(n_rows - 1):
         for c in range(n_cols):
             for term in vertical[r][c]:
-                vert[r * n_cols + c] += _real(term.op, "vertical").reshape(d2, d2)
+                vert[r * n_cols + c] += _mat(term.op, "vertical").reshape(d2, d2)
                 vert_mask[r * n_cols + c] = 1
     nsites, site_off, sites, value_off, values = [], [], [], [], []
     for term in diagonal:

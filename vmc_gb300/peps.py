@@ -74,8 +74,10 @@ def _engine_strategy(strategy):
 class PEPS:
     """Open-boundary PEPS on a rectangular lattice (model.py:22-98).
 
-    ``rngs`` seeds the reference's initialiser (uniform [0, 1) entries,
-    src/vmc/utils/utils.py:22-47) when ``tensors`` is not given.  ``lib``
+    ``rngs`` seeds the reference's initialiser (uniform [0, 1) entries, or
+    0.5 (U + iU) for a complex dtype, src/vmc/utils/utils.py:22-47) when
+    ``tensors`` is not given.  Real dtypes run the float32 engine, complex
+    dtypes the complex64 engine.  ``lib``
     selects an engine library other than the in-tree CUDA build (a ctypes
     handle bound by ``vmc_gb300._abi.bind``); by default the CUDA build is
     required.
@@ -86,9 +88,13 @@ class PEPS:
         self.shape = (int(shape[0]), int(shape[1]))
         self.bond_dim = int(bond_dim)
         self.phys_dim = int(phys_dim)
-        if dtype not in (torch.float32, torch.float64):
-            raise NotImplementedError("the engine evaluates real PEPS (float32 arithmetic)")
-        self.dtype = torch.float32
+        if dtype in (torch.float32, torch.float64):
+            self.dtype = torch.float32
+        elif dtype in (torch.complex64, torch.complex128):
+            self.dtype = torch.complex64
+        else:
+            raise NotImplementedError(f"unsupported PEPS dtype {dtype}")
+        self.is_complex = self.dtype.is_complex
         if contraction_strategy is None:
             contraction_strategy = Variational(self.bond_dim * self.bond_dim)
         self.strategy = contraction_strategy
@@ -96,9 +102,14 @@ class PEPS:
         n_rows, n_cols = self.shape
         if tensors is None:
             rng = rngs if isinstance(rngs, np.random.Generator) else np.random.default_rng(int(rngs))
-            tensors = [[rng.random((self.phys_dim,) + self.site_dims(r, c, n_rows, n_cols, self.bond_dim))
+            def init(shape):
+                if self.is_complex:
+                    return 0.5 * (rng.random(shape) + 1j * rng.random(shape))
+                return rng.random(shape)
+
+            tensors = [[init((self.phys_dim,) + self.site_dims(r, c, n_rows, n_cols, self.bond_dim))
                         for c in range(n_cols)] for r in range(n_rows)]
-        self.tensors = [[torch.as_tensor(np.asarray(t), dtype=torch.float32).to(self.device)
+        self.tensors = [[torch.as_tensor(np.asarray(t)).to(dtype=self.dtype, device=self.device)
                          for t in row] for row in tensors]
         for r in range(n_rows):
             for c in range(n_cols):
@@ -117,8 +128,8 @@ class PEPS:
     def packed(self, tensors=None) -> torch.Tensor:
         tensors = self.tensors if tensors is None else tensors
         if isinstance(tensors, torch.Tensor):
-            return tensors.to(torch.float32).contiguous()
-        return torch.cat([t.reshape(-1).to(torch.float32) for row in tensors for t in row]).contiguous()
+            return tensors.to(self.dtype).contiguous()
+        return torch.cat([t.reshape(-1).to(self.dtype) for row in tensors for t in row]).contiguous()
 
     def unpack(self, flat: torch.Tensor):
         out, off = [], 0
@@ -140,7 +151,8 @@ class PEPS:
         if eng is None:
             sname, chi, n_sweeps = _engine_strategy(self.strategy)
             eng = PEPSEngine(self.shape, self.bond_dim, min(chi, 1 << 20), self.phys_dim, sname, n_sweeps,
-                             operator=operator, device=self.device, lib=self._lib)
+                             operator=operator, device=self.device, lib=self._lib,
+                             dtype="complex64" if self.is_complex else "float32")
             self._engines[key] = (eng, operator)
             return eng
         return eng[0]
@@ -156,10 +168,12 @@ class PEPS:
         return sample.reshape(shape)
 
     def __call__(self, x):
-        """log psi for a batch of samples (complex when psi < 0), as model.py:82-87."""
+        """log psi for a batch of samples (complex: log|psi| + i arg psi), as model.py:82-87."""
         from .compat import log_value
 
         la, sign = log_value(self, x)
+        if self.is_complex:
+            return torch.complex(la, sign)
         return torch.complex(la, torch.where(sign < 0, torch.full_like(la, math.pi), torch.zeros_like(la)))
 
     def random_physical_configuration(self, key=0, n_samples=1):

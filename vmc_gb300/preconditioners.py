@@ -136,10 +136,12 @@ class SRPreconditioner:
             from .gauge import compute_gauge_projection
 
             compute_gauge_projection(self.gauge_config, model, params)
-        e = local_energies.reshape(-1).to(torch.float64)
+        e = local_energies.reshape(-1)
+        e = e.to(torch.complex128 if e.is_complex() else torch.float64)
         n_samples = samples.shape[0]
         dv = (e - e.mean()) / n_samples
-        if isinstance(grad_factor, complex) and grad_factor.imag != 0:
+        complex_factor = isinstance(grad_factor, complex) and grad_factor.imag != 0
+        if complex_factor:
             dv = dv.to(torch.complex128) * grad_factor
         else:
             dv = dv * float(getattr(grad_factor, "real", grad_factor))
@@ -156,7 +158,8 @@ class SRPreconditioner:
             x, metrics = _qr_solve(jac, dv, self.strategy.rcond, self.strategy.min_norm)
         if p is not None:
             x = reorder_updates(self.ordering, x, pps, sd)
-        if not (isinstance(grad_factor, complex) and grad_factor.imag != 0):
+        param_dtype = getattr(model, "dtype", torch.float32)
+        if not complex_factor and not param_dtype.is_complex:
             x = 2.0 * x.real  # real parameters: preconditioners.py:322-329
         self._metrics = metrics
-        return model.unpack(x.to(torch.float32)), metrics
+        return model.unpack(x.to(param_dtype)), metrics

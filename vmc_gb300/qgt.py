@@ -105,10 +105,11 @@ def jacobian_mean(jac) -> torch.Tensor:
 
 
 def _sample_space_dense(jac, n_blocks):
-    n = (jac.O if isinstance(jac, Jacobian) else jac.o).shape[0]
-    dev = (jac.O if isinstance(jac, Jacobian) else jac.o).device
-    G = torch.zeros((n, n), dtype=torch.float64, device=dev)
-    w = torch.zeros(n, dtype=torch.float64, device=dev)
+    src = jac.O if isinstance(jac, Jacobian) else jac.o
+    n, dev = src.shape[0], src.device
+    dt = torch.complex128 if src.is_complex() else torch.float64
+    G = torch.zeros((n, n), dtype=dt, device=dev)
+    w = torch.zeros(n, dtype=dt, device=dev)
     msq = torch.zeros((), dtype=torch.float64, device=dev)
     blocks = [_f64(jac.O)] if isinstance(jac, Jacobian) else iter_sliced_blocks(jac, n_blocks)
     for ob in blocks:
@@ -117,10 +118,10 @@ def _sample_space_dense(jac, n_blocks):
         w += ob @ mb.conj()
         msq += torch.vdot(mb, mb).real
     G /= n
-    ones = torch.ones(n, dtype=torch.float64, device=dev)
+    ones = torch.ones(n, dtype=dt, device=dev)
     G -= (w[:, None] * ones[None, :]) / n
     G -= (ones[:, None] * w.conj()[None, :]) / n
-    G += (msq / n) * torch.ones((n, n), dtype=torch.float64, device=dev)
+    G += (msq / n) * torch.ones((n, n), dtype=dt, device=dev)
     return G
 
 

@@ -18,15 +18,21 @@ __all__ = ["Workload", "random_tensors", "initial_configs", "uniform_stream", "W
 
 
 def random_tensors(shape, bond_dim, phys_dim=2, seed=0, dtype=np.float64):
+    """Entries i.i.d. N(0,1)/sqrt(d D^4); for a complex dtype the real and
+    imaginary parts are each i.i.d. N(0,1)/sqrt(2 d D^4)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     n_rows, n_cols = shape
-    scale = 1.0 / np.sqrt(phys_dim * bond_dim ** 4)
+    cplx = np.issubdtype(np.dtype(dtype), np.complexfloating)
+    scale = 1.0 / np.sqrt((2 if cplx else 1) * phys_dim * bond_dim ** 4)
     out = []
     for r in range(n_rows):
         row = []
         for c in range(n_cols):
             dims = (phys_dim,) + site_dims(r, c, n_rows, n_cols, bond_dim)
-            row.append((rng.standard_normal(dims) * scale).astype(dtype))
+            t = rng.standard_normal(dims) * scale
+            if cplx:
+                t = t + 1j * rng.standard_normal(dims) * scale
+            row.append(t.astype(dtype))
         out.append(row)
     return out
 
@@ -53,6 +59,7 @@ class Workload:
     model: str       # "heisenberg" | "tfim"
     n_chains: int
     strategy: str = "ZipUp"
+    dtype: str = "float32"   # "float32" | "complex64"
 
     def operator(self):
         if self.model == "heisenberg":
@@ -60,9 +67,14 @@ class Workload:
         return transverse_field_ising(self.shape, J=1.0, h=3.0)
 
     def flops_per_sample(self):
-        """Algorithmic FLOP per sample counted with the reference's einsum orders (SVD/QR excluded;
-        oracle/flop_count.py recounts them)."""
-        return _ALGO_FLOPS.get((self.shape, self.bond_dim, self.chi, self.model, self.strategy))
+        """Algorithmic real FLOP per sample counted with the reference's einsum orders (SVD/QR excluded;
+        oracle/flop_count.py recounts them).  A complex multiply-add is 4 real ones."""
+        f = _ALGO_FLOPS.get((self.shape, self.bond_dim, self.chi, self.model, self.strategy))
+        return None if f is None else f * (4 if self.dtype == "complex64" else 1)
+
+    def tensors(self, seed=0):
+        return random_tensors(self.shape, self.bond_dim, self.phys_dim, seed=seed,
+                              dtype=np.complex128 if self.dtype == "complex64" else np.float64)
 
 
 _ALGO_FLOPS = {
@@ -88,4 +100,7 @@ WORKLOADS = {
     "heis8x8_D5_chi25": Workload("heis8x8_D5_chi25", (8, 8), 5, 25, 2, "heisenberg", 4096),
     "heis12x12_D6_chi36": Workload("heis12x12_D6_chi36", (12, 12), 6, 36, 2, "heisenberg", 4096),
     "heis16x16_D6_chi48": Workload("heis16x16_D6_chi48", (16, 16), 6, 48, 2, "heisenberg", 4096),
+    # 10x10 TFIM (J=1, h=3), complex64 PEPS, D=4, chi=16, 8192 samples per step
+    "tfim10x10_D4_chi16_c64": Workload("tfim10x10_D4_chi16_c64", (10, 10), 4, 16, 2, "tfim", 8192, "ZipUp",
+                                       "complex64"),
 }
