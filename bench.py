@@ -147,6 +147,9 @@ def run_reference(args, rank, world):
 
     if rank != 0:
         return
+    if args.workload == "uneven":
+        raise SystemExit("--impl reference times single-lattice workloads; the uneven batch reports each "
+                         "lattice's own rate in per_shape")
     w = WORKLOADS[args.workload]
     cores = len(os.sched_getaffinity(0))
     ctx = mp.get_context("spawn")
@@ -344,6 +347,141 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+UNEVEN = ["heis6x6_D4_chi16", "heis8x8_D5_chi25", "heis12x12_D6_chi36", "heis16x16_D6_chi48"]
+
+
+def run_uneven(args, rank, world, local_rank):
+    """--workload uneven: the four Heisenberg lattices of the uneven batch (6x6 D4 chi16, 8x8 D5 chi25,
+    12x12 D6 chi36, 16x16 D6 chi48; --chains each, default 4096) in ONE persistent launch
+    (vmc_peps_batch) captured in a CUDA graph.  value: samples/s of graph replays, inputs on the device;
+    e2e: the eager PEPSBatch.run with host uniforms in and E/log|psi|/sign out; per_shape: every
+    lattice launched alone (samples/s, algorithmic TFLOP/s and its roofline fraction)."""
+    import torch
+
+    from vmc_gb300.engine import PEPSBatch, PEPSEngine
+    from vmc_gb300.lowering import pack_tensors
+    from vmc_gb300.synthetic import WORKLOADS, initial_configs
+
+    n = args.chains or 4096
+    dev = torch.device(f"cuda:{local_rank}")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    total = args.warmup + args.steps
+    gen = torch.Generator(device=dev).manual_seed(1000 * rank + 7)
+    peaks, peak_kind = _peaks()
+    peak = peaks.get("bf16_tflops")
+    cases = []
+    for name in UNEVEN:
+        w = WORKLOADS[name]
+        n_sites = w.shape[0] * w.shape[1]
+        eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev)
+        tens = torch.from_numpy(pack_tensors(w.tensors(seed=0))).to(dev)
+        cfg0 = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
+        uni = torch.rand((total, n, n_sites), generator=gen, dtype=torch.float64, device=dev)
+        cases.append((w, eng, tens, cfg0, uni))
+
+    def timed(step_fn):
+        for i in range(args.warmup):
+            step_fn(i)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for i in range(args.steps):
+            step_fn(args.warmup + i)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / args.steps
+
+    # ---------------- every lattice alone ----------------
+    per_shape, t_alone = [], 0.0
+    for w, eng, tens, cfg0, uni in cases:
+        cfg = cfg0.clone()
+        cache = eng.init_cache(tens, cfg)
+        box = {"out": None}
+
+        def one(i, eng=eng, tens=tens, cfg=cfg, uni=uni, cache=cache, box=box):
+            box["out"] = eng.sweep(tens, cfg, uni[i], cache, out=box["out"])
+
+        t = timed(one)
+        eng.raise_on_status()
+        t_alone += t
+        flops = w.flops_per_sample()
+        tf = n * flops / t / 1e12
+        per_shape.append({"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
+                          "chains": n, "samples_per_s": n / t, "ms_per_launch": 1e3 * t,
+                          "tflops_algorithmic": tf, "roofline_frac": tf / peak if peak else None})
+        del cache
+
+    # ---------------- one launch over all four, captured in a CUDA graph ----------------
+    jobs, ubuf = [], []
+    for w, eng, tens, cfg0, uni in cases:
+        cfg = cfg0.clone()
+        cache = eng.init_cache(tens, cfg)
+        u = uni[0].clone()
+        ubuf.append(u)
+        jobs.append(eng.sweep_job(tens, cfg, u, cache))
+    batch = PEPSBatch(dev)
+    batch.run(jobs)
+    torch.cuda.synchronize()
+    batch.raise_on_status()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        batch.run(jobs)
+
+    def replay(i):
+        for u, (_, _, _, _, uni) in zip(ubuf, cases):
+            u.copy_(uni[i], non_blocking=True)
+        graph.replay()
+
+    with ClockSampler(local_rank) as clocks:
+        t_graph = timed(replay)
+    batch.raise_on_status()
+
+    # ---------------- end to end: eager batch, host uniforms in, results out ----------------
+    host_u = [[uni[i].cpu().pin_memory() for i in range(total)] for (_, _, _, _, uni) in cases]
+    host_out = [[torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(3)] for _ in cases]
+
+    def e2e_step(i):
+        for k, u in enumerate(ubuf):
+            u.copy_(host_u[k][i], non_blocking=True)
+        outs = batch.run(jobs)
+        for k, o in enumerate(outs):
+            for h, src in zip(host_out[k], (o.E, o.logamp, o.sign)):
+                h.copy_(src, non_blocking=True)
+
+    t_e2e = timed(e2e_step)
+    batch.raise_on_status()
+    h2d = sum(n * w.shape[0] * w.shape[1] * 8 for (w, _, _, _, _) in cases)
+    d2h = len(cases) * 3 * n * 8
+    samples = len(cases) * n
+    flops = sum(n * w.flops_per_sample() for (w, _, _, _, _) in cases)
+    achieved = flops / t_graph / 1e12
+    clk = clocks.summary()
+    line = {
+        "metric": "PEPS samples/s (amp+grad log psi+E_loc), uneven batch in one launch: "
+                  "6x6 D4 chi16 + 8x8 D5 chi25 + 12x12 D6 chi36 + 16x16 D6 chi48",
+        "value": samples / t_graph, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_graph, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "uneven", "shapes": UNEVEN, "chains_per_shape": n, "model": "heisenberg",
+                   "strategy": "ZipUp(chi)", "launch": "one persistent launch (vmc_peps_batch) in a CUDA graph",
+                   "parallelism": "replicas x1",
+                   "l2": "inputs larger than L2 (bottom-env caches of all four lattices)"},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "peak_kind": f"{peak_kind} bf16 burst (cuBLAS)", "kernel": "vmc::peps_kernel (batch)"},
+        "per_shape": per_shape,
+        "sequential_launches_ms": 1e3 * t_alone,
+        "batch_vs_sequential": t_alone / t_graph,
+        "cpu_baseline": None,
+        "e2e": {"value": samples / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": (len(cases) + 1) * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -369,7 +507,10 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     try:
-        run_ours(args, rank, world, local_rank)
+        if args.workload == "uneven":
+            run_uneven(args, rank, world, local_rank)
+        else:
+            run_ours(args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

@@ -213,6 +213,61 @@ vmc_status vmc_peps_local_energy(const vmc_plan* plan, void* stream, const float
                                  const double* sign, double* out_E, void* workspace,
                                  size_t workspace_bytes, int32_t* status_dev);
 
+/*
+ * Uneven batches: up to VMC_MAX_BATCH_JOBS jobs, each one of the calls above
+ * on its own plan (lattice, bond dimension, strategy, operator), in ONE
+ * persistent launch.  No single counterpart in the reference, where every
+ * model runs through its own jitted sampler and evaluator
+ * (src/vmc/peps/standard/kernels.py:91-247, one call per model); a job has the
+ * arguments and the results of the call it names:
+ *   VMC_JOB_INIT_CACHE   vmc_peps_init_cache   (tensors, configs, cache)
+ *   VMC_JOB_SWEEP        vmc_peps_sweep        (all fields; deltas when d > 2)
+ *   VMC_JOB_AMP_GRAD     vmc_peps_amp_grad     (configs = samples; logamp, sign
+ *                                               are outputs; out_O, out_gap optional)
+ *   VMC_JOB_LOCAL_ENERGY vmc_peps_local_energy (logamp, sign are inputs; out_E)
+ * Fields a kind does not use are ignored.  Every plan of a batch has the same
+ * element type and CTA size.  Each chain's results are bit-identical to the
+ * single call's: the same device code runs every chain.  CTAs take
+ * (job, chain) items from a device counter, jobs in decreasing order of cost
+ * per chain, so the lattices that take longest start first.
+ *
+ * vmc_batch_workspace_size: bytes of workspace for these jobs (0 if the batch
+ * is invalid).  The workspace needs no initial value.  The call launches one
+ * permutation kernel per job, one memset and the batch kernel on `stream`,
+ * and allocates nothing; the pointers in jobs[] are read at the call, so
+ * a captured launch replays with the same buffers.
+ */
+#define VMC_MAX_BATCH_JOBS 16
+typedef enum {
+  VMC_JOB_INIT_CACHE = 0,
+  VMC_JOB_SWEEP = 1,
+  VMC_JOB_AMP_GRAD = 2,
+  VMC_JOB_LOCAL_ENERGY = 3
+} vmc_job_kind;
+
+typedef struct {
+  const vmc_plan* plan;
+  int kind; /* vmc_job_kind */
+  int n_chains;
+  int full_gradient;
+  const float* tensors;
+  int32_t* configs;
+  const double* uniforms;
+  const int32_t* deltas;
+  void* cache;
+  float* out_O;
+  int8_t* out_p;
+  double* out_E;
+  double* logamp;
+  double* sign;
+  float* out_margin;
+  float* out_gap;
+} vmc_peps_job;
+
+size_t vmc_batch_workspace_size(const vmc_peps_job* jobs, int n_jobs);
+vmc_status vmc_peps_batch(const vmc_peps_job* jobs, int n_jobs, void* stream, void* workspace,
+                          size_t workspace_bytes, int32_t* status_dev);
+
 #ifdef __cplusplus
 }
 #endif

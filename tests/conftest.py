@@ -6,7 +6,7 @@ Markers:
 
 The CPU suite also checks the engine's device code through its host-emulation
 build (tests/_emu/libvmc_emu.so, compiled here with g++ from
-vmc_gb300/csrc/peps_engine.cu with -DVMC_HOST_EMULATION: every CTA runs with
+vmc_gb300/csrc/*.cu with -DVMC_HOST_EMULATION: every CTA runs with
 one thread).  That library is test infrastructure only; the package never
 loads it.
 """
@@ -36,13 +36,13 @@ def _newest(paths):
 
 
 def build_emulation_library() -> Path:
-    src = ROOT / "vmc_gb300" / "csrc" / "peps_engine.cu"
-    deps = list((ROOT / "vmc_gb300" / "csrc").glob("*.cuh")) + [src, ROOT / "include" / "vmc_gb300.h"]
+    srcs = sorted((ROOT / "vmc_gb300" / "csrc").glob("*.cu"))
+    deps = list((ROOT / "vmc_gb300" / "csrc").glob("*.cuh")) + srcs + [ROOT / "include" / "vmc_gb300.h"]
     EMU_DIR.mkdir(exist_ok=True)
     out = EMU_DIR / "libvmc_emu.so"
     if not out.exists() or out.stat().st_mtime < _newest(deps):
         tmp = out.with_suffix(f".{os.getpid()}.tmp")
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-DVMC_HOST_EMULATION", "-x", "c++", str(src),
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-DVMC_HOST_EMULATION", "-x", "c++", *map(str, srcs),
                "-o", str(tmp)]
         subprocess.run(cmd, check=True, capture_output=True, text=True)
         tmp.replace(out)

@@ -28,6 +28,12 @@ VMC_STRATEGY_VARIATIONAL = 3
 VMC_DEV_NONFINITE = 1
 VMC_DEV_TIMEOUT = 2
 
+VMC_JOB_INIT_CACHE = 0
+VMC_JOB_SWEEP = 1
+VMC_JOB_AMP_GRAD = 2
+VMC_JOB_LOCAL_ENERGY = 3
+VMC_MAX_BATCH_JOBS = 16
+
 
 class VmcShape(ct.Structure):
     _fields_ = [("n_rows", ct.c_int), ("n_cols", ct.c_int)]
@@ -36,6 +42,14 @@ class VmcShape(ct.Structure):
 _P = ct.c_void_p
 _I = ct.c_int
 _SZ = ct.c_size_t
+
+
+class VmcPepsJob(ct.Structure):
+    """vmc_peps_job: one call of an uneven batch."""
+    _fields_ = [("plan", _P), ("kind", _I), ("n_chains", _I), ("full_gradient", _I), ("tensors", _P),
+                ("configs", _P), ("uniforms", _P), ("deltas", _P), ("cache", _P), ("out_O", _P), ("out_p", _P),
+                ("out_E", _P), ("logamp", _P), ("sign", _P), ("out_margin", _P), ("out_gap", _P)]
+
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -53,6 +67,8 @@ SIGNATURES = {
     "vmc_peps_amp_grad": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P]),
     "vmc_peps_amp_grad_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P]),
     "vmc_peps_local_energy": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _P]),
+    "vmc_batch_workspace_size": (_SZ, [ct.POINTER(VmcPepsJob), _I]),
+    "vmc_peps_batch": (_I, [ct.POINTER(VmcPepsJob), _I, _P, _P, _SZ, _P]),
 }
 
 

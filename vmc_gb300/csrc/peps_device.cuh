@@ -976,31 +976,47 @@ __device__ inline double* cache_logs(const DevPlan& P, float* cache, int n_chain
 // ---------------------------------------------------------------------------
 // The fused kernel.
 // ---------------------------------------------------------------------------
-// At most 128 registers per thread (two 256-thread CTAs, or four of the default
-// 128 threads, per SM): left free, the compiler takes all 255 and halves occupancy.
-__global__ void __launch_bounds__(kThreads, 2) peps_kernel(
-    const DevPlan* __restrict__ Pp, int mode, const float* __restrict__ tensors, const float* __restrict__ perm,
-    int32_t* configs, const double* __restrict__ uniforms, const int32_t* __restrict__ deltas, int n_chains,
-    float* cache, int full_gradient, float* out_O, int8_t* out_p, double* out_E, double* logamp_io,
-    double* sign_io, float* out_margin, float* out_gap, float* ws, int32_t* status) {
-  const DevPlan& P = *Pp;
-  VMC_SHARED Shared sh;
-  Slot S = make_slot(P, ws + P.perm_floats + (size_t)blockIdx.x * P.slot_floats);
 #ifdef VMC_HOST_EMULATION
-  static float* dyn_smem = nullptr;
-  static long long dyn_floats = 0;
-  if (P.arena_in_smem && dyn_floats < P.arena_floats) {
-    std::free(dyn_smem);
-    dyn_smem = static_cast<float*>(std::malloc(sizeof(float) * P.arena_floats));
-    dyn_floats = P.arena_floats;
+// Shared memory starts with whatever an earlier chain left: the host build
+// poisons it so that a read before write shows up as NaN in the host tests.
+inline float* emu_dyn_smem(long long floats) {
+  static float* buf = nullptr;
+  static long long have = 0;
+  if (floats > have) {
+    std::free(buf);
+    buf = static_cast<float*>(std::malloc(sizeof(float) * floats));
+    have = floats;
   }
-  // shared memory starts with whatever an earlier block left: poison it so a
-  // read before write shows up as NaN in the host tests
-  if (dyn_smem) std::memset(dyn_smem, 0xff, sizeof(float) * dyn_floats);
+  if (buf) std::memset(buf, 0xff, sizeof(float) * have);
+  return buf;
+}
+#endif
+
+// One chain of a job, on this CTA, with the CTA's workspace slot at slot_base.
+__device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* slot_base, int32_t* status) {
+  const DevPlan& P = *J.P;
+  VMC_SHARED Shared sh;
+#ifdef VMC_HOST_EMULATION
+  float* dyn_smem = emu_dyn_smem(P.arena_in_smem ? P.arena_floats : 0);
   std::memset(&sh, 0xff, sizeof(sh));
 #else
   extern __shared__ float dyn_smem[];
 #endif
+  const int mode = J.mode, n_chains = J.n_chains, full_gradient = J.full_gradient;
+  const float* tensors = J.tensors;
+  const float* perm = J.perm;
+  int32_t* configs = J.configs;
+  const double* uniforms = J.uniforms;
+  const int32_t* deltas = J.deltas;
+  float* cache = J.cache;
+  float* out_O = J.out_O;
+  int8_t* out_p = J.out_p;
+  double* out_E = J.out_E;
+  double* logamp_io = J.logamp_io;
+  double* sign_io = J.sign_io;
+  float* out_margin = J.out_margin;
+  float* out_gap = J.out_gap;
+  Slot S = make_slot(P, slot_base);
   const Arena ar = make_arena(P, P.arena_in_smem ? dyn_smem : S.arena, S.arena);
   if (P.onerow_in_smem) {
     // the 1-row environment GEMM intermediates are never live during a truncation
@@ -1012,144 +1028,167 @@ __global__ void __launch_bounds__(kThreads, 2) peps_kernel(
   const int R = P.R, C = P.C;
   const int n_params = full_gradient ? P.d * P.np_sliced : P.np_sliced;
 
-  for (int chain = blockIdx.x; chain < n_chains; chain += gridDim.x) {
-    int32_t* cfg = configs + (size_t)chain * P.n_sites;
-    float min_gap = INFINITY;
+  int32_t* cfg = configs + (size_t)chain * P.n_sites;
+  float min_gap = INFINITY;
 
-    if (mode == MODE_INIT) {
-      // init_cache (kernels.py:115-129): bottom envs from the bottom up
-      double* lb = cache_logs(P, cache, n_chains, chain);
-      float* b = cache_row(P, cache, chain, R - 1);
-      fill_ones_row(P, b);
-      if (threadIdx.x == 0) lb[R - 1] = 0.0;
-      for (int r = R - 1; r >= 1; --r) {
-        for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
-        __syncthreads();
-        const double ls = apply_row(P, S, sh, perm, cache_row(P, cache, chain, r), bbonds(P, r),
-                                    cache_row(P, cache, chain, r - 1), bbonds(P, r - 1), r, sh.spins[0], true, ar,
-                                    &min_gap);
-        if (threadIdx.x == 0) lb[r - 1] = lb[r] + ls;
-        __syncthreads();
-      }
-      continue;
-    }
-
-    // ---------------- top-down pass: transition or forward ----------------
-    VMC_TSTART(tchain);
-    float min_margin = INFINITY;
-    fill_ones_row(P, S.topc);
-    if (threadIdx.x == 0) S.lt[0] = 0.0;
-    __syncthreads();
-    for (int r = 0; r < R; ++r) {
+  if (mode == MODE_INIT) {
+    // init_cache (kernels.py:115-129): bottom envs from the bottom up
+    double* lb = cache_logs(P, cache, n_chains, chain);
+    float* b = cache_row(P, cache, chain, R - 1);
+    fill_ones_row(P, b);
+    if (threadIdx.x == 0) lb[R - 1] = 0.0;
+    for (int r = R - 1; r >= 1; --r) {
       for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
       __syncthreads();
-      float* top = S.topc + (size_t)r * C * P.TS;
-      if (mode == MODE_SWEEP) {
-        const float* bot = cache_row(P, cache, chain, r);
-        metropolis_row(P, S, sh, perm, top, tbonds(P, r), bot, bbonds(P, r), r, sh.spins[0],
-                       uniforms + (size_t)chain * P.n_sites, deltas ? deltas + (size_t)chain * P.n_sites : nullptr,
-                       &min_margin);
-        for (int c = threadIdx.x; c < C; c += blockDim.x) cfg[r * C + c] = sh.spins[0][c];
-        __syncthreads();
-      }
-      VMC_TSTART(tz);
-      const double ls = apply_row(P, S, sh, perm, top, tbonds(P, r), S.topc + (size_t)(r + 1) * C * P.TS,
-                                  tbonds(P, r + 1), r, sh.spins[0], false, ar, &min_gap);
-      VMC_TSTOP(tz, PH_T_ZIP);
-      if (threadIdx.x == 0) S.lt[r + 1] = S.lt[r] + ls;
+      const double ls = apply_row(P, S, sh, perm, cache_row(P, cache, chain, r), bbonds(P, r),
+                                  cache_row(P, cache, chain, r - 1), bbonds(P, r - 1), r, sh.spins[0], true, ar,
+                                  &min_gap);
+      if (threadIdx.x == 0) lb[r - 1] = lb[r] + ls;
       __syncthreads();
     }
-    double sgn = 1.0;
-    double logamp = S.lt[R] + contract_bottom(P, S.topc + (size_t)R * C * P.TS, tbonds(P, R), sh,
-                                             reinterpret_cast<double*>(S.scr[0]), &sgn);
-    if (mode == MODE_ENERGY) {
-      logamp = logamp_io[chain];
-      sgn = sign_io[chain];
-    } else if (threadIdx.x == 0) {
-      logamp_io[chain] = logamp;
-      sign_io[chain] = sgn;
-      if (out_margin && mode == MODE_SWEEP) out_margin[chain] = min_margin;
-    }
-    if (!isfinite(logamp) && threadIdx.x == 0) atomicOr(status, VMC_DEV_NONFINITE);
+    return;
+  }
 
-    // ---------------- bottom-up estimate ----------------
-    const bool want_grad = (mode == MODE_SWEEP || mode == MODE_AMPGRAD);
-    const bool want_energy = (mode == MODE_SWEEP || mode == MODE_ENERGY);
-    float* Orow = out_O ? elem(out_O, (size_t)chain * n_params) : nullptr;
-    if (Orow && full_gradient) {
-      for (int i = threadIdx.x; i < n_params * kEs; i += blockDim.x) Orow[i] = 0.f;
+  // ---------------- top-down pass: transition or forward ----------------
+  VMC_TSTART(tchain);
+  float min_margin = INFINITY;
+  fill_ones_row(P, S.topc);
+  if (threadIdx.x == 0) S.lt[0] = 0.0;
+  __syncthreads();
+  for (int r = 0; r < R; ++r) {
+    for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
+    __syncthreads();
+    float* top = S.topc + (size_t)r * C * P.TS;
+    if (mode == MODE_SWEEP) {
+      const float* bot = cache_row(P, cache, chain, r);
+      metropolis_row(P, S, sh, perm, top, tbonds(P, r), bot, bbonds(P, r), r, sh.spins[0],
+                     uniforms + (size_t)chain * P.n_sites, deltas ? deltas + (size_t)chain * P.n_sites : nullptr,
+                     &min_margin);
+      for (int c = threadIdx.x; c < C; c += blockDim.x) cfg[r * C + c] = sh.spins[0][c];
       __syncthreads();
     }
-    double energy[2] = {0.0, 0.0};
-    if (want_energy) {
-      // diagonal terms (energy.py:150-156)
-      if (threadIdx.x == 0) {
-        for (int t = 0; t < P.n_diag; ++t) {
-          int idx = 0;
-          for (int k = 0; k < P.diag_nsites[t]; ++k) idx = idx * P.d + cfg[P.diag_sites[P.diag_site_off[t] + k]];
-          energy[0] += P.diag_values[P.diag_value_off[t] + idx];
-        }
+    VMC_TSTART(tz);
+    const double ls = apply_row(P, S, sh, perm, top, tbonds(P, r), S.topc + (size_t)(r + 1) * C * P.TS,
+                                tbonds(P, r + 1), r, sh.spins[0], false, ar, &min_gap);
+    VMC_TSTOP(tz, PH_T_ZIP);
+    if (threadIdx.x == 0) S.lt[r + 1] = S.lt[r] + ls;
+    __syncthreads();
+  }
+  double sgn = 1.0;
+  double logamp = S.lt[R] + contract_bottom(P, S.topc + (size_t)R * C * P.TS, tbonds(P, R), sh,
+                                           reinterpret_cast<double*>(S.scr[0]), &sgn);
+  if (mode == MODE_ENERGY) {
+    logamp = logamp_io[chain];
+    sgn = sign_io[chain];
+  } else if (threadIdx.x == 0) {
+    logamp_io[chain] = logamp;
+    sign_io[chain] = sgn;
+    if (out_margin && mode == MODE_SWEEP) out_margin[chain] = min_margin;
+  }
+  if (!isfinite(logamp) && threadIdx.x == 0) atomicOr(status, VMC_DEV_NONFINITE);
+
+  // ---------------- bottom-up estimate ----------------
+  const bool want_grad = (mode == MODE_SWEEP || mode == MODE_AMPGRAD);
+  const bool want_energy = (mode == MODE_SWEEP || mode == MODE_ENERGY);
+  float* Orow = out_O ? elem(out_O, (size_t)chain * n_params) : nullptr;
+  if (Orow && full_gradient) {
+    for (int i = threadIdx.x; i < n_params * kEs; i += blockDim.x) Orow[i] = 0.f;
+    __syncthreads();
+  }
+  double energy[2] = {0.0, 0.0};
+  if (want_energy) {
+    // diagonal terms (energy.py:150-156)
+    if (threadIdx.x == 0) {
+      for (int t = 0; t < P.n_diag; ++t) {
+        int idx = 0;
+        for (int k = 0; k < P.diag_nsites[t]; ++k) idx = idx * P.d + cfg[P.diag_sites[P.diag_site_off[t] + k]];
+        energy[0] += P.diag_values[P.diag_value_off[t] + idx];
       }
     }
-    // 1 / (sign or phase of psi): multiplies every psi-normalised quantity
-    const double inv_re = kCplx ? cos(sgn) : sgn, inv_im = kCplx ? -sin(sgn) : 0.0;
-    double* lbc = (mode == MODE_SWEEP) ? cache_logs(P, cache, n_chains, chain) : nullptr;
-    double lb_cur = 0.0, lb_prev = 0.0;
-    int ib_cur = 0, ib_prev = 1, ib_next = 2;
-    fill_ones_row(P, S.brow[ib_cur]);
-    for (int r = R - 1; r >= 0; --r) {
-      for (int c = threadIdx.x; c < C; c += blockDim.x) {
-        sh.spins[0][c] = cfg[r * C + c];
-        if (r + 1 < R) sh.spins[1][c] = cfg[(r + 1) * C + c];
-      }
-      __syncthreads();
-      float* bcur = S.brow[ib_cur];
-      if (mode == MODE_SWEEP) {
-        cta_copy(cache_row(P, cache, chain, r), bcur, C * P.TS);
-        if (threadIdx.x == 0) lbc[r] = lb_cur;
-      }
-      const float* top = S.topc + (size_t)r * C * P.TS;
-      const double om = exp(S.lt[r] + lb_cur - logamp);
-      const double osc[2] = {inv_re * om, inv_im * om};
-      estimate_row(P, S, sh, perm, tensors, top, tbonds(P, r), bcur, bbonds(P, r), r, sh.spins[0], osc, Orow,
-                   full_gradient, want_grad, want_energy, energy);
-      if (want_energy && r < R - 1 && P.row_has_v[r]) {
-        const double vm = exp(S.lt[r] + lb_prev - logamp);
-        const double vsc[2] = {inv_re * vm, inv_im * vm};
-        VMC_TSTART(tv);
-        vertical_energy(P, S, sh, perm, top, tbonds(P, r), S.brow[ib_prev], bbonds(P, r + 1), r, sh.spins[0],
-                        sh.spins[1], vsc, vbuf, energy);
-        VMC_TSTOP(tv, PH_E_VERT);
-      }
-      if (r > 0) {
-        VMC_TSTART(tb);
-        const double ls = apply_row(P, S, sh, perm, bcur, bbonds(P, r), S.brow[ib_next], bbonds(P, r - 1), r,
-                                    sh.spins[0], true, ar, &min_gap);
-        VMC_TSTOP(tb, PH_B_ZIP);
-        lb_prev = lb_cur;
-        lb_cur = lb_cur + ls;
-        const int t = ib_prev;
-        ib_prev = ib_cur;
-        ib_cur = ib_next;
-        ib_next = t;
-      }
-    }
-    if (out_gap && threadIdx.x == 0) out_gap[chain] = min_gap;
-    if (want_energy && threadIdx.x == 0) {
-      out_E[kEs * chain] = energy[0];
-      if (kCplx) out_E[kEs * chain + 1] = energy[1];
-      if (!isfinite(energy[0]) || !isfinite(energy[1])) atomicOr(status, VMC_DEV_NONFINITE);
-    }
-    if (out_p && mode == MODE_SWEEP) {
-      // active_slice_indices = repeat(config, params_per_site) (kernels.py:82-87)
-      for (int s = 0; s < P.n_sites; ++s) {
-        const int sz = ssize(P, s);
-        const int8_t v = (int8_t)cfg[s];
-        for (int i = threadIdx.x; i < sz; i += blockDim.x) out_p[(size_t)chain * P.np_sliced + P.site_osl[s] + i] = v;
-      }
+  }
+  // 1 / (sign or phase of psi): multiplies every psi-normalised quantity
+  const double inv_re = kCplx ? cos(sgn) : sgn, inv_im = kCplx ? -sin(sgn) : 0.0;
+  double* lbc = (mode == MODE_SWEEP) ? cache_logs(P, cache, n_chains, chain) : nullptr;
+  double lb_cur = 0.0, lb_prev = 0.0;
+  int ib_cur = 0, ib_prev = 1, ib_next = 2;
+  fill_ones_row(P, S.brow[ib_cur]);
+  for (int r = R - 1; r >= 0; --r) {
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+      sh.spins[0][c] = cfg[r * C + c];
+      if (r + 1 < R) sh.spins[1][c] = cfg[(r + 1) * C + c];
     }
     __syncthreads();
-    VMC_TSTOP(tchain, PH_CHAIN);
+    float* bcur = S.brow[ib_cur];
+    if (mode == MODE_SWEEP) {
+      cta_copy(cache_row(P, cache, chain, r), bcur, C * P.TS);
+      if (threadIdx.x == 0) lbc[r] = lb_cur;
+    }
+    const float* top = S.topc + (size_t)r * C * P.TS;
+    const double om = exp(S.lt[r] + lb_cur - logamp);
+    const double osc[2] = {inv_re * om, inv_im * om};
+    estimate_row(P, S, sh, perm, tensors, top, tbonds(P, r), bcur, bbonds(P, r), r, sh.spins[0], osc, Orow,
+                 full_gradient, want_grad, want_energy, energy);
+    if (want_energy && r < R - 1 && P.row_has_v[r]) {
+      const double vm = exp(S.lt[r] + lb_prev - logamp);
+      const double vsc[2] = {inv_re * vm, inv_im * vm};
+      VMC_TSTART(tv);
+      vertical_energy(P, S, sh, perm, top, tbonds(P, r), S.brow[ib_prev], bbonds(P, r + 1), r, sh.spins[0],
+                      sh.spins[1], vsc, vbuf, energy);
+      VMC_TSTOP(tv, PH_E_VERT);
+    }
+    if (r > 0) {
+      VMC_TSTART(tb);
+      const double ls = apply_row(P, S, sh, perm, bcur, bbonds(P, r), S.brow[ib_next], bbonds(P, r - 1), r,
+                                  sh.spins[0], true, ar, &min_gap);
+      VMC_TSTOP(tb, PH_B_ZIP);
+      lb_prev = lb_cur;
+      lb_cur = lb_cur + ls;
+      const int t = ib_prev;
+      ib_prev = ib_cur;
+      ib_cur = ib_next;
+      ib_next = t;
+    }
+  }
+  if (out_gap && threadIdx.x == 0) out_gap[chain] = min_gap;
+  if (want_energy && threadIdx.x == 0) {
+    out_E[kEs * chain] = energy[0];
+    if (kCplx) out_E[kEs * chain + 1] = energy[1];
+    if (!isfinite(energy[0]) || !isfinite(energy[1])) atomicOr(status, VMC_DEV_NONFINITE);
+  }
+  if (out_p && mode == MODE_SWEEP) {
+    // active_slice_indices = repeat(config, params_per_site) (kernels.py:82-87)
+    for (int s = 0; s < P.n_sites; ++s) {
+      const int sz = ssize(P, s);
+      const int8_t v = (int8_t)cfg[s];
+      for (int i = threadIdx.x; i < sz; i += blockDim.x) out_p[(size_t)chain * P.np_sliced + P.site_osl[s] + i] = v;
+    }
+  }
+  __syncthreads();
+  VMC_TSTOP(tchain, PH_CHAIN);}
+
+// The fused persistent kernel over the (job, chain) items of a job table
+// (uneven batches: lattices, bond dimensions, modes).  next == NULL: CTA b runs
+// items b, b + grid, ...  Otherwise CTAs take items from the counter *next
+// (zero at launch) until none is left; with the jobs ordered by decreasing cost
+// per chain the slowest chains start first and the fast ones fill in.  Every
+// CTA keeps its workspace slot at slots + blockIdx.x * slot_floats.
+// At most 128 registers per thread (two 256-thread CTAs, or four of the default
+// 128 threads, per SM): left free, the compiler takes all 255 and halves occupancy.
+__global__ void __launch_bounds__(kThreads, 2) peps_kernel(const __grid_constant__ BatchJobs jobs, float* slots,
+                                                           int32_t* next, int32_t* status) {
+  VMC_SHARED int item;
+  float* slot = slots + (size_t)blockIdx.x * jobs.slot_floats;
+  const int total = jobs.first[jobs.n_jobs];
+  for (int i = blockIdx.x;; i += gridDim.x) {
+    if (next) {
+      if (threadIdx.x == 0) item = atomicAdd(next, 1);
+      __syncthreads();
+      i = item;
+      __syncthreads();
+    }
+    if (i >= total) break;
+    int j = 0;
+    while (j + 1 < jobs.n_jobs && i >= jobs.first[j + 1]) ++j;
+    run_chain(jobs.job[j], i - jobs.first[j], slot, status);
   }
 }
-

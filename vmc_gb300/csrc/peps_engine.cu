@@ -22,156 +22,13 @@
 #include <cstdlib>
 #include <mutex>
 
-#include "device_common.cuh"
-#include "phase_timers.cuh"
-#include "truncation.cuh"
-#include "householder.cuh"
-#include "../../include/vmc_gb300.h"
+#include "peps_plan.cuh"
 
 #ifdef VMC_HOST_EMULATION
 thread_local vmc_dim3 threadIdx, blockIdx, blockDim, gridDim;
 #endif
 
 namespace vmc {
-
-constexpr int kThreads = 256;         // largest CTA the kernel is compiled for
-constexpr int kDefaultThreads = 128;  // one chain per 4 warps: more chains resident per SM
-constexpr int kMaxVec = 512;   // max vectors in one truncation (chi * D)
-constexpr int kMaxCols = 64;   // max lattice columns
-constexpr int kMaxD = 4;       // max physical dimension
-constexpr int kPermKinds = 6;  // permuted copies of every site tensor
-constexpr float kJacobiTol = 5e-7f;  // stop when every |a_p.a_q| <= tol |a_p||a_q|
-constexpr int kJacobiSweeps = 16;
-// dynamic shared memory per chain; 52 KB keeps 4 chains of 128 threads on an SM
-constexpr long long kMaxArenaSmemBytes = 52 * 1024;
-enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4, P_VRB = 5 };
-enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3 };
-
-
-// Device-side plan: scalars plus device pointers into one allocation.
-struct DevPlan {
-  int R, C, D, d, chi, strategy, n_sweeps, n_sites;
-  int es;                 // floats per element: 1 real FP32, 2 complex64 (re, im)
-  int np_sliced;          // sum of params_per_site
-  int TS, ES, E2S, SCR, MM;  // buffer sizes (floats)
-  int nmax, kmax;         // largest truncation matrix side / kept bond
-  int trunc_method;       // 0: Gram + tridiagonal eigensolver, 1: one-sided Jacobi
-  int arena_in_smem;      // truncation arena in dynamic shared memory
-  int mat_in_smem;        // theta matrix inside the arena (else in a separate global slot region)
-  int threads;            // CTA size of the fused kernel
-  long long arena_floats;
-  int scr1;               // size of one 1-row GEMM intermediate (floats)
-  int vchunk, vbuf;       // vertical-energy chunk (bond values) and buffer size (floats)
-  int vert_in_smem;       // vertical-energy buffers live in the shared-memory arena
-  int onerow_in_smem;     // 1-row intermediates share the shared-memory arena
-  int n_scr;              // number of SCR scratch buffers per slot
-  int VS;                 // one variational environment (floats); 0 unless Variational
-  long long slot_floats;  // floats per workspace slot
-  long long perm_floats;  // floats of the permuted tensor pack
-  long long cache_floats_per_chain;  // bottom env tensors per chain
-  // per-site (n_sites)
-  const int* sdim;        // [n_sites][4] up, down, left, right
-  const int* site_off;    // packed params offset
-  const int* site_osl;    // offset in the sliced O vector
-  const int* perm_off;    // offset in the permuted pack
-  // bond dims
-  const int* tb;          // [(R+1)][(C+1)] top env bonds (row r = before row r)
-  const int* bb;          // [R][(C+1)] bottom env bonds (row r = rows r+1.. from below)
-  // operator
-  const float* onesite;   // [n_sites][d][d]
-  const int* onesite_mask;
-  const float* horiz;     // [R*(C-1)][d*d][d*d]
-  const int* horiz_mask;
-  const float* vert;      // [(R-1)*C][d*d][d*d]
-  const int* vert_mask;
-  const int* row_has_h;   // [R] any horizontal term in row
-  const int* row_has_v;   // [R] any vertical term between r and r+1
-  int n_diag;
-  const int* diag_nsites;
-  const int* diag_site_off;
-  const int* diag_sites;
-  const int* diag_value_off;
-  const double* diag_values;
-};
-
-struct Slot {
-  float* topc;   // (R+1)*C*TS
-  double* lt;    // R+1
-  double* rl;    // [q][c] log-scale of right environment renv[q][c]
-  double* r2l;   // [c] log-scale of 2-row right environment r2[c]
-  float* brow[3];
-  float* renv;   // d*C*ES  [q][c]
-  float* lenv;   // (d+1)*ES
-  float* r2;     // C*E2S
-  float* l2[2];  // E2S
-  float* arena;  // truncation arena when it does not fit shared memory
-  float* venv;   // Variational: left envs C*VS, then right envs C*VS
-  float* scr[24];
-};
-
-__host__ __device__ inline long long al64(long long n) { return (n + 63) & ~63LL; }
-__host__ __device__ inline int min_i(int a, int b) { return a < b ? a : b; }
-
-__device__ inline Slot make_slot(const DevPlan& P, float* base) {
-  Slot s;
-  float* p = base;
-  s.topc = p; p += al64((long long)(P.R + 1) * P.C * P.TS);
-  s.lt = reinterpret_cast<double*>(p); p += al64(2 * (P.R + 2));
-  s.rl = reinterpret_cast<double*>(p); p += al64(2LL * P.d * P.C);
-  s.r2l = reinterpret_cast<double*>(p); p += al64(2LL * P.C);
-  for (int i = 0; i < 3; ++i) { s.brow[i] = p; p += al64((long long)P.C * P.TS); }
-  s.renv = p; p += al64((long long)P.d * P.C * P.ES);
-  s.lenv = p; p += al64((long long)(P.d + 1) * P.ES);
-  s.r2 = p; p += al64((long long)P.C * P.E2S);
-  for (int i = 0; i < 2; ++i) { s.l2[i] = p; p += al64(P.E2S); }
-  s.arena = p; p += P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.es * P.nmax * (P.nmax | 1)))
-                                    : al64(P.arena_floats);
-  for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
-  s.venv = p; p += al64(2LL * P.C * P.VS);
-  return s;
-}
-
-struct Shared {
-  double red[32];
-  int flag;
-  int sel[kMaxVec];
-  float sig[kMaxVec];
-  int spins[2][kMaxCols];
-  int vb[kMaxCols + 1];  // Variational: current bond dimensions of the row being compressed
-  double bcast[8];
-};
-
-// ---------------------------------------------------------------------------
-// Device code, compiled once per element type.
-// ---------------------------------------------------------------------------
-// Floats of the truncation arena (layout: make_arena); es = floats per element.
-__host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_method, int es) {
-  const int ld = nmax | 1;
-  return 2 * al64((long long)es * nmax * ld) + al64((long long)es * nmax * (trunc_method == 1 ? ld : kmax)) +
-         al64((long long)kmax * kmax) + al64(4LL * kmax * nmax) + al64(((long long)kmax * nmax + 3) / 4) +
-         3 * al64(nmax) + 3 * al64((long long)es * nmax) + al64(nmax + 1) + al64(2LL * es * nmax) +
-         al64(nmax + 64) + 64 + (es == 2 ? al64((long long)nmax * kmax) : 0);
-}
-
-namespace rk {
-constexpr bool kCplx = false;
-constexpr int kEs = 1;
-#include "peps_device.cuh"
-}  // namespace rk
-
-namespace ck {
-constexpr bool kCplx = true;
-constexpr int kEs = 2;
-#include "peps_device.cuh"
-}  // namespace ck
-
-// The kernels for a plan's element type.
-using PepsKernelFn = decltype(&rk::peps_kernel);
-using PermuteKernelFn = decltype(&rk::permute_tensors_kernel);
-static PepsKernelFn peps_kernel_of(const DevPlan& P) { return P.es == 2 ? &ck::peps_kernel : &rk::peps_kernel; }
-static PermuteKernelFn permute_kernel_of(const DevPlan& P) {
-  return P.es == 2 ? &ck::permute_tensors_kernel : &rk::permute_tensors_kernel;
-}
 
 // ===========================================================================
 // Host side: plan construction.
@@ -512,14 +369,8 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   }
   {
     const size_t smem = P.arena_in_smem ? (size_t)P.arena_floats * 4 : 0;
-    int per_sm = 4;
-#ifndef VMC_HOST_EMULATION
-    if (smem > 0) cudaFuncSetAttribute(peps_kernel_of(P), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peps_kernel_of(P), P.threads, smem) == cudaSuccess &&
-        occ > 0)
-      per_sm = occ;
-#endif
+    int per_sm = 4, occ = 0;
+    if (kernels_of(P).prepare(P.threads, smem, &occ) == cudaSuccess && occ > 0) per_sm = occ;
     pl->slots_max = vmc_num_sms() * per_sm;
   }
   *out_plan = pl;
@@ -602,6 +453,34 @@ size_t vmc_workspace_size(const vmc_plan* pl, int n_chains) {
   return ((size_t)pl->hp.perm_floats + (size_t)n_slots(pl, n_chains) * pl->hp.slot_floats) * 4;
 }
 
+// One job of a plan: the arguments of one C-ABI call.
+static ChainJob chain_job(const vmc_plan* pl, int mode, const float* tensors, float* perm, int32_t* configs,
+                          const double* uniforms, const int32_t* deltas, int n, void* cache, int full_gradient,
+                          float* out_O, int8_t* out_p, double* out_E, double* logamp, double* sign, float* margin,
+                          float* gap) {
+  return ChainJob{pl->dplan, mode, n, full_gradient, tensors, perm, configs, uniforms, deltas,
+                  static_cast<float*>(cache), out_O, out_p, out_E, logamp, sign, margin, gap};
+}
+
+// The fused kernel over the n_chains of one job J on grid CTAs: the permuted
+// tensors at the start of wsf, the CTA slots after them.
+static vmc_status run_job(const vmc_plan* pl, void* stream, ChainJob J, float* wsf, int grid, int32_t* status) {
+  const KernelSet& K = kernels_of(pl->hp);
+  if (K.permute(pl->dplan, pl->hp.n_sites, J.tensors, wsf, stream) != cudaSuccess) return VMC_ERR_CUDA;
+  J.perm = wsf;
+  BatchJobs bj;
+  std::memset(&bj, 0, sizeof(bj));
+  bj.job[0] = J;
+  bj.first[0] = 0;
+  bj.first[1] = J.n_chains;
+  bj.n_jobs = 1;
+  bj.slot_floats = pl->hp.slot_floats;
+  const size_t smem = pl->hp.arena_in_smem ? (size_t)pl->hp.arena_floats * 4 : 0;
+  return K.run(bj, grid, pl->hp.threads, smem, stream, wsf + pl->hp.perm_floats, nullptr, status) == cudaSuccess
+             ? VMC_OK
+             : VMC_ERR_CUDA;
+}
+
 static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float* tensors, int32_t* configs,
                          const double* uniforms, const int32_t* deltas, int n, void* cache, int full_gradient,
                          float* out_O, int8_t* out_p, double* out_E, double* logamp, double* sign, float* margin,
@@ -609,42 +488,11 @@ static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float
   if (!pl || !tensors || !configs || n < 0 || !ws || !status) return VMC_ERR_INVALID;
   if (n == 0) return VMC_OK;
   if (ws_bytes < vmc_workspace_size(pl, n)) return VMC_ERR_WORKSPACE;
-  const int grid = n_slots(pl, n);
-  float* wsf = static_cast<float*>(ws);
-  const PermuteKernelFn permute = permute_kernel_of(pl->hp);
-  const PepsKernelFn kernel = peps_kernel_of(pl->hp);
-  VMC_LAUNCH(permute, std::min(pl->hp.n_sites, 1024), kThreads, 0, stream, pl->dplan, tensors, wsf);
-  const size_t smem = pl->hp.arena_in_smem ? (size_t)pl->hp.arena_floats * 4 : 0;
-#ifndef VMC_HOST_EMULATION
-  // static (~5 KB) + dynamic shared memory may exceed the 48 KB default: always opt in
-  if (smem > 0 &&
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return VMC_ERR_CUDA;
-#endif
-  VMC_LAUNCH(kernel, grid, pl->hp.threads, smem, stream, pl->dplan, mode, tensors, wsf, configs, uniforms, deltas, n,
-             static_cast<float*>(cache), full_gradient, out_O, out_p, out_E, logamp, sign, margin, gap, wsf, status);
-  return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
+  return run_job(pl, stream,
+                 chain_job(pl, mode, tensors, nullptr, configs, uniforms, deltas, n, cache, full_gradient, out_O,
+                           out_p, out_E, logamp, sign, margin, gap),
+                 static_cast<float*>(ws), n_slots(pl, n), status);
 }
-
-#if defined(VMC_PHASE_TIMERS) && defined(VMC_HOST_EMULATION)
-int vmc_debug_phase_timers(unsigned long long* host_out) {
-  for (int i = 0; i < PH_COUNT; ++i) { host_out[i] = g_phase[i]; g_phase[i] = 0; }
-  return PH_COUNT;
-}
-#endif
-#if defined(VMC_PHASE_TIMERS) && !defined(VMC_HOST_EMULATION)
-// Debug-only (not part of the product ABI): read and reset the phase counters.
-int vmc_debug_phase_timers(unsigned long long* host_out) {
-  cudaError_t e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) return -(int)e;
-  e = cudaMemcpyFromSymbol(host_out, g_phase, sizeof(unsigned long long) * PH_COUNT);
-  if (e != cudaSuccess) return -1000 - (int)e;
-  unsigned long long z[PH_COUNT] = {0};
-  e = cudaMemcpyToSymbol(g_phase, z, sizeof(z));
-  if (e != cudaSuccess) return -2000 - (int)e;
-  return PH_COUNT;
-}
-#endif
 
 vmc_status vmc_peps_init_cache(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* configs,
                                int n_chains, void* cache, void* workspace, size_t workspace_bytes,
@@ -711,20 +559,10 @@ vmc_status vmc_peps_amp_grad_noalloc(const vmc_plan* pl, void* stream, const flo
   if (st != VMC_OK) return st;
   const size_t fit = (VMC_NOALLOC_SCRATCH_BYTES - perm_bytes) / slot_bytes;
   const int grid = (int)std::min<size_t>({fit, (size_t)n, (size_t)pl->slots_max});
-  float* wsf = static_cast<float*>(ws);
-  const PermuteKernelFn permute = permute_kernel_of(pl->hp);
-  const PepsKernelFn kernel = peps_kernel_of(pl->hp);
-  VMC_LAUNCH(permute, std::min(pl->hp.n_sites, 1024), kThreads, 0, stream, pl->dplan, tensors, wsf);
-  const size_t smem = pl->hp.arena_in_smem ? (size_t)pl->hp.arena_floats * 4 : 0;
-#ifndef VMC_HOST_EMULATION
-  if (smem > 0 &&
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return VMC_ERR_CUDA;
-#endif
-  VMC_LAUNCH(kernel, grid, pl->hp.threads, smem, stream, pl->dplan, (int)MODE_AMPGRAD, tensors, wsf,
-             const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr, full_gradient, out_O, nullptr, nullptr,
-             out_logamp, out_sign, nullptr, out_gap, wsf, status_dev);
-  return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
+  return run_job(pl, stream,
+                 chain_job(pl, MODE_AMPGRAD, tensors, nullptr, const_cast<int32_t*>(samples), nullptr, nullptr, n,
+                           nullptr, full_gradient, out_O, nullptr, nullptr, out_logamp, out_sign, nullptr, out_gap),
+                 static_cast<float*>(ws), grid, status_dev);
 }
 
 vmc_status vmc_peps_amp_grad(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples, int n,
@@ -743,6 +581,129 @@ vmc_status vmc_peps_local_energy(const vmc_plan* pl, void* stream, const float* 
   return launch(pl, stream, MODE_ENERGY, tensors, const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr, 0,
                 nullptr, nullptr, out_E, const_cast<double*>(logamp), const_cast<double*>(sign), nullptr, nullptr,
                 workspace, workspace_bytes, status_dev);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Uneven batches.  Workspace: [item counter, 256 B][permuted tensors of each
+// job, in the caller's order][grid slots of the largest slot_floats].
+// ---------------------------------------------------------------------------
+struct BatchLayout {
+  int n = 0;                           // non-empty jobs
+  int order[VMC_MAX_BATCH_JOBS];       // caller indices, decreasing cost per chain
+  size_t perm_off[VMC_MAX_BATCH_JOBS]; // floats from the workspace start, by caller index
+  long long slot_floats = 0;
+  size_t slots_off = 0;  // floats
+  int grid = 0, threads = 0, es = 0, total = 0;
+  size_t smem = 0, bytes = 0;
+};
+
+static bool job_valid(const vmc_peps_job& j) {
+  if (!j.plan || j.n_chains < 0) return false;
+  if (j.n_chains == 0) return true;
+  if (!j.tensors || !j.configs) return false;
+  switch (j.kind) {
+    case VMC_JOB_INIT_CACHE: return j.cache != nullptr;
+    case VMC_JOB_SWEEP:
+      return j.uniforms && j.cache && j.out_E && j.logamp && j.sign && (j.plan->hp.d <= 2 || j.deltas);
+    case VMC_JOB_AMP_GRAD: return j.logamp && j.sign;
+    case VMC_JOB_LOCAL_ENERGY: return j.logamp && j.sign && j.out_E;
+    default: return false;
+  }
+}
+
+static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout* L) {
+  if (!jobs || n_jobs < 1) return VMC_ERR_INVALID;
+  if (n_jobs > VMC_MAX_BATCH_JOBS) return VMC_ERR_UNSUPPORTED;
+  size_t off = 64;  // the item counter
+  long long total = 0;
+  double cost[VMC_MAX_BATCH_JOBS];
+  for (int i = 0; i < n_jobs; ++i) {
+    const vmc_peps_job& j = jobs[i];
+    if (!job_valid(j)) return VMC_ERR_INVALID;
+    const DevPlan& P = j.plan->hp;
+    if (L->threads == 0) {
+      L->threads = P.threads;
+      L->es = P.es;
+    } else if (P.threads != L->threads || P.es != L->es) {
+      return VMC_ERR_UNSUPPORTED;
+    }
+    L->perm_off[i] = off;
+    off += al64(P.perm_floats);
+    if (j.n_chains == 0) continue;
+    total += j.n_chains;
+    L->slot_floats = std::max(L->slot_floats, P.slot_floats);
+    L->smem = std::max(L->smem, P.arena_in_smem ? (size_t)P.arena_floats * 4 : (size_t)0);
+    // truncations dominate: n_sites cuts of an O(nmax^3) eigensolve, 4x the flops per complex element
+    cost[i] = (double)P.n_sites * P.nmax * P.nmax * P.nmax * P.es * P.es;
+    L->order[L->n++] = i;
+  }
+  if (total > 0x7fffffffLL) return VMC_ERR_UNSUPPORTED;
+  std::stable_sort(L->order, L->order + L->n, [&](int a, int b) { return cost[a] > cost[b]; });
+  L->total = (int)total;
+  L->slots_off = off;
+  int per_sm = 4;
+  if (L->n > 0) {
+    const KernelSet& K = L->es == 2 ? ck::kernels() : rk::kernels();
+    if (K.prepare(L->threads, L->smem, &per_sm) != cudaSuccess) return VMC_ERR_CUDA;
+    if (per_sm < 1) return VMC_ERR_UNSUPPORTED;
+  }
+  L->grid = (int)std::min<long long>(total, (long long)vmc_num_sms() * per_sm);
+  L->bytes = (off + (size_t)L->grid * (size_t)L->slot_floats) * 4;
+  return VMC_OK;
+}
+
+static vmc_status launch_batch(const vmc_peps_job* jobs, const BatchLayout& L, void* stream, float* wsf,
+                               int32_t* status) {
+  static const int kMode[4] = {MODE_INIT, MODE_SWEEP, MODE_AMPGRAD, MODE_ENERGY};
+  const KernelSet& K = L.es == 2 ? ck::kernels() : rk::kernels();
+  BatchJobs bj;
+  std::memset(&bj, 0, sizeof(bj));
+  bj.n_jobs = L.n;
+  bj.slot_floats = L.slot_floats;
+  bj.first[0] = 0;
+  for (int k = 0; k < L.n; ++k) {
+    const vmc_peps_job& j = jobs[L.order[k]];
+    const int kind = j.kind;
+    const bool sweep = kind == VMC_JOB_SWEEP, grad = sweep || kind == VMC_JOB_AMP_GRAD;
+    bj.job[k] = chain_job(j.plan, kMode[kind], j.tensors, wsf + L.perm_off[L.order[k]], j.configs,
+                          sweep ? j.uniforms : nullptr, sweep && j.plan->hp.d > 2 ? j.deltas : nullptr, j.n_chains,
+                          (sweep || kind == VMC_JOB_INIT_CACHE) ? j.cache : nullptr, j.full_gradient,
+                          grad ? j.out_O : nullptr, sweep ? j.out_p : nullptr,
+                          (sweep || kind == VMC_JOB_LOCAL_ENERGY) ? j.out_E : nullptr,
+                          kind == VMC_JOB_INIT_CACHE ? nullptr : j.logamp,
+                          kind == VMC_JOB_INIT_CACHE ? nullptr : j.sign, sweep ? j.out_margin : nullptr,
+                          grad ? j.out_gap : nullptr);
+    bj.first[k + 1] = bj.first[k] + j.n_chains;
+    if (K.permute(j.plan->dplan, j.plan->hp.n_sites, j.tensors, wsf + L.perm_off[L.order[k]], stream) !=
+        cudaSuccess)
+      return VMC_ERR_CUDA;
+  }
+  int32_t* next = reinterpret_cast<int32_t*>(wsf);
+  if (vmc_memset(next, 0, sizeof(int32_t), static_cast<cudaStream_t>(stream)) != cudaSuccess) return VMC_ERR_CUDA;
+  return K.run(bj, L.grid, L.threads, L.smem, stream, wsf + L.slots_off, next, status) == cudaSuccess
+             ? VMC_OK
+             : VMC_ERR_CUDA;
+}
+
+extern "C" {
+
+size_t vmc_batch_workspace_size(const vmc_peps_job* jobs, int n_jobs) {
+  BatchLayout L;
+  return batch_layout(jobs, n_jobs, &L) == VMC_OK ? L.bytes : 0;
+}
+
+vmc_status vmc_peps_batch(const vmc_peps_job* jobs, int n_jobs, void* stream, void* workspace,
+                          size_t workspace_bytes, int32_t* status_dev) {
+  if (!workspace || !status_dev) return VMC_ERR_INVALID;
+  BatchLayout L;
+  const vmc_status st = batch_layout(jobs, n_jobs, &L);
+  if (st != VMC_OK) return st;
+  if (L.total == 0) return VMC_OK;
+  if (workspace_bytes < L.bytes) return VMC_ERR_WORKSPACE;
+  float* wsf = static_cast<float*>(workspace);
+  return launch_batch(jobs, L, stream, wsf, status_dev);
 }
 
 }  // extern "C"

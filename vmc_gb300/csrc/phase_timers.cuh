@@ -12,7 +12,7 @@ enum Phase { PH_T_RENV = 0, PH_T_METRO, PH_T_ZIP, PH_JACOBI, PH_E_RENV, PH_E_LEF
              PH_GRAM, PH_TRIDIAG, PH_BISECT, PH_INVIT, PH_CHOLQR, PH_BACK, PH_CARRY, PH_V_RIGHT, PH_V_LEFT,
              PH_COUNT };
 #if defined(VMC_PHASE_TIMERS) && !defined(VMC_HOST_EMULATION)
-__device__ unsigned long long g_phase[PH_COUNT];
+static __device__ unsigned long long g_phase[PH_COUNT];
 #define VMC_TSTART(v) long long v = clock64()
 #define VMC_TSTOP(v, ph) \
   do { if (threadIdx.x == 0) atomicAdd(&g_phase[ph], (unsigned long long)(clock64() - (v))); } while (0)
@@ -20,7 +20,7 @@ __device__ unsigned long long g_phase[PH_COUNT];
 }  // namespace vmc
 #include <chrono>
 namespace vmc {
-unsigned long long g_phase[PH_COUNT];
+static unsigned long long g_phase[PH_COUNT];
 inline long long host_ns() {
   return std::chrono::duration_cast<std::chrono::nanoseconds>(
              std::chrono::steady_clock::now().time_since_epoch()).count();

@@ -20,6 +20,7 @@
 #define __host__
 #define __forceinline__ inline
 #define __noinline__
+#define __grid_constant__
 #define __align__(n) __attribute__((aligned(n)))
 #define __restrict__
 #define __launch_bounds__(...)

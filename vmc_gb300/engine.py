@@ -17,7 +17,7 @@ from . import _abi
 from ._lib import EngineUnavailable
 from .lowering import lower_operator
 
-__all__ = ["PEPSEngine", "SweepResult", "STRATEGY_IDS"]
+__all__ = ["BatchJob", "PEPSBatch", "PEPSEngine", "SweepResult", "STRATEGY_IDS"]
 
 STRATEGY_IDS = {
     "NoTruncation": _abi.VMC_STRATEGY_NO_TRUNCATION,
@@ -42,9 +42,9 @@ class SweepResult:
     configs: torch.Tensor        # (n, n_sites) int32, updated in place
     O: torch.Tensor | None       # (n, n_params) float32
     p: torch.Tensor | None       # (n, n_params_sliced) int8
-    E: torch.Tensor              # (n,) float64, complex128 for a complex engine
-    logamp: torch.Tensor         # (n,) float64 log|psi|
-    sign: torch.Tensor           # (n,) float64 sign of psi, or its phase in radians for a complex engine
+    E: torch.Tensor | None       # (n,) float64, complex128 for a complex engine
+    logamp: torch.Tensor | None  # (n,) float64 log|psi|
+    sign: torch.Tensor | None    # (n,) float64 sign of psi, or its phase in radians for a complex engine
     margin: torch.Tensor | None  # (n,) float32
     gap: torch.Tensor | None = None  # (n,) float32 smallest relative eigen-gap at a cut
 
@@ -180,8 +180,7 @@ class PEPSEngine:
         _abi.check(self.lib, st, "vmc_peps_init_cache")
         return cache
 
-    def sweep(self, tensors, configs, uniforms, cache, deltas=None, full_gradient=False, want_O=True,
-              want_p=True, want_margin=True, out=None):
+    def _sweep_io(self, tensors, configs, uniforms, deltas, full_gradient, want_O, want_p, want_margin, out):
         self._check_tensors(tensors)
         c = self._configs(configs)
         n = c.shape[0]
@@ -207,6 +206,13 @@ class PEPSEngine:
                 margin=torch.empty(n, dtype=torch.float32, device=dev) if want_margin else None,
                 gap=torch.empty(n, dtype=torch.float32, device=dev) if want_margin else None,
             )
+        return c, u, deltas, out
+
+    def sweep(self, tensors, configs, uniforms, cache, deltas=None, full_gradient=False, want_O=True,
+              want_p=True, want_margin=True, out=None):
+        c, u, deltas, out = self._sweep_io(tensors, configs, uniforms, deltas, full_gradient, want_O, want_p,
+                                           want_margin, out)
+        n = c.shape[0]
         ws = self.workspace(n)
         st = self.lib.vmc_peps_sweep(self._plan, self._stream(), _vp(tensors), _vp(c), _vp(u), _vp(deltas), n,
                                      _vp(cache), int(bool(full_gradient)), _vp(out.O), _vp(out.p), _vp(out.E),
@@ -246,6 +252,131 @@ class PEPSEngine:
                                             _vp(sg), _vp(E), _vp(ws), ws.numel(), _vp(self._status))
         _abi.check(self.lib, st, "vmc_peps_local_energy")
         return E
+
+
+    # ------------------------------------------------------- batch jobs
+    # The same calls as jobs of an uneven batch (PEPSBatch.run): arguments are
+    # checked and outputs allocated here, and the launch happens in the batch.
+    def init_cache_job(self, tensors, configs, cache=None):
+        self._check_tensors(tensors)
+        c = self._configs(configs)
+        cache = self.new_cache(c.shape[0]) if cache is None else cache
+        out = SweepResult(configs=c, O=None, p=None, E=None, logamp=None, sign=None, margin=None)
+        return BatchJob(self, _abi.VMC_JOB_INIT_CACHE, tensors, out, cache=cache)
+
+    def sweep_job(self, tensors, configs, uniforms, cache, deltas=None, full_gradient=False, want_O=True,
+                  want_p=True, want_margin=True, out=None):
+        c, u, deltas, out = self._sweep_io(tensors, configs, uniforms, deltas, full_gradient, want_O, want_p,
+                                           want_margin, out)
+        return BatchJob(self, _abi.VMC_JOB_SWEEP, tensors, out, uniforms=u, deltas=deltas, cache=cache,
+                        full_gradient=full_gradient)
+
+    def amp_grad_job(self, tensors, samples, full_gradient=False, want_O=True, want_gap=False):
+        self._check_tensors(tensors)
+        c = self._configs(samples)
+        n, dev = c.shape[0], self.device
+        np_ = self.n_params_full if full_gradient else self.n_params_sliced
+        out = SweepResult(configs=c, O=torch.empty((n, np_), dtype=self.param_dtype, device=dev) if want_O else None,
+                          p=None, E=None, logamp=torch.empty(n, dtype=torch.float64, device=dev),
+                          sign=torch.empty(n, dtype=torch.float64, device=dev), margin=None,
+                          gap=torch.empty(n, dtype=torch.float32, device=dev) if want_gap else None)
+        return BatchJob(self, _abi.VMC_JOB_AMP_GRAD, tensors, out, full_gradient=full_gradient)
+
+    def local_energy_job(self, tensors, samples, logamp, sign):
+        self._check_tensors(tensors)
+        c = self._configs(samples)
+        out = SweepResult(configs=c, O=None, p=None, E=torch.empty(c.shape[0], dtype=self.energy_dtype,
+                                                                     device=self.device),
+                          logamp=logamp.to(torch.float64).contiguous(), sign=sign.to(torch.float64).contiguous(),
+                          margin=None)
+        return BatchJob(self, _abi.VMC_JOB_LOCAL_ENERGY, tensors, out)
+
+
+@dataclass
+class BatchJob:
+    """One call of an uneven batch: the engine (plan) it runs on, its inputs, and
+    ``out``, whose tensors the launch writes (for a local-energy job, ``out.logamp``
+    and ``out.sign`` are the given denominators; an init-cache job writes ``cache``)."""
+    engine: PEPSEngine
+    kind: int
+    tensors: torch.Tensor
+    out: SweepResult
+    uniforms: torch.Tensor | None = None
+    deltas: torch.Tensor | None = None
+    cache: torch.Tensor | None = None
+    full_gradient: bool = False
+
+    def c_struct(self) -> _abi.VmcPepsJob:
+        o = self.out
+
+        def ptr(t):
+            return None if t is None else t.data_ptr()
+
+        return _abi.VmcPepsJob(self.engine._plan, self.kind, o.configs.shape[0], int(bool(self.full_gradient)),
+                               ptr(self.tensors), ptr(o.configs), ptr(self.uniforms), ptr(self.deltas),
+                               ptr(self.cache), ptr(o.O), ptr(o.p), ptr(o.E), ptr(o.logamp), ptr(o.sign),
+                               ptr(o.margin), ptr(o.gap))
+
+
+class PEPSBatch:
+    """Uneven batches: jobs on several engines -- lattices, bond dimensions,
+    strategies, operators of one element type -- in one persistent launch
+    (``vmc_peps_batch``) on torch's current stream.  Each chain's results are
+    bit-identical to the engine's single call.  ``run`` allocates only when its
+    workspace must grow, so after one warm-up call it can be captured in a CUDA
+    graph (the graph replays on the jobs' tensors)."""
+
+    def __init__(self, device=None):
+        self.device = None if device is None else torch.device(device)
+        self._ws = None
+        self._status = None
+
+    def _setup(self, jobs):
+        if not jobs:
+            raise ValueError("a batch needs at least one job")
+        if len(jobs) > _abi.VMC_MAX_BATCH_JOBS:
+            raise ValueError(f"at most {_abi.VMC_MAX_BATCH_JOBS} jobs per batch")
+        eng0 = jobs[0].engine
+        for j in jobs:
+            if j.engine.lib is not eng0.lib or j.engine.device != eng0.device:
+                raise ValueError("all jobs of a batch run on one library and device")
+            if j.engine.complex != eng0.complex:
+                raise ValueError("all jobs of a batch have one element type")
+        if self.device is None:
+            self.device = eng0.device
+        elif self.device != eng0.device:
+            raise ValueError("jobs on another device than this batch's")
+        if self._status is None:
+            self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        return eng0.lib, eng0
+
+    def run(self, jobs):
+        lib, eng0 = self._setup(jobs)
+        arr = (_abi.VmcPepsJob * len(jobs))(*[j.c_struct() for j in jobs])
+        need = int(lib.vmc_batch_workspace_size(arr, len(jobs)))
+        if need == 0:
+            raise ValueError("invalid batch (missing buffers, or plans of different element type or CTA size)")
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        st = lib.vmc_peps_batch(arr, len(jobs), eng0._stream(), _vp(self._ws), self._ws.numel(),
+                                _vp(self._status))
+        _abi.check(lib, st, "vmc_peps_batch")
+        return [j.out for j in jobs]
+
+    def status(self, reset=True) -> int:
+        if self._status is None:
+            return 0
+        v = int(self._status.item())
+        if reset and v:
+            self._status.zero_()
+        return v
+
+    def raise_on_status(self):
+        v = self.status()
+        if v & _abi.VMC_DEV_NONFINITE:
+            raise FloatingPointError("engine reported a non-finite amplitude or energy")
+        if v & _abi.VMC_DEV_TIMEOUT:
+            raise TimeoutError("engine reported a device-side timeout")
 
 
 class _null:
