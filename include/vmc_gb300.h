@@ -268,6 +268,26 @@ size_t vmc_batch_workspace_size(const vmc_peps_job* jobs, int n_jobs);
 vmc_status vmc_peps_batch(const vmc_peps_job* jobs, int n_jobs, void* stream, void* workspace,
                           size_t workspace_bytes, int32_t* status_dev);
 
+/*
+ * Column-pivoted Householder QR, A P = Q R, in FP64 (complex_elements = 0) or
+ * complex128 (interleaved (re, im) doubles): the factorisation of the SR QR
+ * solve, jax.lax.linalg.qr(o_centered, full_matrices=False, pivoting=True)
+ * (src/vmc/preconditioners/preconditioners.py:178-180; LAPACK/MAGMA xGEQP3).
+ *   a: column-major m x (n + nrhs), leading dimension lda >= m.  The first n
+ *      columns are factorised; the last nrhs are right-hand sides b, returned
+ *      as Q^H b.
+ * On return, as xGEQP3 leaves them: R in the upper triangle of the first
+ * min(m, n) rows, the reflectors v (v[0] = 1 implied) below the diagonal,
+ * tau[min(m, n)], and jpvt[n] the 0-based original index of each column of R.
+ * Pivots follow xLAQP2 (the unblocked xGEQP3): largest partial column norm,
+ * the first on ties, with xLAQP2's norm downdating and recomputation.
+ * workspace: vmc_qr_pivoted_workspace_size(n) bytes, no initial value.  The
+ * call launches 2 min(m, n) + 1 kernels on `stream` and allocates nothing.
+ */
+size_t vmc_qr_pivoted_workspace_size(int n);
+vmc_status vmc_qr_pivoted(void* stream, int complex_elements, double* a, int64_t lda, int m, int n, int nrhs,
+                          double* tau, int32_t* jpvt, void* workspace, size_t workspace_bytes);
+
 #ifdef __cplusplus
 }
 #endif

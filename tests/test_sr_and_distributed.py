@@ -113,7 +113,7 @@ def test_sample_space_gram_blocked_equals_dense():
                        rtol=1e-9, atol=1e-12)
 
 
-def test_reorder_and_qr_solve():
+def test_reorder_and_qr_solve(emu_lib):
     shape, D, T, om, o, p, e = _data(40, 5)
     sd = oracle.sliced_dims(om)
     pps = tuple(oracle.params_per_site(om))
@@ -125,7 +125,7 @@ def test_reorder_and_qr_solve():
     dv = np.random.default_rng(6).standard_normal(40)
     from vmc_gb300.preconditioners import _qr_solve
 
-    xq, mq = _qr_solve(gq.Jacobian(torch.as_tensor(grads_full)), torch.as_tensor(dv), None, True)
+    xq, mq = _qr_solve(gq.Jacobian(torch.as_tensor(grads_full)), torch.as_tensor(dv), None, True, lib=emu_lib)
     xr, mr = osr.qr_solve(osr.Jacobian(grads_full), dv)
     assert mq["rank"] == mr["rank"]
     assert np.allclose(xq.numpy(), xr, rtol=1e-8, atol=1e-10)

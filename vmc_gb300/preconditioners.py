@@ -74,43 +74,45 @@ def _direct_solve(space, jac, dv, diag_shift, solver):
     return x, {"residual_error": res}
 
 
-def _qr_solve(jac: Jacobian, dv, rcond, min_norm):
-    """preconditioners.py:166-214: column-pivoted QR of the centred full Jacobian (diag shift unused)."""
-    import numpy as np
-    import scipy.linalg as sla
+def _qr_solve(jac: Jacobian, dv, rcond, min_norm, lib=None):
+    """preconditioners.py:166-214: column-pivoted QR of the centred full Jacobian (diag shift
+    unused), all in FP64 (complex128) on the Jacobian's device: the factorisation is the
+    engine's vmc_qr_pivoted kernel, the rank and triangular solves are torch linear algebra."""
+    from .linalg import qr_pivoted
 
-    # torch has no column-pivoted QR; this branch runs LAPACK geqp3 on the host in FP64.
-    O = _to_np(jac.O)
-    oc = O - O.mean(axis=0)
-    q, r, piv = sla.qr(oc, mode="economic", pivoting=True)
-    dvn = _to_np(dv)
-    y = q.conj().T @ dvn
-    sv = np.linalg.svd(r, compute_uv=False)
-    tol = (max(r.shape) * np.finfo(r.dtype).eps if rcond is None else rcond) * (sv.max() if sv.size else 0)
-    rank = int(np.sum(sv > tol))
+    O = jac.O
+    cplx = O.is_complex() or dv.is_complex()
+    dt = torch.complex128 if cplx else torch.float64
+    o = O.to(dt)
+    oc = o - o.mean(dim=0, keepdim=True)
+    dvd = dv.to(device=o.device, dtype=dt)
+    r, piv, y = qr_pivoted(oc, dvd, lib=lib)
+    y = y[:, 0]
+    sv = torch.linalg.svdvals(r)
+    eps = torch.finfo(torch.float64).eps
+    smax = sv.max() if sv.numel() else torch.zeros((), dtype=torch.float64, device=o.device)
+    tol = (max(r.shape) * eps if rcond is None else rcond) * smax
+    rank = int((sv > tol).sum())  # the reference's int(matrix_rank(r)) also reads it on the host
     n_red = r.shape[1]
     n2 = n_red - rank
-    x = np.zeros(n_red, dtype=np.result_type(oc.dtype, dvn.dtype))
+    x = torch.zeros(n_red, dtype=dt, device=o.device)
     if rank:
-        r11, r12, y1 = r[:rank, :rank], r[:rank, rank:], y[:rank]
+        r11, r12, y1 = r[:rank, :rank], r[:rank, rank:], y[:rank, None]
         if min_norm and n2 > 0:
-            a = sla.solve_triangular(r11, y1, lower=False)
-            b = sla.solve_triangular(r11, r12, lower=False)
-            x2 = sla.solve(b.conj().T @ b + np.eye(n2), b.conj().T @ a, assume_a="pos")
-            x1 = a - b @ x2
+            a = torch.linalg.solve_triangular(r11, y1, upper=True)
+            bm = torch.linalg.solve_triangular(r11, r12, upper=True)
+            lhs = bm.mH @ bm + torch.eye(n2, dtype=dt, device=o.device)
+            chol, _ = torch.linalg.cholesky_ex(lhs)  # lhs = B^H B + I is positive definite
+            x2 = torch.cholesky_solve(bm.mH @ a, chol)
+            x1 = a - bm @ x2
         else:
-            x1 = sla.solve_triangular(r11, y1, lower=False)
-            x2 = np.zeros(n2, dtype=x.dtype)
-        x[piv] = np.concatenate([x1, x2])
-    rhs = oc.conj().T @ dvn
-    resid = oc.conj().T @ (oc @ x) - rhs
-    dev = jac.O.device
-    return torch.as_tensor(x, device=dev), {"residual_error": float(np.linalg.norm(resid) ** 2 /
-                                                                   np.linalg.norm(rhs) ** 2), "rank": rank}
-
-
-def _to_np(t):
-    return t.detach().to(torch.complex128 if t.is_complex() else torch.float64).cpu().numpy()
+            x1 = torch.linalg.solve_triangular(r11, y1, upper=True)
+            x2 = torch.zeros((n2, 1), dtype=dt, device=o.device)
+        x[piv] = torch.cat([x1, x2])[:, 0]
+    rhs = oc.mH @ dvd
+    resid = oc.mH @ (oc @ x) - rhs
+    err = (torch.linalg.norm(resid) ** 2 / torch.linalg.norm(rhs) ** 2).item()
+    return x, {"residual_error": err, "rank": rank}
 
 
 class SRPreconditioner:
