@@ -284,6 +284,18 @@ vmc_status vmc_peps_batch(const vmc_peps_job* jobs, int n_jobs, void* stream, vo
  * workspace: vmc_qr_pivoted_workspace_size(n) bytes, no initial value.  The
  * call launches 2 min(m, n) + 1 kernels on `stream` and allocates nothing.
  */
+/*
+ * Uniform draws in [0, 1) for the Metropolis accept tests (in place of the
+ * reference's per-site jax.random.uniform(accept_key), kernels.py:189-190),
+ * for callers that replay a whole TDVP step as one CUDA graph: fills out[n]
+ * (device FP64) from (seed, *counter) and increments the device word
+ * *counter, so every replay draws fresh numbers and a replay equals the eager
+ * call with the same counter.  SplitMix64 (Steele, Lea, Flood, OOPSLA 2014):
+ * key = mix(seed + (counter + 1) gamma), out[i] = (mix(key + (i + 1) gamma)
+ * >> 11) 2^-53, gamma = 0x9E3779B97F4A7C15.  Two kernels on `stream`.
+ */
+vmc_status vmc_uniforms(void* stream, double* out, int64_t n, uint64_t seed, uint64_t* counter);
+
 size_t vmc_qr_pivoted_workspace_size(int n);
 vmc_status vmc_qr_pivoted(void* stream, int complex_elements, double* a, int64_t lda, int m, int n, int nrhs,
                           double* tau, int32_t* jpvt, void* workspace, size_t workspace_bytes);

@@ -39,6 +39,7 @@ __all__ = [
     "transverse_field_ising",
     "build_mc_kernels",
     "make_mc_sampler",
+    "GraphTDVPDriver",
 ]
 
 
@@ -51,4 +52,8 @@ def __getattr__(name):
         from .sampling import make_mc_sampler
 
         return make_mc_sampler
+    if name == "GraphTDVPDriver":
+        from .tdvp_graph import GraphTDVPDriver
+
+        return GraphTDVPDriver
     raise AttributeError(name)

@@ -69,6 +69,7 @@ SIGNATURES = {
     "vmc_peps_local_energy": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _P]),
     "vmc_batch_workspace_size": (_SZ, [ct.POINTER(VmcPepsJob), _I]),
     "vmc_peps_batch": (_I, [ct.POINTER(VmcPepsJob), _I, _P, _P, _SZ, _P]),
+    "vmc_uniforms": (_I, [_P, _P, ct.c_int64, ct.c_uint64, _P]),
     "vmc_qr_pivoted_workspace_size": (_SZ, [_I]),
     "vmc_qr_pivoted": (_I, [_P, _I, _P, ct.c_int64, _I, _I, _I, _P, _P, _P, _SZ]),
 }

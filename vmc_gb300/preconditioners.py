@@ -43,19 +43,32 @@ class QRSolve:
     min_norm: bool = True
 
 
+_REORDER_INDEX = {}
+
+
+def _reorder_index(pps, sliced_dims, device):
+    key = (tuple(pps), tuple(sliced_dims), str(device))
+    idx = _REORDER_INDEX.get(key)
+    if idx is None:
+        total = sum(pps)
+        perm = []
+        off = 0
+        for site, n in enumerate(pps):
+            for k in range(sliced_dims[site]):
+                base = k * total + off
+                perm.extend(range(base, base + n))
+            off += n
+        idx = torch.as_tensor(perm, device=device)
+        _REORDER_INDEX[key] = idx
+    return idx
+
+
 def reorder_updates(ordering, updates, pps, sliced_dims):
-    """preconditioners.py:61-97: slice-major -> site-major parameter order."""
+    """preconditioners.py:61-97: slice-major -> site-major parameter order.  The index is built once
+    per (sizes, device), so the call reads nothing from the host after the first."""
     if isinstance(ordering, SiteOrdering):
         return updates
-    total = sum(pps)
-    perm = []
-    off = 0
-    for site, n in enumerate(pps):
-        for k in range(sliced_dims[site]):
-            base = k * total + off
-            perm.extend(range(base, base + n))
-        off += n
-    return updates[torch.as_tensor(perm, device=updates.device)]
+    return updates[_reorder_index(pps, sliced_dims, updates.device)]
 
 
 def _direct_solve(space, jac, dv, diag_shift, solver):

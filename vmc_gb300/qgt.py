@@ -167,8 +167,10 @@ def adjoint_matvec(jac, v) -> torch.Tensor:
 
 
 def solve_cholesky(mat, rhs):
-    """solvers.py:25-28 (cuSOLVER potrf/potrs in FP64)."""
-    L = torch.linalg.cholesky(mat)
+    """solvers.py:25-28 (cuSOLVER potrf/potrs in FP64).  Like jax.scipy's cho_factor, a matrix that
+    is not positive definite yields NaNs rather than an exception; nothing here reads the host, so
+    the solve can run inside a captured CUDA graph."""
+    L, _ = torch.linalg.cholesky_ex(mat)
     return torch.cholesky_solve(rhs[:, None], L)[:, 0]
 
 
