@@ -166,6 +166,24 @@ vmc_status vmc_peps_sweep(const vmc_plan* plan, void* stream, const float* tenso
                           size_t workspace_bytes, int32_t* status_dev);
 
 /*
+ * vmc_peps_sweep without a per-chain cache: each chain's bottom environments
+ * are recomputed at the start of its sweep, in one cache entry per resident
+ * CTA inside the workspace, and dropped after it.  The same results as
+ * vmc_peps_init_cache followed by vmc_peps_sweep, bit for bit, for one extra
+ * bottom-up pass per chain; memory grows with the resident CTAs instead of the
+ * chains (the reference recomputes them every call: init_cache,
+ * kernels.py:115-129, runs on each sampler call).  Workspace:
+ * vmc_sweep_recompute_workspace_size(plan, n_chains) bytes.
+ */
+size_t vmc_sweep_recompute_workspace_size(const vmc_plan* plan, int n_chains);
+vmc_status vmc_peps_sweep_recompute(const vmc_plan* plan, void* stream, const float* tensors,
+                                    int32_t* configs_inout, const double* uniforms, const int32_t* deltas,
+                                    int n_chains, int full_gradient, float* out_O, int8_t* out_p,
+                                    double* out_E, double* out_logamp, double* out_sign, float* out_margin,
+                                    float* out_gap, void* workspace, size_t workspace_bytes,
+                                    int32_t* status_dev);
+
+/*
  * Amplitude and hand-written adjoint for samples[n][n_sites]
  * (compat.py:31-64 peps_apply custom_vjp; compat.py:94-133 _value_and_grad;
  * energy.py:276-301 _compute_all_gradients): log|psi|, sign and
@@ -221,7 +239,8 @@ vmc_status vmc_peps_local_energy(const vmc_plan* plan, void* stream, const float
  * (src/vmc/peps/standard/kernels.py:91-247, one call per model); a job has the
  * arguments and the results of the call it names:
  *   VMC_JOB_INIT_CACHE   vmc_peps_init_cache   (tensors, configs, cache)
- *   VMC_JOB_SWEEP        vmc_peps_sweep        (all fields; deltas when d > 2)
+ *   VMC_JOB_SWEEP        vmc_peps_sweep        (all fields; deltas when d > 2;
+ *                                               cache NULL: vmc_peps_sweep_recompute)
  *   VMC_JOB_AMP_GRAD     vmc_peps_amp_grad     (configs = samples; logamp, sign
  *                                               are outputs; out_O, out_gap optional)
  *   VMC_JOB_LOCAL_ENERGY vmc_peps_local_energy (logamp, sign are inputs; out_E)

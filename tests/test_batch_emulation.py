@@ -148,3 +148,35 @@ def test_malformed_batches_return_status_codes(emu_lib):
     assert run([empty]) == _abi.VMC_OK
     with pytest.raises(ValueError):
         PEPSBatch().run([good, ceng.amp_grad_job(ctens, ccfg)])
+
+
+@pytest.mark.parametrize("full", [False, True])
+def test_recomputing_sweeps_equal_init_cache_then_sweep(emu_lib, full):
+    """A sweep without a cache recomputes the bottom environments in the launch: same bits as
+    init_cache + sweep, alone and as a batch job next to a cached one."""
+    cases = [_setup(emu_lib, spec, seed=60 + i) for i, spec in enumerate(JOBS[:3])]
+    for eng, tens, cfg, u in cases:
+        ref = eng.sweep(tens, cfg.clone(), u, eng.init_cache(tens, cfg.clone()), full_gradient=full)
+        _assert_same_bits(ref, eng.sweep(tens, cfg.clone(), u, None, full_gradient=full))
+    jobs, refs = [], []
+    for i, (eng, tens, cfg, u) in enumerate(cases):
+        cache = eng.init_cache(tens, cfg.clone())
+        refs.append(eng.sweep(tens, cfg.clone(), u, cache.clone(), full_gradient=full))
+        jobs.append(eng.sweep_job(tens, cfg.clone(), u, cache if i == 1 else None, full_gradient=full))
+    for ref, out in zip(refs, PEPSBatch().run(jobs)):
+        _assert_same_bits(ref, out)
+
+
+@pytest.mark.parametrize("layout", ["slot", "shared"])
+def test_either_batch_layout_gives_the_single_call_bits(emu_lib, layout, monkeypatch):
+    """The batch runs every plan either with its shared-memory buffer placement or with all buffers
+    in the CTA slot (chosen by cost share); the placement moves data, not arithmetic."""
+    monkeypatch.setenv("VMC_BATCH_LAYOUT", layout)
+    cases = [_setup(emu_lib, spec, seed=80 + i) for i, spec in enumerate(JOBS)]
+    refs, jobs = [], []
+    for eng, tens, cfg, u in cases:
+        cache = eng.init_cache(tens, cfg.clone())
+        refs.append(eng.sweep(tens, cfg.clone(), u, cache.clone()))
+        jobs.append(eng.sweep_job(tens, cfg.clone(), u, cache))
+    for ref, out in zip(refs, PEPSBatch().run(jobs)):
+        _assert_same_bits(ref, out)

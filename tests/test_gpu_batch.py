@@ -82,3 +82,18 @@ def test_batch_replays_from_a_cuda_graph(cuda_device):
                 jobs[1].out.logamp, jobs[2].out.E]
     for a, b in zip(eager, replayed):
         assert torch.equal(a.view(torch.uint8), b.contiguous().view(torch.uint8))
+
+
+def test_recomputing_sweep_matches_cached_sweep(cuda_device):
+    """12x12 D6 chi36: the sweep that recomputes the bottom environments in the launch (memory per
+    resident CTA) gives the bits of init_cache + sweep (memory per chain)."""
+    eng, tens, cfg, u = _case(cuda_device, (12, 12), 6, 36, 6, seed=41)
+    ref = eng.sweep(tens, cfg.clone(), u, eng.init_cache(tens, cfg.clone()))
+    out = eng.sweep(tens, cfg.clone(), u, None)
+    torch.cuda.synchronize()
+    eng.raise_on_status()
+    _same_bits(ref, out)
+    per_chain = eng.cache_bytes(4096)
+    per_cta = int(eng.lib.vmc_sweep_recompute_workspace_size(eng._plan, 4096)) - \
+        int(eng.lib.vmc_workspace_size(eng._plan, 4096))
+    assert per_cta < per_chain / 4  # 608 resident CTAs instead of 4096 chains

@@ -64,6 +64,8 @@ SIGNATURES = {
     "vmc_workspace_size": (_SZ, [_P, _I]),
     "vmc_peps_init_cache": (_I, [_P, _P, _P, _P, _I, _P, _P, _SZ, _P]),
     "vmc_peps_sweep": (_I, [_P, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "vmc_sweep_recompute_workspace_size": (_SZ, [_P, _I]),
+    "vmc_peps_sweep_recompute": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "vmc_peps_amp_grad": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P]),
     "vmc_peps_amp_grad_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P]),
     "vmc_peps_local_energy": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _P]),

@@ -1030,23 +1030,27 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
 
   int32_t* cfg = configs + (size_t)chain * P.n_sites;
   float min_gap = INFINITY;
+  // this chain's cache entry: its own, or (recompute) the CTA's
+  const bool own_entry = J.cache_per_cta != 0;
+  const int ce = own_entry ? (int)blockIdx.x : chain, ce_n = own_entry ? (int)gridDim.x : n_chains;
 
-  if (mode == MODE_INIT) {
+  if (mode == MODE_INIT || (own_entry && mode == MODE_SWEEP)) {
     // init_cache (kernels.py:115-129): bottom envs from the bottom up
-    double* lb = cache_logs(P, cache, n_chains, chain);
-    float* b = cache_row(P, cache, chain, R - 1);
+    double* lb = cache_logs(P, cache, ce_n, ce);
+    float* b = cache_row(P, cache, ce, R - 1);
     fill_ones_row(P, b);
     if (threadIdx.x == 0) lb[R - 1] = 0.0;
     for (int r = R - 1; r >= 1; --r) {
       for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
       __syncthreads();
-      const double ls = apply_row(P, S, sh, perm, cache_row(P, cache, chain, r), bbonds(P, r),
-                                  cache_row(P, cache, chain, r - 1), bbonds(P, r - 1), r, sh.spins[0], true, ar,
+      const double ls = apply_row(P, S, sh, perm, cache_row(P, cache, ce, r), bbonds(P, r),
+                                  cache_row(P, cache, ce, r - 1), bbonds(P, r - 1), r, sh.spins[0], true, ar,
                                   &min_gap);
       if (threadIdx.x == 0) lb[r - 1] = lb[r] + ls;
       __syncthreads();
     }
-    return;
+    if (mode == MODE_INIT) return;
+    min_gap = INFINITY;  // the sweep reports its own cuts, as after a separate init_cache
   }
 
   // ---------------- top-down pass: transition or forward ----------------
@@ -1060,7 +1064,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
     __syncthreads();
     float* top = S.topc + (size_t)r * C * P.TS;
     if (mode == MODE_SWEEP) {
-      const float* bot = cache_row(P, cache, chain, r);
+      const float* bot = cache_row(P, cache, ce, r);
       metropolis_row(P, S, sh, perm, top, tbonds(P, r), bot, bbonds(P, r), r, sh.spins[0],
                      uniforms + (size_t)chain * P.n_sites, deltas ? deltas + (size_t)chain * P.n_sites : nullptr,
                      &min_margin);
@@ -1108,7 +1112,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   }
   // 1 / (sign or phase of psi): multiplies every psi-normalised quantity
   const double inv_re = kCplx ? cos(sgn) : sgn, inv_im = kCplx ? -sin(sgn) : 0.0;
-  double* lbc = (mode == MODE_SWEEP) ? cache_logs(P, cache, n_chains, chain) : nullptr;
+  double* lbc = (mode == MODE_SWEEP) ? cache_logs(P, cache, ce_n, ce) : nullptr;
   double lb_cur = 0.0, lb_prev = 0.0;
   int ib_cur = 0, ib_prev = 1, ib_next = 2;
   fill_ones_row(P, S.brow[ib_cur]);
@@ -1120,7 +1124,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
     __syncthreads();
     float* bcur = S.brow[ib_cur];
     if (mode == MODE_SWEEP) {
-      cta_copy(cache_row(P, cache, chain, r), bcur, C * P.TS);
+      cta_copy(cache_row(P, cache, ce, r), bcur, C * P.TS);
       if (threadIdx.x == 0) lbc[r] = lb_cur;
     }
     const float* top = S.topc + (size_t)r * C * P.TS;

@@ -45,6 +45,8 @@ struct HostOp {
 struct vmc_plan {
   vmc::DevPlan hp;          // host copy with device pointers
   vmc::DevPlan* dplan = nullptr;  // device copy
+  vmc::DevPlan hpg;         // buffer placement with no shared memory (layout fields only are used)
+  vmc::DevPlan* dplan_g = nullptr;  // device copy of hp with hpg's buffer placement
   void* dbuf = nullptr;     // device arrays
   std::vector<int> sdim, site_off, site_osl, perm_off, tb, bb;
   vmc::HostOp op;
@@ -111,6 +113,7 @@ static vmc_status upload_plan(vmc_plan* pl) {
   const size_t o_dvo = push(op.diag_value_off.data(), op.diag_value_off.size() * 4);
   const size_t o_dv = push(op.diag_values.data(), op.diag_values.size() * 8);
   const size_t o_plan = push(nullptr, sizeof(DevPlan));
+  const size_t o_plan_g = push(nullptr, sizeof(DevPlan));
   if (pl->dbuf) vmc_free(pl->dbuf);
   pl->dbuf = nullptr;
   if (vmc_alloc(&pl->dbuf, blob.size()) != cudaSuccess) return VMC_ERR_CUDA;
@@ -136,6 +139,21 @@ static vmc_status upload_plan(vmc_plan* pl) {
   P.diag_values = reinterpret_cast<const double*>(base + o_dv);
   std::memcpy(blob.data() + o_plan, &P, sizeof(DevPlan));
   pl->dplan = reinterpret_cast<DevPlan*>(base + o_plan);
+  {
+    DevPlan G = P;  // arrays and operator of P, buffer placement of the no-shared-memory layout
+    const DevPlan& L = pl->hpg;
+    G.arena_in_smem = L.arena_in_smem;
+    G.mat_in_smem = L.mat_in_smem;
+    G.arena_floats = L.arena_floats;
+    G.scr1 = L.scr1;
+    G.vchunk = L.vchunk;
+    G.vbuf = L.vbuf;
+    G.vert_in_smem = L.vert_in_smem;
+    G.onerow_in_smem = L.onerow_in_smem;
+    G.slot_floats = L.slot_floats;
+    std::memcpy(blob.data() + o_plan_g, &G, sizeof(DevPlan));
+    pl->dplan_g = reinterpret_cast<DevPlan*>(base + o_plan_g);
+  }
   if (vmc_h2d(pl->dbuf, blob.data(), blob.size(), nullptr) != cudaSuccess) return VMC_ERR_CUDA;
   if (vmc_sync(nullptr) != cudaSuccess) return VMC_ERR_CUDA;
   return VMC_OK;
@@ -305,57 +323,68 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   }
   long long budget = kMaxArenaSmemBytes;
   if (const char* kb = std::getenv("VMC_SMEM_KB")) budget = std::max(0, std::atoi(kb)) * 1024LL;
-  const long long mat_floats = al64(es * P.nmax * (P.nmax | 1));
-  const long long trunc_all = arena_floats(P.nmax, P.kmax, P.trunc_method, P.es);
-  P.arena_in_smem = 0;
-  P.mat_in_smem = 1;  // "theta lives inside the arena" (arena itself may be global)
-  P.arena_floats = trunc_all;
-  if (trunc_all * 4 <= budget) {
-    P.arena_in_smem = 1;
-    P.mat_in_smem = 1;
-  } else if ((trunc_all - mat_floats) * 4 <= budget && P.trunc_method == 0) {
-    P.arena_in_smem = 1;
-    P.mat_in_smem = 0;
-    P.arena_floats = trunc_all - mat_floats;
-  }
-  P.scr1 = (int)al64(es * std::max(chimax * chimax * D * D, (long long)D * D * D * D));
-  {
-    // one bond value of a vertical-energy intermediate holds <= chimax * D^3 floats
-    const long long unit = es * chimax * D * D * D;
-    const long long nbuf = 1 + 2LL * d;
-    long long ch = (budget / 4) / (nbuf * unit);
-    ch = std::max(1LL, std::min(ch, chimax));
-    if (const char* vc = std::getenv("VMC_VCHUNK")) ch = std::max(1LL, std::min(ch, (long long)std::atoi(vc)));
-    P.vchunk = (int)ch;
-    P.vbuf = (int)al64(ch * unit);
-    // The vertical-energy buffers live in (L1-cached) global scratch with the
-    // whole bond range in one chunk: fewer, larger GEMMs beat shared-memory
-    // chunks of a few bond values (measured +5 % at 8x8, D=4, chi=16).
-    // VMC_VERT_SMEM=1 puts them in the shared-memory arena, chunked.
-    P.vert_in_smem = 0;
-    if (const char* vs = std::getenv("VMC_VERT_SMEM"))
-      if (std::atoi(vs) != 0 && P.arena_in_smem && nbuf * P.vbuf * 4 <= budget) P.vert_in_smem = 1;
-  }
-  P.onerow_in_smem = 0;
-  if (P.arena_in_smem && std::max(P.arena_floats, 4LL * P.scr1) * 4 <= budget) {
-    P.onerow_in_smem = 1;
-    P.arena_floats = std::max(P.arena_floats, 4LL * P.scr1);
-  }
-  if (P.vert_in_smem) {
-    P.arena_floats = std::max(P.arena_floats, (1 + 2LL * d) * P.vbuf);
-  } else {
-    P.vchunk = (int)chimax;
-    P.vbuf = (int)SCR;
-  }
-  P.TS = (int)TS; P.ES = (int)ES; P.E2S = (int)E2S; P.MM = (int)MM; P.SCR = (int)SCR;
-  P.n_scr = 11 + 2 * kMaxD;
-  P.VS = strategy == VMC_STRATEGY_VARIATIONAL ? (int)(es * chimax * D * chimax) : 0;
-  P.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + al64(2LL * d * C) + al64(2LL * C) +
-                  3 * al64((long long)C * TS) +
-                  al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
-                  2 * al64(E2S) +
-                  (P.arena_in_smem ? (P.mat_in_smem ? 0 : mat_floats) : al64(P.arena_floats)) +
-                  (long long)P.n_scr * al64(SCR) + al64(2LL * C * P.VS);
+  // Buffer placement for a shared-memory budget (bytes per CTA): truncation
+  // arena, 1-row intermediates and vertical-energy buffers go to shared memory
+  // when they fit, else to the CTA's workspace slot.
+  auto lay_out = [&](DevPlan& Q, long long budget) {
+    const long long mat_floats = al64(es * Q.nmax * (Q.nmax | 1));
+    const long long trunc_all = arena_floats(Q.nmax, Q.kmax, Q.trunc_method, Q.es);
+    Q.arena_in_smem = 0;
+    Q.mat_in_smem = 1;  // "theta lives inside the arena" (arena itself may be global)
+    Q.arena_floats = trunc_all;
+    if (trunc_all * 4 <= budget) {
+      Q.arena_in_smem = 1;
+      Q.mat_in_smem = 1;
+    } else if ((trunc_all - mat_floats) * 4 <= budget && Q.trunc_method == 0) {
+      Q.arena_in_smem = 1;
+      Q.mat_in_smem = 0;
+      Q.arena_floats = trunc_all - mat_floats;
+    }
+    Q.scr1 = (int)al64(es * std::max(chimax * chimax * D * D, (long long)D * D * D * D));
+    {
+      // one bond value of a vertical-energy intermediate holds <= chimax * D^3 floats
+      const long long unit = es * chimax * D * D * D;
+      const long long nbuf = 1 + 2LL * d;
+      long long ch = (budget / 4) / (nbuf * unit);
+      ch = std::max(1LL, std::min(ch, chimax));
+      if (const char* vc = std::getenv("VMC_VCHUNK")) ch = std::max(1LL, std::min(ch, (long long)std::atoi(vc)));
+      Q.vchunk = (int)ch;
+      Q.vbuf = (int)al64(ch * unit);
+      // The vertical-energy buffers live in (L1-cached) global scratch with the
+      // whole bond range in one chunk: fewer, larger GEMMs beat shared-memory
+      // chunks of a few bond values (measured +5 % at 8x8, D=4, chi=16).
+      // VMC_VERT_SMEM=1 puts them in the shared-memory arena, chunked.
+      Q.vert_in_smem = 0;
+      if (const char* vs = std::getenv("VMC_VERT_SMEM"))
+        if (std::atoi(vs) != 0 && Q.arena_in_smem && nbuf * Q.vbuf * 4 <= budget) Q.vert_in_smem = 1;
+    }
+    Q.onerow_in_smem = 0;
+    if (Q.arena_in_smem && std::max(Q.arena_floats, 4LL * Q.scr1) * 4 <= budget) {
+      Q.onerow_in_smem = 1;
+      Q.arena_floats = std::max(Q.arena_floats, 4LL * Q.scr1);
+    }
+    if (Q.vert_in_smem) {
+      Q.arena_floats = std::max(Q.arena_floats, (1 + 2LL * d) * Q.vbuf);
+    } else {
+      Q.vchunk = (int)chimax;
+      Q.vbuf = (int)SCR;
+    }
+    Q.TS = (int)TS; Q.ES = (int)ES; Q.E2S = (int)E2S; Q.MM = (int)MM; Q.SCR = (int)SCR;
+    Q.n_scr = 11 + 2 * kMaxD;
+    Q.VS = strategy == VMC_STRATEGY_VARIATIONAL ? (int)(es * chimax * D * chimax) : 0;
+    Q.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + al64(2LL * d * C) + al64(2LL * C) +
+                    3 * al64((long long)C * TS) +
+                    al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
+                    2 * al64(E2S) +
+                    (Q.arena_in_smem ? (Q.mat_in_smem ? 0 : mat_floats) : al64(Q.arena_floats)) +
+                    (long long)Q.n_scr * al64(SCR) + al64(2LL * C * Q.VS);
+  };
+  lay_out(P, budget);
+  // The same plan with everything in the slot (no dynamic shared memory): an
+  // uneven batch dominated by plans too large for shared memory runs them all
+  // this way, so those keep the whole L1 (shared memory and L1 share one array).
+  pl->hpg = P;
+  lay_out(pl->hpg, 0);
   P.cache_floats_per_chain = al64((long long)R * C * TS);
   if (chimax * D > kMaxVec) {
     delete pl;
@@ -458,7 +487,7 @@ static ChainJob chain_job(const vmc_plan* pl, int mode, const float* tensors, fl
                           const double* uniforms, const int32_t* deltas, int n, void* cache, int full_gradient,
                           float* out_O, int8_t* out_p, double* out_E, double* logamp, double* sign, float* margin,
                           float* gap) {
-  return ChainJob{pl->dplan, mode, n, full_gradient, tensors, perm, configs, uniforms, deltas,
+  return ChainJob{pl->dplan, mode, n, full_gradient, 0, tensors, perm, configs, uniforms, deltas,
                   static_cast<float*>(cache), out_O, out_p, out_E, logamp, sign, margin, gap};
 }
 
@@ -513,6 +542,36 @@ vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors
   return launch(pl, stream, MODE_SWEEP, tensors, configs_inout, uniforms, deltas, n_chains, cache_inout,
                 full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, out_gap, workspace,
                 workspace_bytes, status_dev);
+}
+
+// Floats of the per-CTA cache entries of a recomputing sweep on grid CTAs.
+static size_t recompute_cache_floats(const DevPlan& P, int grid) {
+  return (size_t)grid * P.cache_floats_per_chain + 2 * (size_t)grid * P.R;
+}
+
+size_t vmc_sweep_recompute_workspace_size(const vmc_plan* pl, int n_chains) {
+  if (!pl || n_chains < 0) return 0;
+  return vmc_workspace_size(pl, n_chains) + recompute_cache_floats(pl->hp, n_slots(pl, n_chains)) * 4;
+}
+
+vmc_status vmc_peps_sweep_recompute(const vmc_plan* pl, void* stream, const float* tensors, int32_t* configs_inout,
+                                    const double* uniforms, const int32_t* deltas, int n_chains, int full_gradient,
+                                    float* out_O, int8_t* out_p, double* out_E, double* out_logamp,
+                                    double* out_sign, float* out_margin, float* out_gap, void* workspace,
+                                    size_t workspace_bytes, int32_t* status_dev) {
+  if (!pl || !tensors || !configs_inout || !uniforms || !out_E || !out_logamp || !out_sign || n_chains < 0 ||
+      !workspace || !status_dev)
+    return VMC_ERR_INVALID;
+  if (pl->hp.d > 2 && !deltas) return VMC_ERR_INVALID;
+  if (n_chains == 0) return VMC_OK;
+  if (workspace_bytes < vmc_sweep_recompute_workspace_size(pl, n_chains)) return VMC_ERR_WORKSPACE;
+  const int grid = n_slots(pl, n_chains);
+  float* wsf = static_cast<float*>(workspace);
+  float* entries = wsf + pl->hp.perm_floats + (size_t)grid * pl->hp.slot_floats;
+  ChainJob J = chain_job(pl, MODE_SWEEP, tensors, nullptr, configs_inout, uniforms, deltas, n_chains, entries,
+                         full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, out_gap);
+  J.cache_per_cta = 1;
+  return run_job(pl, stream, J, wsf, grid, status_dev);
 }
 
 // ---------------------------------------------------------------------------
@@ -593,9 +652,11 @@ struct BatchLayout {
   int n = 0;                           // non-empty jobs
   int order[VMC_MAX_BATCH_JOBS];       // caller indices, decreasing cost per chain
   size_t perm_off[VMC_MAX_BATCH_JOBS]; // floats from the workspace start, by caller index
+  size_t entry_off[VMC_MAX_BATCH_JOBS];  // per-CTA cache entries of recomputing sweeps (0: none)
   long long slot_floats = 0;
   size_t slots_off = 0;  // floats
   int grid = 0, threads = 0, es = 0, total = 0;
+  int slot_layout = 0;  // 1: every plan with its no-shared-memory buffer placement
   size_t smem = 0, bytes = 0;
 };
 
@@ -605,8 +666,8 @@ static bool job_valid(const vmc_peps_job& j) {
   if (!j.tensors || !j.configs) return false;
   switch (j.kind) {
     case VMC_JOB_INIT_CACHE: return j.cache != nullptr;
-    case VMC_JOB_SWEEP:
-      return j.uniforms && j.cache && j.out_E && j.logamp && j.sign && (j.plan->hp.d <= 2 || j.deltas);
+    case VMC_JOB_SWEEP:  // no cache: the sweep recomputes the bottom environments
+      return j.uniforms && j.out_E && j.logamp && j.sign && (j.plan->hp.d <= 2 || j.deltas);
     case VMC_JOB_AMP_GRAD: return j.logamp && j.sign;
     case VMC_JOB_LOCAL_ENERGY: return j.logamp && j.sign && j.out_E;
     default: return false;
@@ -619,10 +680,22 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout
   size_t off = 64;  // the item counter
   long long total = 0;
   double cost[VMC_MAX_BATCH_JOBS];
+  // Shared memory and L1 share one array per SM: when plans whose arena does
+  // not fit shared memory (they lean on L1) carry most of the work, the whole
+  // batch runs with no dynamic shared memory, every plan in its slot layout.
+  double w_all = 0.0, w_slot = 0.0;
+  for (int i = 0; i < n_jobs; ++i) {
+    if (!job_valid(jobs[i])) return VMC_ERR_INVALID;
+    const DevPlan& P = jobs[i].plan->hp;
+    cost[i] = (double)P.n_sites * P.nmax * P.nmax * P.nmax * P.es * P.es;
+    w_all += cost[i] * jobs[i].n_chains;
+    if (!P.arena_in_smem) w_slot += cost[i] * jobs[i].n_chains;
+  }
+  L->slot_layout = w_slot > 0.5 * w_all;
+  if (const char* bl = std::getenv("VMC_BATCH_LAYOUT")) L->slot_layout = std::strcmp(bl, "slot") == 0;
   for (int i = 0; i < n_jobs; ++i) {
     const vmc_peps_job& j = jobs[i];
-    if (!job_valid(j)) return VMC_ERR_INVALID;
-    const DevPlan& P = j.plan->hp;
+    const DevPlan& P = L->slot_layout ? j.plan->hpg : j.plan->hp;
     if (L->threads == 0) {
       L->threads = P.threads;
       L->es = P.es;
@@ -635,8 +708,6 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout
     total += j.n_chains;
     L->slot_floats = std::max(L->slot_floats, P.slot_floats);
     L->smem = std::max(L->smem, P.arena_in_smem ? (size_t)P.arena_floats * 4 : (size_t)0);
-    // truncations dominate: n_sites cuts of an O(nmax^3) eigensolve, 4x the flops per complex element
-    cost[i] = (double)P.n_sites * P.nmax * P.nmax * P.nmax * P.es * P.es;
     L->order[L->n++] = i;
   }
   if (total > 0x7fffffffLL) return VMC_ERR_UNSUPPORTED;
@@ -650,7 +721,15 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout
     if (per_sm < 1) return VMC_ERR_UNSUPPORTED;
   }
   L->grid = (int)std::min<long long>(total, (long long)vmc_num_sms() * per_sm);
-  L->bytes = (off + (size_t)L->grid * (size_t)L->slot_floats) * 4;
+  off += (size_t)L->grid * (size_t)L->slot_floats;
+  for (int i = 0; i < n_jobs; ++i) {
+    L->entry_off[i] = 0;
+    if (jobs[i].kind == VMC_JOB_SWEEP && !jobs[i].cache && jobs[i].n_chains > 0) {
+      L->entry_off[i] = off;
+      off += al64((long long)recompute_cache_floats(jobs[i].plan->hp, L->grid));
+    }
+  }
+  L->bytes = off * 4;
   return VMC_OK;
 }
 
@@ -669,12 +748,16 @@ static vmc_status launch_batch(const vmc_peps_job* jobs, const BatchLayout& L, v
     const bool sweep = kind == VMC_JOB_SWEEP, grad = sweep || kind == VMC_JOB_AMP_GRAD;
     bj.job[k] = chain_job(j.plan, kMode[kind], j.tensors, wsf + L.perm_off[L.order[k]], j.configs,
                           sweep ? j.uniforms : nullptr, sweep && j.plan->hp.d > 2 ? j.deltas : nullptr, j.n_chains,
-                          (sweep || kind == VMC_JOB_INIT_CACHE) ? j.cache : nullptr, j.full_gradient,
+                          sweep && L.entry_off[L.order[k]] ? static_cast<void*>(wsf + L.entry_off[L.order[k]])
+                          : (sweep || kind == VMC_JOB_INIT_CACHE) ? j.cache : nullptr,
+                          j.full_gradient,
                           grad ? j.out_O : nullptr, sweep ? j.out_p : nullptr,
                           (sweep || kind == VMC_JOB_LOCAL_ENERGY) ? j.out_E : nullptr,
                           kind == VMC_JOB_INIT_CACHE ? nullptr : j.logamp,
                           kind == VMC_JOB_INIT_CACHE ? nullptr : j.sign, sweep ? j.out_margin : nullptr,
                           grad ? j.out_gap : nullptr);
+    bj.job[k].cache_per_cta = sweep && L.entry_off[L.order[k]] ? 1 : 0;
+    if (L.slot_layout) bj.job[k].P = j.plan->dplan_g;
     bj.first[k + 1] = bj.first[k] + j.n_chains;
     if (K.permute(j.plan->dplan, j.plan->hp.n_sites, j.tensors, wsf + L.perm_off[L.order[k]], stream) !=
         cudaSuccess)

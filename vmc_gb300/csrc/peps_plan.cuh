@@ -140,6 +140,10 @@ struct ChainJob {
   int mode;
   int n_chains;
   int full_gradient;
+  // 0: cache holds one entry per chain (the caller's bottom-environment
+  // cache); 1: cache holds one entry per CTA and a sweep first recomputes the
+  // chain's bottom environments there (nothing is kept between sweeps)
+  int cache_per_cta;
   const float* tensors;
   const float* perm;
   int32_t* configs;

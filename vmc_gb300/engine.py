@@ -113,8 +113,9 @@ class PEPSEngine:
     def cache_bytes(self, n):
         return int(self.lib.vmc_cache_size(self._plan, int(n)))
 
-    def workspace(self, n):
-        need = int(self.lib.vmc_workspace_size(self._plan, int(n)))
+    def workspace(self, n, recompute=False):
+        size = self.lib.vmc_sweep_recompute_workspace_size if recompute else self.lib.vmc_workspace_size
+        need = int(size(self._plan, int(n)))
         if self._ws is None or self._ws.numel() < need:
             self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
         return self._ws
@@ -208,11 +209,23 @@ class PEPSEngine:
             )
         return c, u, deltas, out
 
-    def sweep(self, tensors, configs, uniforms, cache, deltas=None, full_gradient=False, want_O=True,
+    def sweep(self, tensors, configs, uniforms, cache=None, deltas=None, full_gradient=False, want_O=True,
               want_p=True, want_margin=True, out=None):
+        """One sweep of every chain.  ``cache``: the bottom-environment cache from ``init_cache`` (read and
+        rewritten); None recomputes the environments inside the launch instead (the same results as
+        init_cache + sweep, memory per resident CTA rather than per chain)."""
         c, u, deltas, out = self._sweep_io(tensors, configs, uniforms, deltas, full_gradient, want_O, want_p,
                                            want_margin, out)
         n = c.shape[0]
+        if cache is None:
+            # no per-chain cache: the bottom environments are recomputed inside the launch
+            ws = self.workspace(n, recompute=True)
+            st = self.lib.vmc_peps_sweep_recompute(
+                self._plan, self._stream(), _vp(tensors), _vp(c), _vp(u), _vp(deltas), n, int(bool(full_gradient)),
+                _vp(out.O), _vp(out.p), _vp(out.E), _vp(out.logamp), _vp(out.sign), _vp(out.margin), _vp(out.gap),
+                _vp(ws), ws.numel(), _vp(self._status))
+            _abi.check(self.lib, st, "vmc_peps_sweep_recompute")
+            return out
         ws = self.workspace(n)
         st = self.lib.vmc_peps_sweep(self._plan, self._stream(), _vp(tensors), _vp(c), _vp(u), _vp(deltas), n,
                                      _vp(cache), int(bool(full_gradient)), _vp(out.O), _vp(out.p), _vp(out.E),
@@ -264,7 +277,7 @@ class PEPSEngine:
         out = SweepResult(configs=c, O=None, p=None, E=None, logamp=None, sign=None, margin=None)
         return BatchJob(self, _abi.VMC_JOB_INIT_CACHE, tensors, out, cache=cache)
 
-    def sweep_job(self, tensors, configs, uniforms, cache, deltas=None, full_gradient=False, want_O=True,
+    def sweep_job(self, tensors, configs, uniforms, cache=None, deltas=None, full_gradient=False, want_O=True,
                   want_p=True, want_margin=True, out=None):
         c, u, deltas, out = self._sweep_io(tensors, configs, uniforms, deltas, full_gradient, want_O, want_p,
                                            want_margin, out)
