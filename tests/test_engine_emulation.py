@@ -107,7 +107,8 @@ def test_amp_grad_and_local_energy_match_oracle(emu_lib):
 
 
 @pytest.mark.parametrize("env", [{"VMC_VCHUNK": "1", "VMC_VERT_SMEM": "1"}, {"VMC_TRUNCATION": "jacobi"}, {"VMC_SMEM_KB": "0"},
-                                 {"VMC_SMEM_KB": "24"}], ids=["chunk1", "jacobi", "all-global", "mat-global"])
+                                 {"VMC_SMEM_KB": "24"}, {"VMC_TILE_POLICY": "1"}, {"VMC_TILE_POLICY": "2"}],
+                         ids=["chunk1", "jacobi", "all-global", "mat-global", "small-tiles", "large-tiles"])
 def test_alternative_engine_paths_match_oracle(emu_lib, env, monkeypatch):
     """Chunked vertical energy, the Jacobi truncation and the global-memory fallbacks agree with the oracle."""
     for k, v in env.items():

@@ -271,9 +271,16 @@ __device__ inline void gemm_mma(const Gemm& g) {
 #endif
 
 // CTA-wide GEMM; ends with a barrier so C is visible to the whole CTA.
+// Register-tile policy of the CTA's GEMMs, set per chain from its plan (an
+// autotuned choice per (D, chi)): 0 the default thresholds below; 1 smaller
+// tiles (more threads busy on small products); 2 larger tiles (fewer loads
+// per multiply-add on large ones).
+VMC_SHARED int g_tile_policy;
+
 __device__ inline void cta_gemm(const Gemm& g) {
   const int work = g.M * g.N;
-  const int nt = blockDim.x;
+  const int pol = g_tile_policy;
+  const int nt = pol == 1 ? 2 * blockDim.x : pol == 2 ? blockDim.x / 2 : blockDim.x;
   if (g.cplx) {
     if (g.M >= 4 && g.N >= 2 && work >= nt * 8) {
       gemm_tiles_c<4, 2>(g);

@@ -1017,6 +1017,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   float* out_margin = J.out_margin;
   float* out_gap = J.out_gap;
   Slot S = make_slot(P, slot_base);
+  if (threadIdx.x == 0) g_tile_policy = P.tile_policy;  // read by cta_gemm after the next barrier
   const Arena ar = make_arena(P, P.arena_in_smem ? dyn_smem : S.arena, S.arena);
   if (P.onerow_in_smem) {
     // the 1-row environment GEMM intermediates are never live during a truncation

@@ -320,6 +320,8 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   {
     const char* th = std::getenv("VMC_THREADS");
     P.threads = th ? std::max(64, std::min(kThreads, std::atoi(th))) : kDefaultThreads;
+    const char* tp = std::getenv("VMC_TILE_POLICY");
+    P.tile_policy = tp ? std::max(0, std::min(2, std::atoi(tp))) : 0;
   }
   long long budget = kMaxArenaSmemBytes;
   if (const char* kb = std::getenv("VMC_SMEM_KB")) budget = std::max(0, std::atoi(kb)) * 1024LL;

@@ -43,6 +43,7 @@ struct DevPlan {
   int arena_in_smem;      // truncation arena in dynamic shared memory
   int mat_in_smem;        // theta matrix inside the arena (else in a separate global slot region)
   int threads;            // CTA size of the fused kernel
+  int tile_policy;        // register-tile policy of the CTA GEMMs (cta_gemm)
   long long arena_floats;
   int scr1;               // size of one 1-row GEMM intermediate (floats)
   int vchunk, vbuf;       // vertical-energy chunk (bond values) and buffer size (floats)
