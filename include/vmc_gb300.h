@@ -90,6 +90,29 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
                          int dtype, int strategy, int n_sweeps, vmc_plan** out_plan);
 
 /*
+ * Launch configuration of a plan -- what the autotuner (vmc_gb300.autotune)
+ * picks per (lattice, D, chi, dtype, strategy).  No reference counterpart
+ * (XLA picks its own kernels).  Every choice computes the same quantities;
+ * they differ in FP32 rounding only (GEMM and reduction order).
+ *   threads      CTA size, a multiple of 32 in [64, 256]; 0: 128
+ *   smem_kb      dynamic shared memory per CTA for the truncation arena and
+ *                the 1-row intermediates, 0..52 KB; -1: 52 (0: all in the
+ *                CTA's workspace slot, L1-cached)
+ *   tile_policy  register tiles of the CTA GEMMs: 0 default, 1 smaller, 2 larger
+ * vmc_peps_plan uses the defaults, overridden by the VMC_THREADS, VMC_SMEM_KB
+ * and VMC_TILE_POLICY environment variables when set; vmc_peps_plan_ex with
+ * options ignores the environment.
+ */
+typedef struct {
+  int threads;
+  int smem_kb;
+  int tile_policy;
+} vmc_plan_options;
+vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype,
+                            int strategy, int n_sweeps, const vmc_plan_options* options,
+                            vmc_plan** out_plan);
+
+/*
  * Attach the bucketed LocalHamiltonian (local_terms.py:165-200).  Terms of
  * the same kind and location are summed by the caller.  All arrays are HOST
  * arrays of float64, copied into the plan:
@@ -118,6 +141,10 @@ void vmc_plan_destroy(vmc_plan* plan);
  * params_per_site, src/vmc/utils/smallo.py:23-35) and of the full tensors. */
 int64_t vmc_peps_n_params_sliced(const vmc_plan* plan);
 int64_t vmc_peps_n_params_full(const vmc_plan* plan);
+
+/* Chains a launch runs at once: resident CTAs per SM (for the plan's CTA size
+ * and shared memory) times the SM count; the workspace holds one slot each. */
+int vmc_plan_resident_ctas(const vmc_plan* plan);
 
 /* Bytes of the per-chain bottom-environment cache (Cache.bottom_envs,
  * kernels.py:32-35) for n_chains chains, and of the scratch workspace one

@@ -1,0 +1,60 @@
+"""Launch options and the autotuner on the host-emulation build: explicit options build plans,
+invalid ones are refused, and tune / tuned_options time the candidates and keep the winner in the
+cache file (the emulation's times mean nothing for a GPU; the code path is what is checked)."""
+from __future__ import annotations
+
+import ctypes as ct
+import json
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import peps as oracle
+from tests.helpers import assert_parity, fp32, hamiltonian, make_case, oracle_sweep
+from vmc_gb300 import _abi
+from vmc_gb300.autotune import CANDIDATES, tune, tuned_options
+from vmc_gb300.engine import PEPSEngine
+from vmc_gb300.lowering import pack_tensors
+
+
+@pytest.mark.parametrize("options", CANDIDATES)
+def test_every_candidate_matches_the_oracle(emu_lib, options):
+    shape, D, chi = (4, 4), 3, 6
+    H = hamiltonian("heisenberg", shape)
+    T, cfg, u = make_case(shape, D, 4, seed=5)
+    eng = PEPSEngine(shape, D, chi, 2, "ZipUp", operator=H, device="cpu", lib=emu_lib, options=options)
+    assert eng.options == options and eng.resident_chains > 0
+    tens = torch.from_numpy(pack_tensors(T))
+    c = torch.from_numpy(cfg.copy())
+    res = eng.sweep(tens, c, torch.from_numpy(u), eng.init_cache(tens, c))
+    c2, ctx, le = oracle_sweep(fp32(T), shape, D, "ZipUp", chi, H, cfg, u)
+    assert np.array_equal(res.configs.numpy(), c2)
+    e_ref = le.local_estimate
+    assert_parity(np.abs(res.E.numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
+
+
+def test_invalid_options_are_refused(emu_lib):
+    shape = _abi.VmcShape(3, 3)
+    plan = ct.c_void_p()
+    for bad in [(48, -1, 0), (300, -1, 0), (128, -2, 0), (128, -1, 3)]:
+        o = _abi.VmcPlanOptions(*bad)
+        assert emu_lib.vmc_peps_plan_ex(ct.byref(shape), 2, 4, 2, 0, 1, 2, ct.byref(o), ct.byref(plan)) == \
+            _abi.VMC_ERR_INVALID
+    with pytest.raises(ValueError):
+        PEPSEngine((3, 3), 2, 4, device="cpu", lib=emu_lib, options="fastest")
+
+
+def test_tune_and_cache(emu_lib, tmp_path, monkeypatch):
+    monkeypatch.setenv("VMC_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    entry = tune((3, 3), 2, 4, lib=emu_lib, candidates=CANDIDATES[:2])
+    assert entry["options"] in CANDIDATES[:2] and len(entry["candidates"]) == 2
+    data = json.loads((tmp_path / "tune.json").read_text())
+    (key,) = data
+    assert "3x3|D2|chi4" in key and data[key]["options"] == entry["options"]
+    # a cached problem is not re-timed: the stored winner comes back
+    data[key]["options"] = CANDIDATES[5]
+    (tmp_path / "tune.json").write_text(json.dumps(data))
+    assert tuned_options((3, 3), 2, 4, lib=emu_lib) == CANDIDATES[5]
+    eng = PEPSEngine((3, 3), 2, 4, device="cpu", lib=emu_lib, options="auto")
+    assert eng.options == CANDIDATES[5]

@@ -44,6 +44,11 @@ _I = ct.c_int
 _SZ = ct.c_size_t
 
 
+class VmcPlanOptions(ct.Structure):
+    """vmc_plan_options: a plan's launch configuration."""
+    _fields_ = [("threads", _I), ("smem_kb", _I), ("tile_policy", _I)]
+
+
 class VmcPepsJob(ct.Structure):
     """vmc_peps_job: one call of an uneven batch."""
     _fields_ = [("plan", _P), ("kind", _I), ("n_chains", _I), ("full_gradient", _I), ("tensors", _P),
@@ -56,10 +61,12 @@ SIGNATURES = {
     "vmc_version": (ct.c_char_p, []),
     "vmc_status_string": (ct.c_char_p, [_I]),
     "vmc_peps_plan": (_I, [ct.POINTER(VmcShape), _I, _I, _I, _I, _I, _I, ct.POINTER(_P)]),
+    "vmc_peps_plan_ex": (_I, [ct.POINTER(VmcShape), _I, _I, _I, _I, _I, _I, ct.POINTER(VmcPlanOptions), ct.POINTER(_P)]),
     "vmc_peps_plan_set_operator": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P]),
     "vmc_plan_destroy": (None, [_P]),
     "vmc_peps_n_params_sliced": (ct.c_int64, [_P]),
     "vmc_peps_n_params_full": (ct.c_int64, [_P]),
+    "vmc_plan_resident_ctas": (_I, [_P]),
     "vmc_cache_size": (_SZ, [_P, _I]),
     "vmc_workspace_size": (_SZ, [_P, _I]),
     "vmc_peps_init_cache": (_I, [_P, _P, _P, _P, _I, _P, _P, _SZ, _P]),

@@ -1,0 +1,147 @@
+"""Launch-configuration autotuner: per (lattice, D, chi, d, dtype, strategy), the CTA size, shared-memory
+budget and GEMM register-tile policy of the fused kernel that give the most samples/s on this GPU.
+
+``tune`` builds one plan per candidate (``vmc_peps_plan_ex``), times full sweeps on seeded synthetic
+inputs -- whole waves of chains, after a warm-up sweep -- and records every candidate's rate with the
+winner in a JSON cache keyed by GPU name and problem (``$VMC_AUTOTUNE_CACHE``, default
+``~/.cache/vmc_gb300/autotune.json``).  ``tuned_options`` returns the cached winner, tuning first when
+the problem is new.  All candidates compute the same quantities and differ only in FP32 rounding
+order; each is covered by the parity tests.  The cache is the only process-wide mutable state of the
+package and is guarded by a lock.
+"""
+from __future__ import annotations
+
+import json
+import os
+import threading
+from pathlib import Path
+
+import numpy as np
+import torch
+
+__all__ = ["CANDIDATES", "cache_path", "tune", "tuned_options"]
+
+# (threads, smem_kb, tile_policy); smem_kb -1 = the 52 KB default, 0 = all buffers in the slot
+CANDIDATES = [
+    {"threads": 128, "smem_kb": -1, "tile_policy": 0},
+    {"threads": 128, "smem_kb": -1, "tile_policy": 1},
+    {"threads": 128, "smem_kb": -1, "tile_policy": 2},
+    {"threads": 128, "smem_kb": 0, "tile_policy": 0},
+    {"threads": 256, "smem_kb": -1, "tile_policy": 0},
+    {"threads": 256, "smem_kb": -1, "tile_policy": 2},
+]
+
+_LOCK = threading.Lock()
+
+
+def cache_path() -> Path:
+    p = os.environ.get("VMC_AUTOTUNE_CACHE")
+    return Path(p) if p else Path.home() / ".cache" / "vmc_gb300" / "autotune.json"
+
+
+def _device_name(device) -> str:
+    device = torch.device(device)
+    if device.type == "cuda":
+        return torch.cuda.get_device_name(device)
+    return "host-emulation"
+
+
+def _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype) -> str:
+    return (f"{_device_name(device)}|{shape[0]}x{shape[1]}|D{bond_dim}|chi{chi}|d{phys_dim}|{strategy}"
+            f"|sweeps{n_sweeps}|{dtype}")
+
+
+def _load() -> dict:
+    p = cache_path()
+    try:
+        return json.loads(p.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(key: str, entry: dict) -> None:
+    p = cache_path()
+    p.parent.mkdir(parents=True, exist_ok=True)
+    data = _load()
+    data[key] = entry
+    tmp = p.with_suffix(f".{os.getpid()}.tmp")
+    tmp.write_text(json.dumps(data, indent=1, sort_keys=True))
+    tmp.replace(p)
+
+
+def _time_candidate(options, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator, device, lib,
+                    waves, reps, seed=0):
+    from .engine import PEPSEngine
+    from .lowering import pack_tensors
+    from .synthetic import initial_configs, random_tensors
+
+    eng = PEPSEngine(shape, bond_dim, chi, phys_dim, strategy, n_sweeps, operator=operator, device=device,
+                     lib=lib, dtype=dtype, options=options)
+    n = max(1, waves * eng.resident_chains)
+    n_sites = shape[0] * shape[1]
+    T = random_tensors(shape, bond_dim, phys_dim=phys_dim, seed=seed,
+                       dtype=np.complex128 if dtype == "complex64" else np.float64)
+    dev = eng.device
+    tens = torch.from_numpy(pack_tensors(T)).to(dev)
+    cfg = torch.from_numpy(initial_configs(n, n_sites, phys_dim, seed=seed)).to(dev)
+    rng = np.random.default_rng(seed + 1)
+    u = [torch.from_numpy(rng.random((n, n_sites))).to(dev) for _ in range(reps + 1)]
+    deltas = None
+    if phys_dim > 2:
+        deltas = torch.from_numpy(rng.integers(1, phys_dim, (n, n_sites)).astype(np.int32)).to(dev)
+    cache = eng.init_cache(tens, cfg)
+    out = eng.sweep(tens, cfg, u[0], cache, deltas=deltas)
+    if dev.type == "cuda":
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for i in range(reps):
+            out = eng.sweep(tens, cfg, u[i + 1], cache, deltas=deltas, out=out)
+        b.record()
+        torch.cuda.synchronize(dev)
+        seconds = a.elapsed_time(b) / 1e3
+    else:  # host-emulation build: exercises the code path; its times mean nothing for a GPU
+        import time
+
+        t0 = time.perf_counter()
+        for i in range(reps):
+            out = eng.sweep(tens, cfg, u[i + 1], cache, deltas=deltas, out=out)
+        seconds = time.perf_counter() - t0
+    eng.raise_on_status()
+    return n * reps / seconds
+
+
+def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32", operator=None,
+         device=None, lib=None, candidates=None, waves=1, reps=1, store=True) -> dict:
+    """Time every candidate on this problem; returns {"options", "samples_per_s", "candidates"}."""
+    from .operators import heisenberg
+
+    shape = (int(shape[0]), int(shape[1]))
+    device = torch.device(device if device is not None else ("cuda" if lib is None else "cpu"))
+    if operator is None and phys_dim != 2:
+        raise ValueError("tuning a d != 2 plan needs its operator")
+    op = operator if operator is not None else heisenberg(shape)
+    results = []
+    for cand in candidates or CANDIDATES:
+        rate = _time_candidate(cand, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op, device, lib,
+                               waves, reps)
+        results.append({"options": dict(cand), "samples_per_s": rate})
+    best = max(results, key=lambda r: r["samples_per_s"])
+    entry = {"options": best["options"], "samples_per_s": best["samples_per_s"], "candidates": results}
+    if store:
+        with _LOCK:
+            _store(_key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype), entry)
+    return entry
+
+
+def tuned_options(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32", operator=None,
+                  device=None, lib=None) -> dict:
+    """The cached winner for this problem on this GPU, tuning it first when it is not cached."""
+    shape = (int(shape[0]), int(shape[1]))
+    device = torch.device(device if device is not None else ("cuda" if lib is None else "cpu"))
+    key = _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype)
+    with _LOCK:
+        hit = _load().get(key)
+    if hit is not None:
+        return dict(hit["options"])
+    return dict(tune(shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator, device, lib)["options"])

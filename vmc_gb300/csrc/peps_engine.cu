@@ -203,7 +203,15 @@ const char* vmc_status_string(vmc_status s) {
 
 vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype, int strategy,
                          int n_sweeps, vmc_plan** out_plan) {
+  return vmc_peps_plan_ex(shape, bond_dim, chi, phys_dim, dtype, strategy, n_sweeps, nullptr, out_plan);
+}
+
+vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype, int strategy,
+                            int n_sweeps, const vmc_plan_options* opts, vmc_plan** out_plan) {
   if (!shape || !out_plan) return VMC_ERR_INVALID;
+  if (opts && (opts->threads != 0 && (opts->threads < 64 || opts->threads > kThreads || opts->threads % 32 != 0)))
+    return VMC_ERR_INVALID;
+  if (opts && (opts->tile_policy < 0 || opts->tile_policy > 2 || opts->smem_kb < -1)) return VMC_ERR_INVALID;
   *out_plan = nullptr;
   const int R = shape->n_rows, C = shape->n_cols;
   if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
@@ -318,13 +326,19 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
     P.trunc_method = (tm && std::strcmp(tm, "jacobi") == 0 && es == 1) ? 1 : 0;
   }
   {
-    const char* th = std::getenv("VMC_THREADS");
-    P.threads = th ? std::max(64, std::min(kThreads, std::atoi(th))) : kDefaultThreads;
-    const char* tp = std::getenv("VMC_TILE_POLICY");
-    P.tile_policy = tp ? std::max(0, std::min(2, std::atoi(tp))) : 0;
+    // explicit options (an autotuned choice) or, without them, the VMC_* environment
+    const char* th = opts ? nullptr : std::getenv("VMC_THREADS");
+    P.threads = opts ? (opts->threads ? opts->threads : kDefaultThreads)
+                     : th ? std::max(64, std::min(kThreads, std::atoi(th))) : kDefaultThreads;
+    const char* tp = opts ? nullptr : std::getenv("VMC_TILE_POLICY");
+    P.tile_policy = opts ? opts->tile_policy : tp ? std::max(0, std::min(2, std::atoi(tp))) : 0;
   }
   long long budget = kMaxArenaSmemBytes;
-  if (const char* kb = std::getenv("VMC_SMEM_KB")) budget = std::max(0, std::atoi(kb)) * 1024LL;
+  if (opts) {
+    if (opts->smem_kb >= 0) budget = std::min<long long>(opts->smem_kb, kMaxArenaSmemBytes / 1024) * 1024LL;
+  } else if (const char* kb = std::getenv("VMC_SMEM_KB")) {
+    budget = std::max(0, std::atoi(kb)) * 1024LL;
+  }
   // Buffer placement for a shared-memory budget (bytes per CTA): truncation
   // arena, 1-row intermediates and vertical-energy buffers go to shared memory
   // when they fit, else to the CTA's workspace slot.
@@ -470,6 +484,7 @@ void vmc_plan_destroy(vmc_plan* pl) {
 }
 
 int64_t vmc_peps_n_params_sliced(const vmc_plan* pl) { return pl ? pl->hp.np_sliced : 0; }
+int vmc_plan_resident_ctas(const vmc_plan* pl) { return pl ? pl->slots_max : 0; }
 int64_t vmc_peps_n_params_full(const vmc_plan* pl) { return pl ? (int64_t)pl->hp.np_sliced * pl->hp.d : 0; }
 
 size_t vmc_cache_size(const vmc_plan* pl, int n_chains) {

@@ -53,7 +53,10 @@ class PEPSEngine:
     """Plan + workspace for one (shape, D, chi, d, strategy, operator)."""
 
     def __init__(self, shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, operator=None,
-                 device=None, lib=None, dtype="float32"):
+                 device=None, lib=None, dtype="float32", options=None):
+        """``options``: the plan's launch configuration -- None (defaults, or the VMC_* environment), a
+        dict with keys threads / smem_kb / tile_policy (vmc_plan_options), or "auto" for the
+        autotuned choice of this (lattice, D, chi, dtype, strategy) from vmc_gb300.autotune."""
         self.shape = (int(shape[0]), int(shape[1]))
         self.complex = str(dtype).replace("torch.", "") in ("complex64", "complex128")
         # dtypes of this engine's parameters / O_k and of E_loc
@@ -75,11 +78,27 @@ class PEPSEngine:
         self.lib = lib
         plan = ct.c_void_p()
         sid = STRATEGY_IDS[strategy] if isinstance(strategy, str) else int(strategy)
+        if isinstance(options, str):
+            if options != "auto":
+                raise ValueError("options must be None, a dict or 'auto'")
+            from .autotune import tuned_options
+
+            options = tuned_options(self.shape, self.bond_dim, self.chi, self.phys_dim, strategy, n_sweeps,
+                                    "complex64" if self.complex else "float32", operator=operator,
+                                    device=self.device, lib=lib)
+        self.options = None if options is None else dict(options)
+        dt = _abi.VMC_DTYPE_C64 if self.complex else _abi.VMC_DTYPE_F32
         with torch.cuda.device(self.device) if self.device.type == "cuda" else _null():
-            st = lib.vmc_peps_plan(ct.byref(_abi.VmcShape(*self.shape)), self.bond_dim, self.chi,
-                                   self.phys_dim, _abi.VMC_DTYPE_C64 if self.complex else _abi.VMC_DTYPE_F32,
-                                   sid, int(n_sweeps), ct.byref(plan))
+            if options is None:
+                st = lib.vmc_peps_plan(ct.byref(_abi.VmcShape(*self.shape)), self.bond_dim, self.chi,
+                                       self.phys_dim, dt, sid, int(n_sweeps), ct.byref(plan))
+            else:
+                o = _abi.VmcPlanOptions(int(options.get("threads", 0)), int(options.get("smem_kb", -1)),
+                                        int(options.get("tile_policy", 0)))
+                st = lib.vmc_peps_plan_ex(ct.byref(_abi.VmcShape(*self.shape)), self.bond_dim, self.chi,
+                                          self.phys_dim, dt, sid, int(n_sweeps), ct.byref(o), ct.byref(plan))
         _abi.check(lib, st, "vmc_peps_plan")
+        self.resident_chains = int(lib.vmc_plan_resident_ctas(plan))
         self._plan = plan
         self.n_params_sliced = int(lib.vmc_peps_n_params_sliced(plan))
         self.n_params_full = int(lib.vmc_peps_n_params_full(plan))
