@@ -74,3 +74,22 @@ def test_no_cpu_fallback():
 
     with pytest.raises(EngineUnavailable):
         qr_pivoted(torch.zeros((3, 3), dtype=torch.float64))
+
+
+@pytest.mark.parametrize("m,n,rank", [(30, 100, 12), (60, 40, 25), (50, 50, 50)],
+                         ids=["wide-rank-deficient", "tall-rank-deficient", "square-full"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_qr_solve_both_min_norm_branches_match_oracle(emu_lib, m, n, rank, cplx):
+    """preconditioners.py:166-214 through the device factorisation: the minimum-norm solve picks the
+    smaller of its two equivalent systems (rank x rank or n2 x n2); both give the oracle's x."""
+    from oracle import sr as osr
+    from vmc_gb300 import qgt as gq
+    from vmc_gb300.preconditioners import _qr_solve
+
+    rng = np.random.default_rng(m + n + rank)
+    O = _rand(rng, (m, rank), cplx) @ _rand(rng, (rank, n), cplx)
+    dv = _rand(rng, (m,), cplx)
+    x, met = _qr_solve(gq.Jacobian(torch.as_tensor(O)), torch.as_tensor(dv), None, True, lib=emu_lib)
+    xr, mr = osr.qr_solve(osr.Jacobian(O), dv)
+    assert met["rank"] == mr["rank"]
+    assert np.linalg.norm(x.numpy() - xr) <= 1e-9 * np.linalg.norm(xr)

@@ -101,7 +101,10 @@ def _qr_solve(jac: Jacobian, dv, rcond, min_norm, lib=None):
     dvd = dv.to(device=o.device, dtype=dt)
     r, piv, y = qr_pivoted(oc, dvd, lib=lib)
     y = y[:, 0]
-    sv = torch.linalg.svdvals(r)
+    # matrix_rank(r): R's singular values are those of the k x k triangle of a QR of R^H (no
+    # squaring, unlike R R^H), so the SVD runs on k x k instead of k x n
+    rt = torch.linalg.qr(r.mH, mode="r")[1] if r.shape[1] > r.shape[0] else r
+    sv = torch.linalg.svdvals(rt)
     eps = torch.finfo(torch.float64).eps
     smax = sv.max() if sv.numel() else torch.zeros((), dtype=torch.float64, device=o.device)
     tol = (max(r.shape) * eps if rcond is None else rcond) * smax
@@ -112,12 +115,19 @@ def _qr_solve(jac: Jacobian, dv, rcond, min_norm, lib=None):
     if rank:
         r11, r12, y1 = r[:rank, :rank], r[:rank, rank:], y[:rank, None]
         if min_norm and n2 > 0:
+            # minimum-norm z = (z1, z2) of z1 + B z2 = a, a = R11^-1 y1, B = R11^-1 R12.  The reference
+            # solves (B^H B + I) z2 = B^H a (n2 x n2); by the push-through identity the same z is
+            # z1 = (I + B B^H)^-1 a, z2 = B^H z1 (rank x rank): the smaller system is solved.
             a = torch.linalg.solve_triangular(r11, y1, upper=True)
             bm = torch.linalg.solve_triangular(r11, r12, upper=True)
-            lhs = bm.mH @ bm + torch.eye(n2, dtype=dt, device=o.device)
-            chol, _ = torch.linalg.cholesky_ex(lhs)  # lhs = B^H B + I is positive definite
-            x2 = torch.cholesky_solve(bm.mH @ a, chol)
-            x1 = a - bm @ x2
+            if n2 > rank:
+                chol, _ = torch.linalg.cholesky_ex(bm @ bm.mH + torch.eye(rank, dtype=dt, device=o.device))
+                x1 = torch.cholesky_solve(a, chol)
+                x2 = bm.mH @ x1
+            else:
+                chol, _ = torch.linalg.cholesky_ex(bm.mH @ bm + torch.eye(n2, dtype=dt, device=o.device))
+                x2 = torch.cholesky_solve(bm.mH @ a, chol)
+                x1 = a - bm @ x2
         else:
             x1 = torch.linalg.solve_triangular(r11, y1, upper=True)
             x2 = torch.zeros((n2, 1), dtype=dt, device=o.device)
