@@ -277,7 +277,15 @@ __device__ inline void gemm_mma(const Gemm& g) {
 // per multiply-add on large ones).
 VMC_SHARED int g_tile_policy;
 
-__device__ inline void cta_gemm(const Gemm& g) {
+// VMC_GEMM_NOINLINE=1 compiles one out-of-line copy of the GEMM instead of one
+// per call site (smaller code, one call per GEMM).
+#if defined(VMC_GEMM_NOINLINE) && VMC_GEMM_NOINLINE
+#define VMC_GEMM_LINKAGE static __device__ __noinline__
+#else
+#define VMC_GEMM_LINKAGE __device__ inline
+#endif
+
+VMC_GEMM_LINKAGE void cta_gemm(const Gemm& g) {
   const int work = g.M * g.N;
   const int pol = g_tile_policy;
   const int nt = pol == 1 ? 2 * blockDim.x : pol == 2 ? blockDim.x / 2 : blockDim.x;

@@ -1179,7 +1179,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
 // CTA keeps its workspace slot at slots + blockIdx.x * slot_floats.
 // At most 128 registers per thread (two 256-thread CTAs, or four of the default
 // 128 threads, per SM): left free, the compiler takes all 255 and halves occupancy.
-__global__ void __launch_bounds__(kThreads, 2) peps_kernel(const __grid_constant__ BatchJobs jobs, float* slots,
+__global__ void __launch_bounds__(kThreads, VMC_MIN_CTAS) peps_kernel(const __grid_constant__ BatchJobs jobs, float* slots,
                                                            int32_t* next, int32_t* status) {
   VMC_SHARED int item;
   float* slot = slots + (size_t)blockIdx.x * jobs.slot_floats;

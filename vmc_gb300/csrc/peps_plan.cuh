@@ -18,7 +18,15 @@
 
 namespace vmc {
 
-constexpr int kThreads = 256;         // largest CTA the kernel is compiled for
+// Largest CTA the fused kernel is compiled for, and the CTAs of that size an
+// SM must hold (__launch_bounds__): 256 x 2 caps registers at 128 per thread.
+#ifndef VMC_MAX_THREADS
+#define VMC_MAX_THREADS 256
+#endif
+#ifndef VMC_MIN_CTAS
+#define VMC_MIN_CTAS 2
+#endif
+constexpr int kThreads = VMC_MAX_THREADS;
 constexpr int kDefaultThreads = 128;  // one chain per 4 warps: more chains resident per SM
 constexpr int kMaxVec = 512;   // max vectors in one truncation (chi * D)
 constexpr int kMaxCols = 64;   // max lattice columns
