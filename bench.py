@@ -128,7 +128,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-NCU_DRAM_BYTES_PER_SAMPLE = {"heis8x8_D4_chi16": 13.179e9 / 608}
+NCU_DRAM_BYTES_PER_SAMPLE = {"heis8x8_D4_chi16": 13.359e9 / 608}
 
 
 def _peaks():
@@ -309,10 +309,10 @@ def run_ours(args, rank, world, local_rank):
     mean_launch_s = statistics.mean(launch_ms) / 1e3
     achieved = n * flops / mean_launch_s / 1e12 if flops else None
     peak = peaks.get("bf16_tflops")
-    # DRAM bytes per sample of peps_kernel from one ncu capture of this workload
-    # (608 chains, dram__bytes_read.sum + dram__bytes_write.sum = 13.18 GB, see
-    # profiles/peps_kernel_heis8x8_D4_chi16.md); each chain reuses its CTA slot,
-    # so traffic scales with the chains of a launch
+    # DRAM bytes per sample of peps_kernel from one ncu --set full capture of this
+    # workload (608 chains, dram__bytes_read.sum + dram__bytes_write.sum =
+    # 13.36 GB); each chain reuses its CTA slot, so traffic scales with the chains
+    # of a launch
     traffic = NCU_DRAM_BYTES_PER_SAMPLE.get(w.name)
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved and peak else None,
@@ -370,11 +370,21 @@ def run_uneven(args, rank, world, local_rank):
     gen = torch.Generator(device=dev).manual_seed(1000 * rank + 7)
     peaks, peak_kind = _peaks()
     peak = peaks.get("bf16_tflops")
+    from vmc_gb300.autotune import tuned_options
+
+    # launch configuration per lattice: the autotuned one (alone); the batch runs every plan with
+    # one CTA size, so it takes the options of the lattice with the most work per chain
+    tuned = {name: tuned_options(WORKLOADS[name].shape, WORKLOADS[name].bond_dim, WORKLOADS[name].chi,
+                                 WORKLOADS[name].phys_dim, WORKLOADS[name].strategy, 2, WORKLOADS[name].dtype,
+                                 operator=WORKLOADS[name].operator(), device=dev) for name in UNEVEN}
+    dominant = max(UNEVEN, key=lambda name: WORKLOADS[name].flops_per_sample())
+    batch_options = tuned[dominant]
     cases = []
     for name in UNEVEN:
         w = WORKLOADS[name]
         n_sites = w.shape[0] * w.shape[1]
-        eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev)
+        eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev,
+                         options=tuned[name])
         tens = torch.from_numpy(pack_tensors(w.tensors(seed=0))).to(dev)
         cfg0 = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
         uni = torch.rand((total, n, n_sites), generator=gen, dtype=torch.float64, device=dev)
@@ -407,14 +417,18 @@ def run_uneven(args, rank, world, local_rank):
         t_alone += t
         flops = w.flops_per_sample()
         tf = n * flops / t / 1e12
-        per_shape.append({"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
+        per_shape.append({"workload": w.name, "options": tuned[w.name], "shape": list(w.shape),
+                          "bond_dim": w.bond_dim, "chi": w.chi,
                           "chains": n, "samples_per_s": n / t, "ms_per_launch": 1e3 * t,
                           "tflops_algorithmic": tf, "roofline_frac": tf / peak if peak else None})
         del cache
 
     # ---------------- one launch over all four, captured in a CUDA graph ----------------
     jobs, ubuf = [], []
-    for w, eng, tens, cfg0, uni in cases:
+    for i, (w, eng, tens, cfg0, uni) in enumerate(cases):
+        eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev,
+                         options=batch_options)
+        cases[i] = (w, eng, tens, cfg0, uni)
         cfg = cfg0.clone()
         cache = eng.init_cache(tens, cfg)
         u = uni[0].clone()
@@ -465,6 +479,7 @@ def run_uneven(args, rank, world, local_rank):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "uneven", "shapes": UNEVEN, "chains_per_shape": n, "model": "heisenberg",
                    "strategy": "ZipUp(chi)", "launch": "one persistent launch (vmc_peps_batch) in a CUDA graph",
+                   "options_alone": tuned, "options_batch": batch_options,
                    "parallelism": "replicas x1",
                    "l2": "inputs larger than L2 (bottom-env caches of all four lattices)"},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

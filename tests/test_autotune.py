@@ -58,3 +58,15 @@ def test_tune_and_cache(emu_lib, tmp_path, monkeypatch):
     assert tuned_options((3, 3), 2, 4, lib=emu_lib) == CANDIDATES[5]
     eng = PEPSEngine((3, 3), 2, 4, device="cpu", lib=emu_lib, options="auto")
     assert eng.options == CANDIDATES[5]
+
+
+def test_shipped_table_is_the_fallback(emu_lib, tmp_path, monkeypatch):
+    import vmc_gb300.autotune as at
+
+    monkeypatch.setenv("VMC_AUTOTUNE_CACHE", str(tmp_path / "empty.json"))
+    key = at._key(torch.device("cpu"), (3, 3), 2, 4, 2, "ZipUp", 2, "float32")
+    shipped = tmp_path / "shipped.json"
+    shipped.write_text(json.dumps({key: {"options": CANDIDATES[4], "samples_per_s": 1.0, "candidates": []}}))
+    monkeypatch.setattr(at, "SHIPPED", shipped)
+    assert tuned_options((3, 3), 2, 4, lib=emu_lib) == CANDIDATES[4]
+    assert not (tmp_path / "empty.json").exists()  # nothing was tuned
