@@ -327,6 +327,14 @@ def run_ours(args, rank, world, local_rank):
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{ns} chains x 1 sweep ({wall:.1f} s), FP64 NumPy oracle restatement over {cores} processes"}
     clk = clocks.summary()
+    # the kernel runs on the FP32 CUDA cores: its fraction of their nominal FMA peak, at the SM clock
+    # sampled during the run (SMs x 128 FP32 lanes x 2 flops x clock)
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    fp32_peak = n_sm * 128 * 2 * mhz * 1e6 / 1e12 if mhz else None
+    roofline_fp32 = {"achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if achieved and fp32_peak else None,
+                     "peak_kind": f"nominal FP32 FMA: {n_sm} SMs x 128 lanes x 2 x {mhz} MHz"}
     line = {
         "metric": metric_name(w), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
@@ -338,6 +346,7 @@ def run_ours(args, rank, world, local_rank):
                    "l2": "inputs larger than L2 (bottom-env cache "
                          f"{eng.cache_bytes(n) / 1e9:.2f} GB read+written per step)"},
         "roofline": roofline,
+        "roofline_fp32": roofline_fp32,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 2 * args.steps,
