@@ -135,6 +135,32 @@ vmc_status vmc_peps_plan_set_operator(vmc_plan* plan,
                                       const int* diag_site_off, const int* diag_sites,
                                       const int* diag_value_off, const double* diag_values);
 
+/*
+ * Gauge-invariant PEPS for pure Z_N lattice gauge theory (phys_dim = 1):
+ * GIPEPS / GIPEPSConfig of src/vmc/peps/gi/model.py:41-119 with equal
+ * degeneracy per charge (bond dimension dmax per sector), and its kernels
+ * (src/vmc/peps/gi/kernels.py:17-126).  The plan is a standard plan whose
+ * "physical" index is a site's gauge configuration (its slice,
+ * model.py:308-347): phys_dim = the largest count N^(links - 1).  The site
+ * tensors are packed as (slice, up, down, left, right) per site, slices past a
+ * site's own count zero.  With a GI plan the calls above take:
+ *   configs[n][n_state] int32, n_state = R*C + R*(C-1) + (R-1)*C: the
+ *     flattened (sites, h links, v links) sample (model.py:121-144), sites 0;
+ *   uniforms[n][(R-1)*(C-1)] and deltas[n][(R-1)*(C-1)] (in [1, N), NULL for
+ *     N = 2): the per-plaquette accept draws and flip offsets of the
+ *     plaquette sweep (model.py:629-703, 901-957);
+ *   out_p: the slice index of every parameter (kernels.py:101-118);
+ *   out_E: link-diagonal plus plaquette energies (model.py:392-617).
+ * Slices per site are at most 8 (N = 2); larger N returns VMC_ERR_UNSUPPORTED.
+ * vmc_gi_set_operator: host FP64 arrays hdiag[R*(C-1)][N], vdiag[(R-1)*C][N]
+ * (energy of a link with value k: LinkDiagonalTerm, gi/local_terms.py:12-39)
+ * and plaq[(R-1)*(C-1)] (coefficient of P + P^dag, PlaquetteTerm).
+ */
+vmc_status vmc_gi_plan(const vmc_shape* shape, int N, int dmax, int chi, int dtype, int strategy,
+                       int n_sweeps, const vmc_plan_options* options, vmc_plan** out_plan);
+vmc_status vmc_gi_set_operator(vmc_plan* plan, const double* hdiag, const double* vdiag,
+                               const double* plaq);
+
 void vmc_plan_destroy(vmc_plan* plan);
 
 /* Number of parameters per sample of the sliced log-derivative (sum of

@@ -1,0 +1,108 @@
+"""The gauge-invariant engine path (GI plan: slices selected by links, plaquette sweeps, link-diagonal
+and plaquette energies) in the host-emulation build against the FP64 GI oracle."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import gi as ogi
+from oracle import peps as op
+from tests.helpers import assert_parity
+from vmc_gb300 import NoTruncation, ZipUp
+from vmc_gb300.gi import GIPEPS, GIPEPSConfig, build_gi_mc_kernels, z2_pure_gauge_hamiltonian
+
+CASES = [((3, 3), 2, None), ((3, 4), 2, 4), ((4, 4), 2, 6)]
+
+
+def _fp32(T):
+    return [[t.astype(np.float32).astype(np.float64) for t in row] for row in T]
+
+
+def _setup(emu_lib, shape, dmax, chi, seed, n):
+    ocfg = ogi.GIConfig(shape, 2, dmax)
+    T = _fp32(ogi.init_tensors(ocfg, seed=seed))
+    cfg = GIPEPSConfig(shape=shape, N=2, phys_dim=1, Qx=0, degeneracy_per_charge=(dmax, dmax))
+    model = GIPEPS(config=cfg, contraction_strategy=NoTruncation() if chi is None else ZipUp(chi), device="cpu",
+                   tensors=T, lib=emu_lib)
+    samples = ogi.random_physical_configuration(ocfg, n, seed=seed + 1)
+    strat = op.NoTruncation() if chi is None else op.ZipUp(chi)
+    return ocfg, T, model, samples, strat
+
+
+def _forward_top_envs(T, cfg, samples, strat):
+    _, h, v = ogi.unflatten_sample(samples, cfg.shape)
+    top = tuple(op._ones(samples.shape[0], 3, np.float64) for _ in range(cfg.shape[1]))
+    envs = []
+    for r in range(cfg.shape[0]):
+        envs.append(top)
+        top = strat.apply(top, ogi.row_mpo(T, cfg, h, v, r))
+    return envs
+
+
+@pytest.mark.parametrize("shape,dmax,chi", CASES)
+def test_amplitudes_gradients_energies(emu_lib, shape, dmax, chi):
+    ocfg, T, model, samples, strat = _setup(emu_lib, shape, dmax, chi, seed=3, n=6)
+    H = z2_pure_gauge_hamiltonian(shape, h=1.0, g=0.4)
+    OH = ogi.z2_pure_gauge_hamiltonian(shape, h=1.0, g=0.4)
+    eng = model.engine(H)
+    tens = model.packed()
+    c = torch.from_numpy(samples.astype(np.int32))
+    la, sg, O = eng.amp_grad(tens, c)
+    E = eng.local_energy(tens, c, la, sg)
+    amp_ref = ogi.amplitude(T, ocfg, samples, strat)
+    trunc = chi is not None
+    amp = (sg * torch.exp(la)).numpy()
+    assert_parity(np.abs(amp / amp_ref - 1), trunc)
+    grads, e_ref, _ = ogi.estimate(T, ocfg, samples, amp_ref, OH, strat, _forward_top_envs(T, ocfg, samples, strat))
+    o_ref, p_ref = ogi.local_log_derivatives(T, ocfg, samples, grads, amp_ref)
+    assert_parity(np.linalg.norm(O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), trunc)
+    assert_parity(np.abs(E.numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), trunc)
+    assert eng.status() == 0
+
+
+@pytest.mark.parametrize("shape,dmax,chi", CASES)
+def test_sweep_matches_oracle(emu_lib, shape, dmax, chi):
+    ocfg, T, model, samples, strat = _setup(emu_lib, shape, dmax, chi, seed=5, n=8)
+    R, C = shape
+    H = z2_pure_gauge_hamiltonian(shape, h=1.0, g=0.4)
+    OH = ogi.z2_pure_gauge_hamiltonian(shape, h=1.0, g=0.4)
+    u = np.random.default_rng(9).random((8, (R - 1) * (C - 1)))
+    init, trans, est = build_gi_mc_kernels(model, H)
+    c = torch.from_numpy(samples.astype(np.int32))
+    cache = init(model.tensors, c)
+    c2, _, ctx = trans(model.tensors, c, torch.from_numpy(u), cache)
+    _, le = est(model.tensors, c2, ctx)
+    ocache = ogi.init_cache(T, ocfg, samples, strat)
+    s2, amp_ref, tops, margin = ogi.transition(T, ocfg, samples, np.ones((8, R - 1, C - 1), dtype=np.int64),
+                                               u.reshape(8, R - 1, C - 1), ocache, strat)
+    same = np.all(c2.numpy() == s2, axis=1)
+    assert np.all(same | (margin < 1e-4)) and same.mean() > 0.7
+    grads, e_ref, _ = ogi.estimate(T, ocfg, s2, amp_ref, OH, strat, tops)
+    o_ref, p_ref = ogi.local_log_derivatives(T, ocfg, s2, grads, amp_ref)
+    trunc = chi is not None
+    amp = le.amp.numpy()
+    assert_parity(np.abs(amp[same] / amp_ref[same] - 1), trunc)
+    e = le.local_estimate.numpy()
+    assert_parity(np.abs(e[same] - e_ref[same]) / np.maximum(1.0, np.abs(e_ref[same])), trunc)
+    o = le.local_log_derivatives.numpy()
+    assert_parity(np.linalg.norm(o[same] - o_ref[same], axis=1) / np.linalg.norm(o_ref[same], axis=1), trunc)
+    assert np.array_equal(le.active_slice_indices.numpy()[same], p_ref[same])
+
+
+def test_full_gradient_in_the_reference_layout(emu_lib):
+    ocfg, T, model, samples, strat = _setup(emu_lib, (3, 3), 2, None, seed=7, n=4)
+    H = z2_pure_gauge_hamiltonian((3, 3))
+    init, trans, est = build_gi_mc_kernels(model, H, full_gradient=True)
+    c = torch.from_numpy(samples.astype(np.int32))
+    u = torch.ones((4, 4), dtype=torch.float64)  # u = 1 rejects every proposal: the sample stays
+    c2, _, ctx = trans(model.tensors, c, u, init(model.tensors, c))
+    _, le = est(model.tensors, c2, ctx)
+    assert np.array_equal(c2.numpy(), samples)
+    amp_ref = ogi.amplitude(T, ocfg, samples, strat)
+    grads, _, _ = ogi.estimate(T, ocfg, samples, amp_ref, ogi.GIHamiltonian((3, 3), ()), strat,
+                               _forward_top_envs(T, ocfg, samples, strat))
+    o_ref, _ = ogi.local_log_derivatives(T, ocfg, samples, grads, amp_ref, full_gradient=True)
+    o = le.local_log_derivatives.numpy()
+    assert o.shape == o_ref.shape
+    assert np.linalg.norm(o - o_ref) / np.linalg.norm(o_ref) < 1e-5

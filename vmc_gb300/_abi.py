@@ -62,6 +62,8 @@ SIGNATURES = {
     "vmc_status_string": (ct.c_char_p, [_I]),
     "vmc_peps_plan": (_I, [ct.POINTER(VmcShape), _I, _I, _I, _I, _I, _I, ct.POINTER(_P)]),
     "vmc_peps_plan_ex": (_I, [ct.POINTER(VmcShape), _I, _I, _I, _I, _I, _I, ct.POINTER(VmcPlanOptions), ct.POINTER(_P)]),
+    "vmc_gi_plan": (_I, [ct.POINTER(VmcShape), _I, _I, _I, _I, _I, _I, ct.POINTER(VmcPlanOptions), ct.POINTER(_P)]),
+    "vmc_gi_set_operator": (_I, [_P, _P, _P, _P]),
     "vmc_peps_plan_set_operator": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P]),
     "vmc_plan_destroy": (None, [_P]),
     "vmc_peps_n_params_sliced": (ct.c_int64, [_P]),

@@ -888,7 +888,7 @@ __device__ __noinline__ void vertical_energy(const DevPlan& P, const Slot& S, Sh
     const bool vt = P.vert_mask[r * C + c];
     const bool last = (c == C - 1);
     if (!vt && last) break;
-    double psi[kMaxD * kMaxD], psi_im[kMaxD * kMaxD];
+    double psi[kMaxPhys * kMaxPhys], psi_im[kMaxPhys * kMaxPhys];  // standard plans only: d <= kMaxPhys
     for (int i = 0; i < d * d; ++i) psi[i] = psi_im[i] = 0.0;
     const int s_cur = sp0[c];
     const int sz0 = ssize(P, s0), sz1 = ssize(P, s1);
@@ -1023,9 +1023,11 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
     // the 1-row environment GEMM intermediates are never live during a truncation
     for (int i = 0; i < 4; ++i) S.scr[3 + i] = dyn_smem + (size_t)i * P.scr1;
   }
-  float* vbuf[1 + 2 * kMaxD];
-  for (int i = 0; i < 1 + 2 * P.d; ++i)
+  // vertical-energy buffers (standard plans, d <= kMaxPhys); a GI plan uses the first two as scratch
+  float* vbuf[1 + 2 * kMaxPhys];
+  for (int i = 0; i < 1 + 2 * (P.d < kMaxPhys ? P.d : kMaxPhys); ++i)
     vbuf[i] = P.vert_in_smem ? dyn_smem + (size_t)i * P.vbuf : S.scr[7 + i];
+
   const int R = P.R, C = P.C;
   const int n_params = full_gradient ? P.d * P.np_sliced : P.np_sliced;
 
@@ -1171,6 +1173,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   __syncthreads();
   VMC_TSTOP(tchain, PH_CHAIN);}
 
+#ifndef VMC_GI_TU
 // The fused persistent kernel over the (job, chain) items of a job table
 // (uneven batches: lattices, bond dimensions, modes).  next == NULL: CTA b runs
 // items b, b + grid, ...  Otherwise CTAs take items from the counter *next
@@ -1197,3 +1200,28 @@ __global__ void __launch_bounds__(kThreads, VMC_MIN_CTAS) peps_kernel(const __gr
     run_chain(jobs.job[j], i - jobs.first[j], slot, status);
   }
 }
+#else  // the gauge-invariant translation unit
+
+#include "gi_device.cuh"
+
+// The gauge-invariant plans' kernel: the same job-table walk over gi_chain (a separate kernel, so the
+// standard chain code keeps its register allocation).  A job table holds GI plans only.
+__global__ void __launch_bounds__(kThreads, VMC_MIN_CTAS) gi_kernel(const __grid_constant__ BatchJobs jobs,
+                                                                     float* slots, int32_t* next, int32_t* status) {
+  VMC_SHARED int item;
+  float* slot = slots + (size_t)blockIdx.x * jobs.slot_floats;
+  const int total = jobs.first[jobs.n_jobs];
+  for (int i = blockIdx.x;; i += gridDim.x) {
+    if (next) {
+      if (threadIdx.x == 0) item = atomicAdd(next, 1);
+      __syncthreads();
+      i = item;
+      __syncthreads();
+    }
+    if (i >= total) break;
+    int j = 0;
+    while (j + 1 < jobs.n_jobs && i >= jobs.first[j + 1]) ++j;
+    gi_chain(jobs.job[j], i - jobs.first[j], slot, status);
+  }
+}
+#endif

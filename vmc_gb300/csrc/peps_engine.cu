@@ -38,6 +38,7 @@ struct HostOp {
   std::vector<int> onesite_mask, horiz_mask, vert_mask, row_has_h, row_has_v;
   std::vector<int> diag_nsites, diag_site_off, diag_sites, diag_value_off;
   std::vector<double> diag_values;
+  std::vector<double> gi_hdiag, gi_vdiag, gi_plaq;  // gauge-invariant plans
 };
 
 }  // namespace vmc
@@ -112,6 +113,9 @@ static vmc_status upload_plan(vmc_plan* pl) {
   const size_t o_ds = push(op.diag_sites.data(), op.diag_sites.size() * 4);
   const size_t o_dvo = push(op.diag_value_off.data(), op.diag_value_off.size() * 4);
   const size_t o_dv = push(op.diag_values.data(), op.diag_values.size() * 8);
+  const size_t o_gh = push(op.gi_hdiag.data(), op.gi_hdiag.size() * 8);
+  const size_t o_gv = push(op.gi_vdiag.data(), op.gi_vdiag.size() * 8);
+  const size_t o_gp = push(op.gi_plaq.data(), op.gi_plaq.size() * 8);
   const size_t o_plan = push(nullptr, sizeof(DevPlan));
   const size_t o_plan_g = push(nullptr, sizeof(DevPlan));
   if (pl->dbuf) vmc_free(pl->dbuf);
@@ -137,6 +141,9 @@ static vmc_status upload_plan(vmc_plan* pl) {
   P.diag_sites = reinterpret_cast<const int*>(base + o_ds);
   P.diag_value_off = reinterpret_cast<const int*>(base + o_dvo);
   P.diag_values = reinterpret_cast<const double*>(base + o_dv);
+  P.gi_hdiag = reinterpret_cast<const double*>(base + o_gh);
+  P.gi_vdiag = reinterpret_cast<const double*>(base + o_gv);
+  P.gi_plaq = reinterpret_cast<const double*>(base + o_gp);
   std::memcpy(blob.data() + o_plan, &P, sizeof(DevPlan));
   pl->dplan = reinterpret_cast<DevPlan*>(base + o_plan);
   {
@@ -159,6 +166,9 @@ static vmc_status upload_plan(vmc_plan* pl) {
   return VMC_OK;
 }
 
+// Sweeps of this plan need explicit flip offsets: d > 2 site flips, or Z_N plaquette flips with N > 2.
+static bool needs_deltas(const DevPlan& P) { return P.gi ? P.gi_N > 2 : P.d > 2; }
+
 static void default_operator(vmc_plan* pl) {
   DevPlan& P = pl->hp;
   HostOp& op = pl->op;
@@ -177,6 +187,10 @@ static void default_operator(vmc_plan* pl) {
   op.diag_value_off.assign(1, 0);
   op.diag_values.assign(1, 0.0);
   P.n_diag = 0;
+  const size_t N = P.gi ? (size_t)P.gi_N : 1;
+  op.gi_hdiag.assign(std::max(P.R * (P.C - 1), 1) * N, 0.0);
+  op.gi_vdiag.assign(std::max((P.R - 1) * P.C, 1) * N, 0.0);
+  op.gi_plaq.assign(std::max((P.R - 1) * (P.C - 1), 1), 0.0);
 }
 
 }  // namespace vmc
@@ -206,8 +220,36 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
   return vmc_peps_plan_ex(shape, bond_dim, chi, phys_dim, dtype, strategy, n_sweeps, nullptr, out_plan);
 }
 
+// A plan; gi_N > 0 makes it the gauge-invariant pure-Z_N-gauge plan whose "physical" index is a
+// site's gauge configuration (phys_dim = the largest number of configurations of a site).
+static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype, int strategy,
+                              int n_sweeps, const vmc_plan_options* opts, int gi_N, vmc_plan** out_plan);
+
 vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype, int strategy,
                             int n_sweeps, const vmc_plan_options* opts, vmc_plan** out_plan) {
+  return create_plan(shape, bond_dim, chi, phys_dim, dtype, strategy, n_sweeps, opts, 0, out_plan);
+}
+
+vmc_status vmc_gi_plan(const vmc_shape* shape, int N, int dmax, int chi, int dtype, int strategy, int n_sweeps,
+                       const vmc_plan_options* opts, vmc_plan** out_plan) {
+  if (!shape || !out_plan || N < 2 || dmax < 1) return VMC_ERR_INVALID;
+  const int R = shape->n_rows, C = shape->n_cols;
+  if (R < 2 || C < 2) return VMC_ERR_UNSUPPORTED;  // no plaquette to sweep
+  // configurations per site: N^(links - 1) (model.py:99-101); the plan's slices are the largest count
+  int slices = 1;
+  for (int r = 0; r < R; ++r)
+    for (int c = 0; c < C; ++c) {
+      const int links = (r > 0) + (r < R - 1) + (c > 0) + (c < C - 1);
+      int n = 1;
+      for (int k = 1; k < links; ++k) n *= N;
+      slices = std::max(slices, n);
+    }
+  if (slices > kMaxD) return VMC_ERR_UNSUPPORTED;
+  return create_plan(shape, dmax, chi, slices, dtype, strategy, n_sweeps, opts, N, out_plan);
+}
+
+static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype, int strategy,
+                              int n_sweeps, const vmc_plan_options* opts, int gi_N, vmc_plan** out_plan) {
   if (!shape || !out_plan) return VMC_ERR_INVALID;
   if (opts && (opts->threads != 0 && (opts->threads < 64 || opts->threads > kThreads || opts->threads % 32 != 0)))
     return VMC_ERR_INVALID;
@@ -215,7 +257,7 @@ vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int p
   *out_plan = nullptr;
   const int R = shape->n_rows, C = shape->n_cols;
   if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
-  if (phys_dim > kMaxD) return VMC_ERR_UNSUPPORTED;
+  if (phys_dim > (gi_N ? kMaxD : kMaxPhys)) return VMC_ERR_UNSUPPORTED;
   if (dtype != VMC_DTYPE_F32 && dtype != VMC_DTYPE_C64) return VMC_ERR_UNSUPPORTED;
   if (strategy < 0 || strategy > VMC_STRATEGY_VARIATIONAL || n_sweeps < 0) return VMC_ERR_INVALID;
   // DensityMatrix (strategy.py:153-176) carries V_k^H without the singular
@@ -229,6 +271,9 @@ vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int p
   P.R = R; P.C = C; P.D = bond_dim; P.d = phys_dim; P.chi = chi; P.strategy = strategy;
   P.es = dtype == VMC_DTYPE_C64 ? 2 : 1;
   P.n_sweeps = n_sweeps; P.n_sites = R * C;
+  P.gi = gi_N > 0;
+  P.gi_N = gi_N;
+  P.n_state = P.gi ? R * C + R * (C - 1) + (R - 1) * C : R * C;
   const int D = bond_dim, d = phys_dim;
   pl->sdim.resize(4 * R * C);
   pl->site_off.resize(R * C);
@@ -372,7 +417,7 @@ vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int p
       // VMC_VERT_SMEM=1 puts them in the shared-memory arena, chunked.
       Q.vert_in_smem = 0;
       if (const char* vs = std::getenv("VMC_VERT_SMEM"))
-        if (std::atoi(vs) != 0 && Q.arena_in_smem && nbuf * Q.vbuf * 4 <= budget) Q.vert_in_smem = 1;
+        if (std::atoi(vs) != 0 && !Q.gi && Q.arena_in_smem && nbuf * Q.vbuf * 4 <= budget) Q.vert_in_smem = 1;
     }
     Q.onerow_in_smem = 0;
     if (Q.arena_in_smem && std::max(Q.arena_floats, 4LL * Q.scr1) * 4 <= budget) {
@@ -386,7 +431,7 @@ vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int p
       Q.vbuf = (int)SCR;
     }
     Q.TS = (int)TS; Q.ES = (int)ES; Q.E2S = (int)E2S; Q.MM = (int)MM; Q.SCR = (int)SCR;
-    Q.n_scr = 11 + 2 * kMaxD;
+    Q.n_scr = 11 + 2 * kMaxPhys;
     Q.VS = strategy == VMC_STRATEGY_VARIATIONAL ? (int)(es * chimax * D * chimax) : 0;
     Q.slot_floats = al64((long long)(R + 1) * C * TS) + al64(2 * (R + 2)) + al64(2LL * d * C) + al64(2LL * C) +
                     3 * al64((long long)C * TS) +
@@ -477,6 +522,19 @@ vmc_status vmc_peps_plan_set_operator(vmc_plan* pl, const double* onesite, const
   return upload_plan(pl);
 }
 
+vmc_status vmc_gi_set_operator(vmc_plan* pl, const double* hdiag, const double* vdiag, const double* plaq) {
+  if (!pl || !pl->hp.gi) return VMC_ERR_INVALID;
+  const DevPlan& P = pl->hp;
+  HostOp& op = pl->op;
+  default_operator(pl);
+  const size_t N = (size_t)P.gi_N;
+  if (hdiag) op.gi_hdiag.assign(hdiag, hdiag + (size_t)P.R * (P.C - 1) * N);
+  if (vdiag) op.gi_vdiag.assign(vdiag, vdiag + (size_t)(P.R - 1) * P.C * N);
+  if (plaq) op.gi_plaq.assign(plaq, plaq + (size_t)(P.R - 1) * (P.C - 1));
+  pl->op_set = true;
+  return upload_plan(pl);
+}
+
 void vmc_plan_destroy(vmc_plan* pl) {
   if (!pl) return;
   if (pl->dbuf) vmc_free(pl->dbuf);
@@ -555,7 +613,7 @@ vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors
                           double* out_sign, float* out_margin, float* out_gap, void* workspace,
                           size_t workspace_bytes, int32_t* status_dev) {
   if (!pl || !uniforms || !cache_inout || !out_E || !out_logamp || !out_sign) return VMC_ERR_INVALID;
-  if (pl->hp.d > 2 && !deltas) return VMC_ERR_INVALID;
+  if (needs_deltas(pl->hp) && !deltas) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_SWEEP, tensors, configs_inout, uniforms, deltas, n_chains, cache_inout,
                 full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, out_gap, workspace,
                 workspace_bytes, status_dev);
@@ -579,7 +637,7 @@ vmc_status vmc_peps_sweep_recompute(const vmc_plan* pl, void* stream, const floa
   if (!pl || !tensors || !configs_inout || !uniforms || !out_E || !out_logamp || !out_sign || n_chains < 0 ||
       !workspace || !status_dev)
     return VMC_ERR_INVALID;
-  if (pl->hp.d > 2 && !deltas) return VMC_ERR_INVALID;
+  if (needs_deltas(pl->hp) && !deltas) return VMC_ERR_INVALID;
   if (n_chains == 0) return VMC_OK;
   if (workspace_bytes < vmc_sweep_recompute_workspace_size(pl, n_chains)) return VMC_ERR_WORKSPACE;
   const int grid = n_slots(pl, n_chains);
@@ -674,6 +732,7 @@ struct BatchLayout {
   size_t slots_off = 0;  // floats
   int grid = 0, threads = 0, es = 0, total = 0;
   int slot_layout = 0;  // 1: every plan with its no-shared-memory buffer placement
+  const KernelSet* K = nullptr;  // one fused kernel for the whole table (standard or GI, one element type)
   size_t smem = 0, bytes = 0;
 };
 
@@ -684,7 +743,7 @@ static bool job_valid(const vmc_peps_job& j) {
   switch (j.kind) {
     case VMC_JOB_INIT_CACHE: return j.cache != nullptr;
     case VMC_JOB_SWEEP:  // no cache: the sweep recomputes the bottom environments
-      return j.uniforms && j.out_E && j.logamp && j.sign && (j.plan->hp.d <= 2 || j.deltas);
+      return j.uniforms && j.out_E && j.logamp && j.sign && (!needs_deltas(j.plan->hp) || j.deltas);
     case VMC_JOB_AMP_GRAD: return j.logamp && j.sign;
     case VMC_JOB_LOCAL_ENERGY: return j.logamp && j.sign && j.out_E;
     default: return false;
@@ -716,7 +775,8 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout
     if (L->threads == 0) {
       L->threads = P.threads;
       L->es = P.es;
-    } else if (P.threads != L->threads || P.es != L->es) {
+      L->K = &kernels_of(P);
+    } else if (P.threads != L->threads || P.es != L->es || &kernels_of(P) != L->K) {
       return VMC_ERR_UNSUPPORTED;
     }
     L->perm_off[i] = off;
@@ -733,8 +793,7 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout
   L->slots_off = off;
   int per_sm = 4;
   if (L->n > 0) {
-    const KernelSet& K = L->es == 2 ? ck::kernels() : rk::kernels();
-    if (K.prepare(L->threads, L->smem, &per_sm) != cudaSuccess) return VMC_ERR_CUDA;
+    if (L->K->prepare(L->threads, L->smem, &per_sm) != cudaSuccess) return VMC_ERR_CUDA;
     if (per_sm < 1) return VMC_ERR_UNSUPPORTED;
   }
   L->grid = (int)std::min<long long>(total, (long long)vmc_num_sms() * per_sm);
@@ -753,7 +812,7 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout
 static vmc_status launch_batch(const vmc_peps_job* jobs, const BatchLayout& L, void* stream, float* wsf,
                                int32_t* status) {
   static const int kMode[4] = {MODE_INIT, MODE_SWEEP, MODE_AMPGRAD, MODE_ENERGY};
-  const KernelSet& K = L.es == 2 ? ck::kernels() : rk::kernels();
+  const KernelSet& K = *L.K;
   BatchJobs bj;
   std::memset(&bj, 0, sizeof(bj));
   bj.n_jobs = L.n;
@@ -764,7 +823,8 @@ static vmc_status launch_batch(const vmc_peps_job* jobs, const BatchLayout& L, v
     const int kind = j.kind;
     const bool sweep = kind == VMC_JOB_SWEEP, grad = sweep || kind == VMC_JOB_AMP_GRAD;
     bj.job[k] = chain_job(j.plan, kMode[kind], j.tensors, wsf + L.perm_off[L.order[k]], j.configs,
-                          sweep ? j.uniforms : nullptr, sweep && j.plan->hp.d > 2 ? j.deltas : nullptr, j.n_chains,
+                          sweep ? j.uniforms : nullptr, sweep && needs_deltas(j.plan->hp) ? j.deltas : nullptr,
+                          j.n_chains,
                           sweep && L.entry_off[L.order[k]] ? static_cast<void*>(wsf + L.entry_off[L.order[k]])
                           : (sweep || kind == VMC_JOB_INIT_CACHE) ? j.cache : nullptr,
                           j.full_gradient,

@@ -8,10 +8,17 @@ static cudaError_t launch_permute(const DevPlan* dplan, int n_sites, const float
   return vmc_last_error();
 }
 
+#ifdef VMC_GI_TU
+#define VMC_FUSED_KERNEL gi_kernel
+#else
+#define VMC_FUSED_KERNEL peps_kernel
+#endif
+
 static cudaError_t opt_in_smem(size_t smem) {
 #ifndef VMC_HOST_EMULATION
   // static (~5 KB) + dynamic shared memory may exceed the 48 KB default: always opt in
-  if (smem > 0) return cudaFuncSetAttribute(peps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 0)
+    return cudaFuncSetAttribute(VMC_FUSED_KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 #endif
   (void)smem;
   return cudaSuccess;
@@ -25,7 +32,7 @@ static cudaError_t prepare_peps(int threads, size_t smem, int* per_sm) {
   *per_sm = 4;
   return cudaSuccess;
 #else
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, peps_kernel, threads, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, VMC_FUSED_KERNEL, threads, smem);
 #endif
 }
 
@@ -33,7 +40,7 @@ static cudaError_t launch_peps(const BatchJobs& jobs, int grid, int threads, siz
                                float* slots, int32_t* next, int32_t* status) {
   const cudaError_t e = opt_in_smem(smem);
   if (e != cudaSuccess) return e;
-  VMC_LAUNCH(peps_kernel, grid, threads, smem, stream, jobs, slots, next, status);
+  VMC_LAUNCH(VMC_FUSED_KERNEL, grid, threads, smem, stream, jobs, slots, next, status);
   return vmc_last_error();
 }
 
@@ -41,3 +48,5 @@ const KernelSet& kernels() {
   static const KernelSet k{&launch_permute, &prepare_peps, &launch_peps};
   return k;
 }
+
+#undef VMC_FUSED_KERNEL

@@ -30,7 +30,8 @@ constexpr int kThreads = VMC_MAX_THREADS;
 constexpr int kDefaultThreads = 128;  // one chain per 4 warps: more chains resident per SM
 constexpr int kMaxVec = 512;   // max vectors in one truncation (chi * D)
 constexpr int kMaxCols = 64;   // max lattice columns
-constexpr int kMaxD = 4;       // max physical dimension
+constexpr int kMaxD = 8;       // max slices per site: physical dimension (<= 4), or gauge configurations
+constexpr int kMaxPhys = 4;    // max physical dimension of a standard plan (its energy paths size d x d)
 constexpr int kPermKinds = 6;  // permuted copies of every site tensor
 constexpr float kJacobiTol = 5e-7f;  // stop when every |a_p.a_q| <= tol |a_p||a_q|
 constexpr int kJacobiSweeps = 16;
@@ -85,6 +86,12 @@ struct DevPlan {
   const int* diag_sites;
   const int* diag_value_off;
   const double* diag_values;
+  // gauge-invariant PEPS (pure Z_N gauge, gi != 0): the "physical" index of a site is its gauge
+  // configuration (slice), selected by the link values; a chain's state is (sites, h links, v links)
+  int gi, gi_N, n_state;          // n_state: ints per chain (n_sites for a standard plan)
+  const double* gi_hdiag;         // [R*(C-1)][N] energy of a horizontal link with value k
+  const double* gi_vdiag;         // [(R-1)*C][N] energy of a vertical link with value k
+  const double* gi_plaq;          // [(R-1)*(C-1)] plaquette coefficient (P + P^dag)
 };
 
 struct Slot {
@@ -99,7 +106,7 @@ struct Slot {
   float* l2[2];  // E2S
   float* arena;  // truncation arena when it does not fit shared memory
   float* venv;   // Variational: left envs C*VS, then right envs C*VS
-  float* scr[24];
+  float* scr[11 + 2 * kMaxPhys + 5];  // n_scr = 11 + 2 kMaxPhys buffers (GI plans use the first 12)
 };
 
 __host__ __device__ inline long long al64(long long n) { return (n + 63) & ~63LL; }
@@ -192,6 +199,11 @@ struct KernelSet {
 };
 namespace rk { const KernelSet& kernels(); }  // real FP32 elements
 namespace ck { const KernelSet& kernels(); }  // complex64 elements
-inline const KernelSet& kernels_of(const DevPlan& P) { return P.es == 2 ? ck::kernels() : rk::kernels(); }
+namespace gr { const KernelSet& kernels(); }  // gauge-invariant plans, real FP32
+namespace gc { const KernelSet& kernels(); }  // gauge-invariant plans, complex64
+inline const KernelSet& kernels_of(const DevPlan& P) {
+  if (P.gi) return P.es == 2 ? gc::kernels() : gr::kernels();
+  return P.es == 2 ? ck::kernels() : rk::kernels();
+}
 
 }  // namespace vmc

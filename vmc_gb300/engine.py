@@ -88,18 +88,17 @@ class PEPSEngine:
                                     device=self.device, lib=lib)
         self.options = None if options is None else dict(options)
         dt = _abi.VMC_DTYPE_C64 if self.complex else _abi.VMC_DTYPE_F32
+        o = None if options is None else _abi.VmcPlanOptions(
+            int(options.get("threads", 0)), int(options.get("smem_kb", -1)), int(options.get("tile_policy", 0)))
         with torch.cuda.device(self.device) if self.device.type == "cuda" else _null():
-            if options is None:
-                st = lib.vmc_peps_plan(ct.byref(_abi.VmcShape(*self.shape)), self.bond_dim, self.chi,
-                                       self.phys_dim, dt, sid, int(n_sweeps), ct.byref(plan))
-            else:
-                o = _abi.VmcPlanOptions(int(options.get("threads", 0)), int(options.get("smem_kb", -1)),
-                                        int(options.get("tile_policy", 0)))
-                st = lib.vmc_peps_plan_ex(ct.byref(_abi.VmcShape(*self.shape)), self.bond_dim, self.chi,
-                                          self.phys_dim, dt, sid, int(n_sweeps), ct.byref(o), ct.byref(plan))
+            st = self._make_plan(lib, _abi.VmcShape(*self.shape), dt, sid, int(n_sweeps), o, plan)
         _abi.check(lib, st, "vmc_peps_plan")
         self.resident_chains = int(lib.vmc_plan_resident_ctas(plan))
         self._plan = plan
+        # ints of state per chain, accept draws per chain (and flip offsets, if needed) per sweep
+        self.n_state = self.n_sites
+        self.n_draws = self.n_sites
+        self.needs_deltas = self.phys_dim > 2
         self.n_params_sliced = int(lib.vmc_peps_n_params_sliced(plan))
         self.n_params_full = int(lib.vmc_peps_n_params_full(plan))
         self._ws = None
@@ -107,6 +106,13 @@ class PEPSEngine:
         self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
         if operator is not None:
             self.set_operator(operator)
+
+    def _make_plan(self, lib, shape, dt, sid, n_sweeps, options, plan):
+        if options is None:
+            return lib.vmc_peps_plan(ct.byref(shape), self.bond_dim, self.chi, self.phys_dim, dt, sid, n_sweeps,
+                                     ct.byref(plan))
+        return lib.vmc_peps_plan_ex(ct.byref(shape), self.bond_dim, self.chi, self.phys_dim, dt, sid, n_sweeps,
+                                    ct.byref(options), ct.byref(plan))
 
     def __del__(self):
         plan = getattr(self, "_plan", None)
@@ -154,9 +160,9 @@ class PEPSEngine:
             raise ValueError(f"expected {self.n_params_full} packed parameters, got {tensors.numel()}")
 
     def _configs(self, configs):
-        c = configs.reshape(-1, self.n_sites)
+        c = configs.reshape(-1, self.n_state)
         if c.dtype != torch.int32 or c.device != self.device or not c.is_contiguous():
-            raise ValueError("configs must be a contiguous int32 (n, n_sites) tensor on the engine device")
+            raise ValueError("configs must be a contiguous int32 (n, n_state) tensor on the engine device")
         return c
 
     def status(self, reset=True) -> int:
@@ -204,13 +210,13 @@ class PEPSEngine:
         self._check_tensors(tensors)
         c = self._configs(configs)
         n = c.shape[0]
-        u = uniforms.reshape(n, self.n_sites)
+        u = uniforms.reshape(n, self.n_draws)
         if u.dtype != torch.float64 or u.device != self.device or not u.is_contiguous():
-            raise ValueError("uniforms must be a contiguous float64 (n, n_sites) tensor on the engine device")
-        if self.phys_dim > 2:
+            raise ValueError("uniforms must be a contiguous float64 (n, n_draws) tensor on the engine device")
+        if self.needs_deltas:
             if deltas is None:
-                raise ValueError("d > 2 needs explicit flip offsets (deltas)")
-            deltas = deltas.reshape(n, self.n_sites).to(torch.int32).contiguous()
+                raise ValueError("this plan needs explicit flip offsets (deltas)")
+            deltas = deltas.reshape(n, self.n_draws).to(torch.int32).contiguous()
         else:
             deltas = None
         np_ = self.n_params_full if full_gradient else self.n_params_sliced

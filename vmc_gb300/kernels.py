@@ -55,7 +55,12 @@ def _uniforms(key, n, n_sites, device):
 
 
 def build_mc_kernels(model, operator, *, full_gradient: bool = False):
-    """kernels.py:91-247 for the standard PEPS on the GB300 engine."""
+    """kernels.py:91-247 for the standard PEPS on the GB300 engine; a GIPEPS model gets the
+    gauge-invariant kernels (src/vmc/peps/gi/kernels.py:17-126, dispatched on the model type there)."""
+    from .gi import GIPEPS, build_gi_mc_kernels
+
+    if isinstance(model, GIPEPS):
+        return build_gi_mc_kernels(model, operator, full_gradient=full_gradient)
     engine = model.engine(operator)
     n_sites = model.shape[0] * model.shape[1]
     d = model.phys_dim
