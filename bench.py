@@ -147,7 +147,7 @@ def run_reference(args, rank, world):
 
     if rank != 0:
         return
-    if args.workload == "uneven":
+    if args.workload in ("uneven", "gi9x9"):
         raise SystemExit("--impl reference times single-lattice workloads; the uneven batch reports each "
                          "lattice's own rate in per_shape")
     w = WORKLOADS[args.workload]
@@ -506,6 +506,94 @@ def run_uneven(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_gi(args, rank, world, local_rank):
+    """--workload gi9x9: the gauge-invariant PEPS of pure Z2 lattice gauge theory on 9x9 vertices
+    (8x8 plaquettes), 2 states per charge sector, chi=32, --chains chains (default 4096).  H of the
+    lattice-gauge workload, -g sum sigma^x - (1/g) sum prod sigma^z with g = 0.8, written in the
+    electric basis the GI model samples: g/2 (2 - 2 (-1)^E) per link (the same up to a constant) and
+    -1/(2g) (P + P^dag) per plaquette.  value: plaquette sweep + O_k + E_loc samples/s, inputs on the
+    device; e2e: the public kernels (build_mc_kernels) with host uniforms in and E/log|psi|/sign out."""
+    import torch
+
+    from vmc_gb300 import ZipUp
+    from vmc_gb300.gi import GIPEPS, GIPEPSConfig, build_gi_mc_kernels, z2_pure_gauge_hamiltonian
+
+    n = args.chains or 4096
+    g = 0.8
+    shape, dmax, chi = (9, 9), 2, 32
+    dev = torch.device(f"cuda:{local_rank}")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    cfg = GIPEPSConfig(shape=shape, N=2, phys_dim=1, Qx=0, degeneracy_per_charge=(dmax, dmax))
+    model = GIPEPS(rngs=0, config=cfg, contraction_strategy=ZipUp(chi), device=dev)
+    H = z2_pure_gauge_hamiltonian(shape, h=1.0 / (2.0 * g), g=g / 2.0)
+    eng = model.engine(H)
+    tens = model.packed()
+    n_plaq = (shape[0] - 1) * (shape[1] - 1)
+    total = args.warmup + args.steps
+    gen = torch.Generator(device=dev).manual_seed(1000 * rank + 11)
+    uni = torch.rand((total, n, n_plaq), generator=gen, dtype=torch.float64, device=dev)
+    cfg0 = model.random_physical_configuration(rank, n)
+    c = cfg0.clone()
+    cache = eng.init_cache(tens, c)
+    out = None
+    for i in range(args.warmup):
+        out = eng.sweep(tens, c, uni[i], cache, out=out)
+    torch.cuda.synchronize()
+    eng.raise_on_status()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        a.record(stream)
+        for i in range(args.steps):
+            out = eng.sweep(tens, c, uni[args.warmup + i], cache, out=out)
+        b.record(stream)
+        torch.cuda.synchronize()
+    eng.raise_on_status()
+    t = a.elapsed_time(b) / 1e3 / args.steps
+    # end to end through the public kernels, host buffers
+    init, trans, est = build_gi_mc_kernels(model, H)
+    c = cfg0.clone()
+    kcache = init(model.tensors, c)
+    host_u = [uni[i].cpu().pin_memory() for i in range(total)]
+    host = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(3)]
+
+    def step(i, c, kcache):
+        u = host_u[i].to(dev, non_blocking=True)
+        c, _, ctx = trans(model.tensors, c, u, kcache)
+        kcache, le = est(model.tensors, c, ctx)
+        for h_, src in zip(host, (le.local_estimate, le.log_amp, le.sign)):
+            h_.copy_(src, non_blocking=True)
+        return c, kcache
+
+    for i in range(args.warmup):
+        c, kcache = step(i, c, kcache)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for i in range(args.steps):
+        c, kcache = step(args.warmup + i, c, kcache)
+    b.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = a.elapsed_time(b) / 1e3 / args.steps
+    line = {
+        "metric": "GI-PEPS samples/s (plaquette sweep + grad log psi + E_loc), pure Z2 gauge 9x9, D=2/sector, chi=32",
+        "value": n / t, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "gi9x9", "vertices": list(shape), "degeneracy_per_charge": [dmax, dmax], "chi": chi,
+                   "N": 2, "g": g, "model": "pure Z2 lattice gauge theory", "chains_per_gpu": n,
+                   "parallelism": "replicas x1",
+                   "l2": f"inputs larger than L2 (bottom-env cache {eng.cache_bytes(n) / 1e9:.2f} GB)"},
+        "roofline": {"bound": "tensor", "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None,
+                     "traffic": None, "note": "no algorithmic FLOP count exists for the GI path"},
+        "cpu_baseline": None,
+        "e2e": {"value": n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n * n_plaq * 8, "d2h_bytes_per_step": 3 * n * 8},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -533,6 +621,8 @@ def main():
     try:
         if args.workload == "uneven":
             run_uneven(args, rank, world, local_rank)
+        elif args.workload == "gi9x9":
+            run_gi(args, rank, world, local_rank)
         else:
             run_ours(args, rank, world, local_rank)
     finally:

@@ -73,6 +73,8 @@ class PEPSEngine:
             self.device = torch.device(device if device is not None else "cuda")
             if self.device.type != "cuda":
                 raise EngineUnavailable("vmc_gb300 engine tensors must live on a CUDA device")
+            if self.device.index is None:  # tensors report their index: compare like with like
+                self.device = torch.device("cuda", torch.cuda.current_device())
         else:
             self.device = torch.device(device if device is not None else "cpu")
         self.lib = lib

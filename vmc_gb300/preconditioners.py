@@ -104,10 +104,19 @@ def _qr_solve(jac: Jacobian, dv, rcond, min_norm, lib=None):
     # matrix_rank(r): R's singular values are those of the k x k triangle of a QR of R^H (no
     # squaring, unlike R R^H), so the SVD runs on k x k instead of k x n
     rt = torch.linalg.qr(r.mH, mode="r")[1] if r.shape[1] > r.shape[0] else r
-    sv = torch.linalg.svdvals(rt)
     eps = torch.finfo(torch.float64).eps
+    rtol = max(r.shape) * eps if rcond is None else rcond
+    if rt.is_cuda and rt.numel():
+        # cuSOLVER's gesvda is 6-8x faster than gesvd here and agrees with it to ~1e-12 sigma_max;
+        # when a singular value lies within 10x of the threshold the rank is taken from gesvd
+        sv = torch.linalg.svd(rt, full_matrices=False, driver="gesvda")[1]
+        tol = rtol * sv.max()
+        if bool(((sv > tol / 10) & (sv < tol * 10)).any()):
+            sv = torch.linalg.svd(rt, full_matrices=False, driver="gesvd")[1]
+    else:
+        sv = torch.linalg.svdvals(rt)
     smax = sv.max() if sv.numel() else torch.zeros((), dtype=torch.float64, device=o.device)
-    tol = (max(r.shape) * eps if rcond is None else rcond) * smax
+    tol = rtol * smax
     rank = int((sv > tol).sum())  # the reference's int(matrix_rank(r)) also reads it on the host
     n_red = r.shape[1]
     n2 = n_red - rank
