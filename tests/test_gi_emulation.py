@@ -106,3 +106,36 @@ def test_full_gradient_in_the_reference_layout(emu_lib):
     o = le.local_log_derivatives.numpy()
     assert o.shape == o_ref.shape
     assert np.linalg.norm(o - o_ref) / np.linalg.norm(o_ref) < 1e-5
+
+
+def test_complex_gi_matches_oracle(emu_lib):
+    shape, dmax, chi = (3, 4), 2, 4
+    ocfg = ogi.GIConfig(shape, 2, dmax)
+    T = [[t.astype(np.complex64).astype(np.complex128) for t in row]
+         for row in ogi.init_tensors(ocfg, seed=11, dtype=np.complex128)]
+    cfg = GIPEPSConfig(shape=shape, N=2, phys_dim=1, Qx=0, degeneracy_per_charge=(dmax, dmax), dtype=torch.complex64)
+    model = GIPEPS(config=cfg, contraction_strategy=ZipUp(chi), device="cpu", tensors=T, lib=emu_lib)
+    H = z2_pure_gauge_hamiltonian(shape, h=1.0, g=0.4)
+    eng = model.engine(H)
+    samples = ogi.random_physical_configuration(ocfg, 6, seed=12)
+    c = torch.from_numpy(samples.astype(np.int32))
+    la, ph, O = eng.amp_grad(model.packed(), c)
+    E = eng.local_energy(model.packed(), c, la, ph)
+    strat = op.ZipUp(chi)
+    amp_ref = ogi.amplitude(T, ocfg, samples, strat)
+    assert_parity(np.abs(np.exp(la.numpy() + 1j * ph.numpy()) / amp_ref - 1), True)
+    grads, e_ref, _ = ogi.estimate(T, ocfg, samples, amp_ref, ogi.z2_pure_gauge_hamiltonian(shape, h=1.0, g=0.4),
+                                   strat, _forward_top_envs_c(T, ocfg, samples, strat))
+    o_ref, _ = ogi.local_log_derivatives(T, ocfg, samples, grads, amp_ref)
+    assert_parity(np.linalg.norm(O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
+    assert_parity(np.abs(E.numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
+
+
+def _forward_top_envs_c(T, cfg, samples, strat):
+    _, h, v = ogi.unflatten_sample(samples, cfg.shape)
+    top = tuple(op._ones(samples.shape[0], 3, np.complex128) for _ in range(cfg.shape[1]))
+    envs = []
+    for r in range(cfg.shape[0]):
+        envs.append(top)
+        top = strat.apply(top, ogi.row_mpo(T, cfg, h, v, r))
+    return envs
