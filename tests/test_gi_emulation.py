@@ -139,3 +139,25 @@ def _forward_top_envs_c(T, cfg, samples, strat):
         envs.append(top)
         top = strat.apply(top, ogi.row_mpo(T, cfg, h, v, r))
     return envs
+
+
+def test_tdvp_on_a_gi_model_with_full_gradients(emu_lib):
+    """The reference's lattice-gauge drivers run TDVPDriver(full_gradient=True) on a GIPEPS
+    (examples/lgt/z2_pure_gauge.py:79-95): the same on the engine, imaginary time."""
+    from vmc_gb300.drivers import ImaginaryTimeUnit, TDVPDriver
+    from vmc_gb300.preconditioners import SRPreconditioner
+    from vmc_gb300.qgt import SampleSpace
+
+    shape = (3, 3)
+    cfg = GIPEPSConfig(shape=shape, N=2, phys_dim=1, Qx=0, degeneracy_per_charge=(2, 2))
+    model = GIPEPS(rngs=1, config=cfg, contraction_strategy=ZipUp(4), device="cpu", lib=emu_lib)
+    H = z2_pure_gauge_hamiltonian(shape, h=1.0, g=0.4)
+    drv = TDVPDriver(model, H, preconditioner=SRPreconditioner(space=SampleSpace(), diag_shift=0.1), dt=0.05,
+                     time_unit=ImaginaryTimeUnit(), n_samples=64, n_chains=32, full_gradient=True)
+    t0 = [[t.clone() for t in row] for row in model.tensors]
+    drv.run(0.1)
+    assert drv.step_count == 2 and np.isfinite(drv.energy["mean"])
+    assert any(not torch.equal(a, b) for ra, rb in zip(t0, drv._tensors) for a, b in zip(ra, rb))
+    with pytest.raises(NotImplementedError):
+        TDVPDriver(model, H, preconditioner=SRPreconditioner(space=SampleSpace()), dt=0.05,
+                   time_unit=ImaginaryTimeUnit(), n_samples=8, n_chains=8).run(0.05)

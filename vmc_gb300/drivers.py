@@ -108,8 +108,11 @@ class TDVPDriver:
         self._gen = torch.Generator(device=dev)
         self._gen.manual_seed(int(sampler_key))
         self._tensors = [[t.clone() for t in row] for row in model.tensors]
-        self._sampler_configuration = torch.randint(0, model.phys_dim, (self.n_chains,) + model.shape,
-                                                    generator=self._gen, device=dev, dtype=torch.int32)
+        if hasattr(model, "gi_config_states"):  # a gauge-invariant PEPS: Gauss-law configurations
+            self._sampler_configuration = model.gi_config_states(self._gen, self.n_chains)
+        else:
+            self._sampler_configuration = torch.randint(0, model.phys_dim, (self.n_chains,) + model.shape,
+                                                        generator=self._gen, device=dev, dtype=torch.int32)
         init_cache, transition, estimate = build_mc_kernels(model, operator, full_gradient=self.full_gradient)
         self._init_cache = init_cache
         self._mc_sampler = make_mc_sampler(transition, estimate)

@@ -192,6 +192,21 @@ class GIPEPS:
                 parts.append(pad.reshape(-1))
         return torch.cat(parts).contiguous()
 
+    @property
+    def n_params(self) -> int:
+        return sum(t.numel() for row in self.tensors for t in row)
+
+    def unpack(self, flat: torch.Tensor):
+        """A flat vector in the reference's parameter order -> per-site (1, nc, ...) tensors."""
+        out, off = [], 0
+        for row in self.tensors:
+            r = []
+            for t in row:
+                r.append(flat[off:off + t.numel()].reshape(t.shape))
+                off += t.numel()
+            out.append(r)
+        return out
+
     def full_gradient(self, o_full: torch.Tensor):
         """The engine's full gradient (per site slices x params) in the reference's layout
         (concatenated (1, nc, ...) per site, gi/kernels.py:80-93)."""
@@ -227,6 +242,11 @@ class GIPEPS:
         R, C = shape
         ns, nh = R * C, R * (C - 1)
         return (sample[:ns].reshape(R, C), sample[ns:ns + nh].reshape(R, C - 1), sample[ns + nh:].reshape(R - 1, C))
+
+    def gi_config_states(self, gen: torch.Generator, n: int) -> torch.Tensor:
+        """Initial chains for a driver: random plaquette charges from the driver's generator."""
+        seed = int(torch.randint(0, 2 ** 31 - 1, (1,), generator=gen, device=gen.device).item())
+        return self.random_physical_configuration(seed, n)
 
     def random_physical_configuration(self, key=0, n_samples=1):
         """model.py:146-189 for pure gauge: random plaquette charges on the zero configuration."""

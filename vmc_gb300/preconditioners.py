@@ -179,6 +179,9 @@ class SRPreconditioner:
             dv = dv.to(torch.complex128) * grad_factor
         else:
             dv = dv * float(getattr(grad_factor, "real", grad_factor))
+        if p is not None and hasattr(model, "N"):
+            raise NotImplementedError("the sliced SR solve of a gauge-invariant PEPS is not implemented: "
+                                      "use full_gradient=True (as the reference's lattice-gauge drivers do)")
         pps = tuple(params_per_site(model.shape, model.bond_dim))
         sd = (model.phys_dim,) * (model.shape[0] * model.shape[1])
         jac = Jacobian(o) if p is None else SlicedJacobian(o, p, sd, self.ordering)
