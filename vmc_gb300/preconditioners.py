@@ -107,12 +107,10 @@ def _qr_solve(jac: Jacobian, dv, rcond, min_norm, lib=None):
     eps = torch.finfo(torch.float64).eps
     rtol = max(r.shape) * eps if rcond is None else rcond
     if rt.is_cuda and rt.numel():
-        # cuSOLVER's gesvda is 6-8x faster than gesvd here and agrees with it to ~1e-12 sigma_max;
-        # when a singular value lies within 10x of the threshold the rank is taken from gesvd
-        sv = torch.linalg.svd(rt, full_matrices=False, driver="gesvda")[1]
-        tol = rtol * sv.max()
-        if bool(((sv > tol / 10) & (sv < tol * 10)).any()):
-            sv = torch.linalg.svd(rt, full_matrices=False, driver="gesvd")[1]
+        # cuSOLVER's QR-iteration SVD (gesvd): robust on the rank-deficient triangles that repeated
+        # samples produce, and faster here than svdvals' default driver (8.8 s against 12.1 s at
+        # 4096 x 4096); the approximate gesvda does not converge on them
+        sv = torch.linalg.svd(rt, full_matrices=False, driver="gesvd")[1]
     else:
         sv = torch.linalg.svdvals(rt)
     smax = sv.max() if sv.numel() else torch.zeros((), dtype=torch.float64, device=o.device)
