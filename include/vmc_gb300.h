@@ -151,7 +151,7 @@ vmc_status vmc_peps_plan_set_operator(vmc_plan* plan,
  *     plaquette sweep (model.py:629-703, 901-957);
  *   out_p: the slice index of every parameter (kernels.py:101-118);
  *   out_E: link-diagonal plus plaquette energies (model.py:392-617).
- * Slices per site are at most 8 (N = 2); larger N returns VMC_ERR_UNSUPPORTED.
+ * Slices per site are at most 27 (N <= 3); larger N returns VMC_ERR_UNSUPPORTED.
  * vmc_gi_set_operator: host FP64 arrays hdiag[R*(C-1)][N], vdiag[(R-1)*C][N]
  * (energy of a link with value k: LinkDiagonalTerm, gi/local_terms.py:12-39)
  * and plaq[(R-1)*(C-1)] (coefficient of P + P^dag, PlaquetteTerm).

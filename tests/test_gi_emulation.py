@@ -161,3 +161,48 @@ def test_tdvp_on_a_gi_model_with_full_gradients(emu_lib):
     with pytest.raises(NotImplementedError):
         TDVPDriver(model, H, preconditioner=SRPreconditioner(space=SampleSpace()), dt=0.05,
                    time_unit=ImaginaryTimeUnit(), n_samples=8, n_chains=8).run(0.05)
+
+
+def test_z3_pure_gauge_matches_oracle(emu_lib):
+    """Z3 (examples/lgt/z3_pure_gauge.py): 27 slices on a bulk site, +-1 plaquette flips distinct,
+    explicit flip offsets; sweep, amplitudes, O_k and energies against the oracle."""
+    from vmc_gb300.gi import GILocalHamiltonian, build_electric_terms
+    from vmc_gb300.operators import PlaquetteTerm
+
+    shape, dmax, chi, n = (3, 3), 2, 8, 8
+    R, C = shape
+    ocfg = ogi.GIConfig(shape, 3, dmax)
+    T = _fp32(ogi.init_tensors(ocfg, seed=21))
+    cfg = GIPEPSConfig(shape=shape, N=3, phys_dim=1, Qx=0, degeneracy_per_charge=(dmax, dmax, dmax))
+    model = GIPEPS(config=cfg, contraction_strategy=ZipUp(chi), device="cpu", tensors=T, lib=emu_lib)
+    terms = build_electric_terms(shape, 0.5, 3) + tuple(PlaquetteTerm(row=r, col=c, coeff=-1.0)
+                                                        for r in range(R - 1) for c in range(C - 1))
+    H = GILocalHamiltonian(shape=shape, terms=terms)
+    diag = 0.5 * (2.0 - 2.0 * np.cos(2.0 * np.pi * np.arange(3) / 3))
+    OH = ogi.GIHamiltonian(shape, tuple(ogi.PlaquetteTerm(r, c, -1.0) for r in range(R - 1) for c in range(C - 1))
+                           + tuple(ogi.LinkDiagonalTerm("h", ((r, c),), diag) for r in range(R) for c in range(C - 1))
+                           + tuple(ogi.LinkDiagonalTerm("v", ((r, c),), diag) for r in range(R - 1) for c in range(C)))
+    samples = ogi.random_physical_configuration(ocfg, n, seed=22)
+    rng = np.random.default_rng(23)
+    u = rng.random((n, (R - 1) * (C - 1)))
+    deltas = rng.integers(1, 3, (n, (R - 1) * (C - 1)))
+    eng = model.engine(H)
+    assert eng.phys_dim == 27 and eng.needs_deltas
+    tens = model.packed()
+    c = torch.from_numpy(samples.astype(np.int32))
+    cache = eng.init_cache(tens, c.clone())
+    res = eng.sweep(tens, c.clone(), torch.from_numpy(u), cache, deltas=torch.from_numpy(deltas.astype(np.int32)))
+    strat = op.ZipUp(chi)
+    s2, amp_ref, tops, margin = ogi.transition(T, ocfg, samples, deltas.reshape(n, R - 1, C - 1),
+                                               u.reshape(n, R - 1, C - 1), ogi.init_cache(T, ocfg, samples, strat),
+                                               strat)
+    same = np.all(res.configs.numpy() == s2, axis=1)
+    assert np.all(same | (margin < 1e-4)) and same.mean() > 0.7 and (s2 != samples).any()
+    grads, e_ref, _ = ogi.estimate(T, ocfg, s2, amp_ref, OH, strat, tops)
+    o_ref, p_ref = ogi.local_log_derivatives(T, ocfg, s2, grads, amp_ref)
+    amp = (res.sign * torch.exp(res.logamp)).numpy()
+    assert_parity(np.abs(amp[same] / amp_ref[same] - 1), True)
+    assert_parity(np.abs(res.E.numpy()[same] - e_ref[same]) / np.maximum(1.0, np.abs(e_ref[same])), True)
+    assert_parity(np.linalg.norm(res.O.numpy()[same] - o_ref[same], axis=1) / np.linalg.norm(o_ref[same], axis=1),
+                  True)
+    assert np.array_equal(res.p.numpy()[same], p_ref[same])

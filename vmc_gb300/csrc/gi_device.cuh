@@ -128,6 +128,8 @@ __device__ __noinline__ void gi_sweep_pair(const DevPlan& P, const Slot& S, Shar
   gi_row_slices(P, st, r + 1, sh.spins[1]);
   __syncthreads();
   gi_right_envs_2row(P, S, sh, perm, top, tbond, bot, bbond, r, sh.spins[0], sh.spins[1], vb);
+  // L: left environment before column c; La: L extended by column c with its current slices (carried
+  // from the previous plaquette); Lb: La extended by column c+1; Pa / Pb: the proposal's extensions
   float* L = S.l2[0];
   float* La = S.l2[1];
   float* Lb = S.scr[9];
@@ -135,16 +137,16 @@ __device__ __noinline__ void gi_sweep_pair(const DevPlan& P, const Slot& S, Shar
   float* Pb = S.scr[11];
   if (threadIdx.x == 0) set_elem(L, 0, 1.f);
   __syncthreads();
+  if (C > 1) gi_left_column(P, perm, top, tbond, bot, bbond, r, 0, sh.spins[0][0], sh.spins[1][0], L, La, vb);
   for (int c = 0; c + 1 < C; ++c) {
     const int k = r * (C - 1) + c;
     const int delta = deltas ? deltas[k] : 1;
     // current and proposed slices of the plaquette's four sites
-    const int c00 = sh.spins[0][c], c01 = sh.spins[0][c + 1], c10 = sh.spins[1][c], c11 = sh.spins[1][c + 1];
+    const int c01 = sh.spins[0][c + 1], c11 = sh.spins[1][c + 1];
     const int p00 = gi_slice(P, st, r, c, r, c, delta), p01 = gi_slice(P, st, r, c + 1, r, c, delta);
     const int p10 = gi_slice(P, st, r + 1, c, r, c, delta), p11 = gi_slice(P, st, r + 1, c + 1, r, c, delta);
     const float* Rn = S.r2 + (size_t)(c + 1) * P.E2S;
     const int n2 = gi_env2_size(P, tbond, bbond, r, c + 2);
-    gi_left_column(P, perm, top, tbond, bot, bbond, r, c, c00, c10, L, La, vb);
     gi_left_column(P, perm, top, tbond, bot, bbond, r, c + 1, c01, c11, La, Lb, vb);
     const double pc = abs2_dot(Lb, Rn, n2, sh.red);
     gi_left_column(P, perm, top, tbond, bot, bbond, r, c, p00, p10, L, Pa, vb);
@@ -171,13 +173,26 @@ __device__ __noinline__ void gi_sweep_pair(const DevPlan& P, const Slot& S, Shar
       sh.spins[1][c + 1] = p11;
     }
     __syncthreads();
-    // the left environment past column c: its accepted extension, renormalised
+    // the kept branch: the left environment past column c, renormalised by 2^-e, and its extension by
+    // column c+1 (the next plaquette's La) scaled by the same exact power of two
     float* next = accept ? Pa : La;
-    float* spare = accept ? La : Pa;
-    (void)cta_normalize(next, gi_env2_size(P, tbond, bbond, r, c + 1) * kEs, sh.red);
-    La = L;
+    float* next_a = accept ? Pb : Lb;
+    float* free0 = accept ? La : Pa;
+    float* free1 = accept ? Lb : Pb;
+    const double lg = cta_normalize(next, gi_env2_size(P, tbond, bbond, r, c + 1) * kEs, sh.red);
+    const int e = (int)lrint(lg / 0.69314718055994530942);
+    if (e != 0) {
+      const float sc = ldexpf(1.f, -e);
+      const int na = n2 * kEs;
+      for (int i = threadIdx.x; i < na; i += blockDim.x) next_a[i] *= sc;
+      __syncthreads();
+    }
+    float* old_L = L;
     L = next;
-    Pa = spare;
+    La = next_a;
+    Lb = old_L;
+    Pa = free0;
+    Pb = free1;
   }
 }
 

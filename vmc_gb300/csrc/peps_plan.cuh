@@ -30,7 +30,7 @@ constexpr int kThreads = VMC_MAX_THREADS;
 constexpr int kDefaultThreads = 128;  // one chain per 4 warps: more chains resident per SM
 constexpr int kMaxVec = 512;   // max vectors in one truncation (chi * D)
 constexpr int kMaxCols = 64;   // max lattice columns
-constexpr int kMaxD = 8;       // max slices per site: physical dimension (<= 4), or gauge configurations
+constexpr int kMaxD = 27;      // max slices per site: physical dimension (<= 4), or gauge configurations (Z3: 27)
 constexpr int kMaxPhys = 4;    // max physical dimension of a standard plan (its energy paths size d x d)
 constexpr int kPermKinds = 6;  // permuted copies of every site tensor
 constexpr float kJacobiTol = 5e-7f;  // stop when every |a_p.a_q| <= tol |a_p||a_q|
