@@ -158,9 +158,32 @@ def test_tdvp_on_a_gi_model_with_full_gradients(emu_lib):
     drv.run(0.1)
     assert drv.step_count == 2 and np.isfinite(drv.energy["mean"])
     assert any(not torch.equal(a, b) for ra, rb in zip(t0, drv._tensors) for a, b in zip(ra, rb))
-    with pytest.raises(NotImplementedError):
-        TDVPDriver(model, H, preconditioner=SRPreconditioner(space=SampleSpace()), dt=0.05,
-                   time_unit=ImaginaryTimeUnit(), n_samples=8, n_chains=8).run(0.05)
+    # the sliced solve (full_gradient=False) with the per-site slice counts of the GI model
+    sliced = TDVPDriver(model, H, preconditioner=SRPreconditioner(space=SampleSpace(), diag_shift=0.1), dt=0.05,
+                        time_unit=ImaginaryTimeUnit(), n_samples=64, n_chains=32)
+    sliced.run(0.05)
+    assert np.isfinite(sliced.energy["mean"])
+
+
+def test_sliced_and_full_sr_updates_agree_on_a_gi_model(emu_lib):
+    """The sliced Jacobian expanded with the GI model's per-site slice counts is the full Jacobian:
+    both SR solves give the same update (ParameterSpace, preconditioners.py:265-330)."""
+    from vmc_gb300.preconditioners import SRPreconditioner
+    from vmc_gb300.qgt import ParameterSpace
+
+    ocfg, T, model, samples, strat = _setup(emu_lib, (3, 3), 2, None, seed=31, n=24)
+    H = z2_pure_gauge_hamiltonian((3, 3))
+    outs = []
+    for full in (False, True):
+        init, trans, est = build_gi_mc_kernels(model, H, full_gradient=full)
+        c = torch.from_numpy(samples.astype(np.int32))
+        u = torch.ones((24, 4), dtype=torch.float64)  # keep the samples: both solves see the same ones
+        c2, _, ctx = trans(model.tensors, c, u, init(model.tensors, c))
+        _, le = est(model.tensors, c2, ctx)
+        upd, _ = SRPreconditioner(space=ParameterSpace(), diag_shift=0.1).apply(
+            model, model.tensors, c2, le.local_log_derivatives, le.active_slice_indices, le.local_estimate)
+        outs.append(torch.cat([x.reshape(-1) for row in upd for x in row]))
+    assert torch.allclose(outs[0], outs[1], rtol=1e-6, atol=1e-9)
 
 
 def test_z3_pure_gauge_matches_oracle(emu_lib):

@@ -192,6 +192,10 @@ class GIPEPS:
                 parts.append(pad.reshape(-1))
         return torch.cat(parts).contiguous()
 
+    def sliced_dims(self) -> tuple:
+        """Distinct active slices per site, phys_dim * nc (model.py:1066-1080)."""
+        return tuple(int(t.shape[1]) for row in self.tensors for t in row)
+
     @property
     def n_params(self) -> int:
         return sum(t.numel() for row in self.tensors for t in row)

@@ -177,11 +177,10 @@ class SRPreconditioner:
             dv = dv.to(torch.complex128) * grad_factor
         else:
             dv = dv * float(getattr(grad_factor, "real", grad_factor))
-        if p is not None and hasattr(model, "N"):
-            raise NotImplementedError("the sliced SR solve of a gauge-invariant PEPS is not implemented: "
-                                      "use full_gradient=True (as the reference's lattice-gauge drivers do)")
         pps = tuple(params_per_site(model.shape, model.bond_dim))
-        sd = (model.phys_dim,) * (model.shape[0] * model.shape[1])
+        # slices per site: phys_dim, or a GI model's phys_dim * nc per site (src/vmc/peps/gi/model.py:1066-1080)
+        sd = model.sliced_dims() if hasattr(model, "sliced_dims") else (model.phys_dim,) * (
+            model.shape[0] * model.shape[1])
         jac = Jacobian(o) if p is None else SlicedJacobian(o, p, sd, self.ordering)
         if isinstance(self.strategy, DirectSolve):
             x, metrics = _direct_solve(self.space, jac, dv, self.diag_shift, self.strategy.solver)

@@ -55,6 +55,8 @@ class GraphTDVPDriver:
             raise NotImplementedError("gauge projection is not part of a graph step")
         if model.phys_dim > 2:
             raise NotImplementedError("graph steps draw accept uniforms only; d > 2 also needs flip offsets")
+        if hasattr(model, "sliced_dims"):
+            raise NotImplementedError("graph steps run standard PEPS; a gauge-invariant PEPS runs in TDVPDriver")
         self._model = model
         self.operator = operator
         self.preconditioner = preconditioner
