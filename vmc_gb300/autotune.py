@@ -30,6 +30,7 @@ CANDIDATES = [
     {"threads": 128, "smem_kb": 0, "tile_policy": 0},
     {"threads": 256, "smem_kb": -1, "tile_policy": 0},
     {"threads": 256, "smem_kb": -1, "tile_policy": 2},
+    {"threads": 64, "smem_kb": -1, "tile_policy": 0},
 ]
 
 _LOCK = threading.Lock()

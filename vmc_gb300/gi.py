@@ -147,8 +147,11 @@ class GIEngine(PEPSEngine):
 class GIPEPS:
     """model.py:67-189 (pure gauge).  ``tensors[r][c]``: (1, nc, mu_u, mu_d, mu_l, mu_r) torch tensors."""
 
-    def __init__(self, *, rngs=0, config: GIPEPSConfig, contraction_strategy, device=None, tensors=None, lib=None):
+    def __init__(self, *, rngs=0, config: GIPEPSConfig, contraction_strategy, device=None, tensors=None, lib=None,
+                 engine_options=None):
+        """``engine_options``: the GI plan's launch configuration (vmc_plan_options as a dict), or None."""
         self.config = config
+        self.engine_options = None if engine_options is None else dict(engine_options)
         self.shape = tuple(config.shape)
         self.N = int(config.N)
         self.phys_dim = 1
@@ -230,7 +233,8 @@ class GIPEPS:
         if hit is None:
             sname, chi, n_sweeps = _engine_strategy(self.strategy)
             eng = GIEngine(self.shape, self.N, self.dmax, min(chi, 1 << 20), sname, n_sweeps, operator=operator,
-                           device=self.device, lib=self._lib, dtype="complex64" if self.is_complex else "float32")
+                           device=self.device, lib=self._lib, dtype="complex64" if self.is_complex else "float32",
+                           options=self.engine_options)
             self._engines[key] = (eng, operator)
             return eng
         return hit[0]
