@@ -229,6 +229,31 @@ def e2e_public_api(w, n, rank, dev, ustream, args, barrier):
     return n * args.steps / elapsed, h2d, d2h
 
 
+def unfused_rate(eng, tens, cfg, args, barrier):
+    """The same evaluation split the way the reference's driver splits it: amplitude + O_k in one
+    launch (vmc_peps_amp_grad) and E_loc in another (vmc_peps_local_energy), each contracting the
+    lattice from scratch, on configurations already sampled.  It does no sampling, so it does less
+    work than the fused sweep it is compared with.  Returns samples/s over --steps evaluations."""
+    import torch
+
+    n = cfg.shape[0]
+    for _ in range(max(1, args.warmup)):
+        la, sg, _ = eng.amp_grad(tens, cfg)
+        eng.local_energy(tens, cfg, la, sg)
+    barrier()
+    stream = torch.cuda.current_stream(eng.device)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        la, sg, _ = eng.amp_grad(tens, cfg)
+        eng.local_energy(tens, cfg, la, sg)
+    t1.record(stream)
+    barrier()
+    eng.raise_on_status()
+    return n * args.steps / (t0.elapsed_time(t1) / 1e3)
+
+
 def run_ours(args, rank, world, local_rank):
     import multiprocessing as mp
 
@@ -295,6 +320,9 @@ def run_ours(args, rank, world, local_rank):
     elapsed = float(t_all.item())
     value = world * n * args.steps / elapsed
 
+    # ---------------- the unfused split (amp+O_k launch, then E_loc launch) ----------------
+    unfused = unfused_rate(eng, tens, cfg, args, barrier) if not args.no_unfused else None
+
     # ---------------- end-to-end through the public API, host buffers ----------------
     e2e_value, h2d, d2h = e2e_public_api(w, n, rank, dev, ustream, args, barrier)
     if world > 1:
@@ -353,6 +381,11 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
         "kernel_ms_per_launch": statistics.mean(launch_ms),
     }
+    if unfused is not None:
+        line["unfused"] = {"value": unfused, "unit": UNIT, "launches_per_step": 2,
+                           "what": "FP32 amp+O_k launch then E_loc launch on sampled configurations (no "
+                                   "sampling), device-resident; the fused sweep also samples",
+                           "fused_over_unfused": value / unfused}
     print(json.dumps(line), flush=True)
 
 
@@ -605,6 +638,7 @@ def main():
     ap.add_argument("--cpu-chains-per-core", type=int, default=128)
     ap.add_argument("--ref-chains-per-core", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-unfused", action="store_true", help="skip the unfused amp+O_k / E_loc comparison leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

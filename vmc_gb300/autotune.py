@@ -31,6 +31,9 @@ CANDIDATES = [
     {"threads": 256, "smem_kb": -1, "tile_policy": 0},
     {"threads": 256, "smem_kb": -1, "tile_policy": 2},
     {"threads": 64, "smem_kb": -1, "tile_policy": 0},
+    {"threads": 64, "smem_kb": 0, "tile_policy": 0},
+    {"threads": 64, "smem_kb": 0, "tile_policy": 2},
+    {"threads": 64, "smem_kb": 20, "tile_policy": 0},
 ]
 
 _LOCK = threading.Lock()

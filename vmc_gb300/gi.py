@@ -144,14 +144,21 @@ class GIEngine(PEPSEngine):
         _abi.check(self.lib, st, "vmc_gi_set_operator")
 
 
+# The GI chain is a sequence of small GEMMs on 2-row environments, each ending in a CTA barrier: two warps
+# per chain and eight resident chains per SM run it faster than four warps and four chains (on GB300, 9x9
+# vertices, D=4, chi=32: 8,843 samples/s at 64 threads, 7,618 at 128, 4,511 at 256).
+GI_DEFAULT_OPTIONS = {"threads": 64, "smem_kb": -1, "tile_policy": 0}
+
+
 class GIPEPS:
     """model.py:67-189 (pure gauge).  ``tensors[r][c]``: (1, nc, mu_u, mu_d, mu_l, mu_r) torch tensors."""
 
     def __init__(self, *, rngs=0, config: GIPEPSConfig, contraction_strategy, device=None, tensors=None, lib=None,
                  engine_options=None):
-        """``engine_options``: the GI plan's launch configuration (vmc_plan_options as a dict), or None."""
+        """``engine_options``: the GI plan's launch configuration (vmc_plan_options as a dict); None takes
+        ``GI_DEFAULT_OPTIONS``."""
         self.config = config
-        self.engine_options = None if engine_options is None else dict(engine_options)
+        self.engine_options = dict(GI_DEFAULT_OPTIONS if engine_options is None else engine_options)
         self.shape = tuple(config.shape)
         self.N = int(config.N)
         self.phys_dim = 1
