@@ -179,7 +179,7 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def e2e_public_api(w, n, rank, dev, ustream, args, barrier):
+def e2e_public_api(w, n, rank, dev, ustream, args, barrier, options=None):
     """Same sweep through the user-facing API (PEPS + build_mc_kernels + make_mc_sampler),
     with every step's uniforms copied from pinned host memory and E_loc, log|psi| and
     sign read back to the host inside the timed region."""
@@ -194,7 +194,7 @@ def e2e_public_api(w, n, rank, dev, ustream, args, barrier):
     strategy = {"ZipUp": ZipUp, "Variational": Variational}.get(w.strategy, lambda _: NoTruncation())(w.chi)
     model = PEPS(shape=w.shape, bond_dim=w.bond_dim, phys_dim=w.phys_dim, contraction_strategy=strategy,
                  device=dev, tensors=w.tensors(seed=0),
-                 dtype=torch.complex64 if w.dtype == "complex64" else torch.float32)
+                 dtype=torch.complex64 if w.dtype == "complex64" else torch.float32, engine_options=options)
     init_cache, transition, estimate = build_mc_kernels(model, w.operator())
     sampler = make_mc_sampler(transition, estimate)
     cfg = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
@@ -227,6 +227,20 @@ def e2e_public_api(w, n, rank, dev, ustream, args, barrier):
     h2d = n * n_sites * 8
     d2h = 3 * n * 8
     return n * args.steps / elapsed, h2d, d2h
+
+
+def shipped_options(w):
+    """The launch configuration the shipped GB300 autotune table holds for this workload, or None (the
+    engine's default) when the table has no entry for it."""
+    import json
+
+    import torch
+
+    from vmc_gb300.autotune import SHIPPED, _key
+
+    key = _key(torch.device("cuda"), w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype)
+    hit = json.loads(SHIPPED.read_text()).get(key)
+    return dict(hit["options"]) if hit else None
 
 
 def unfused_rate(eng, tens, cfg, args, barrier):
@@ -277,8 +291,9 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device(f"cuda:{local_rank}")
     torch.cuda.set_device(dev)
     n_sites = w.shape[0] * w.shape[1]
+    options = shipped_options(w)
     eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev,
-                     dtype=w.dtype)
+                     dtype=w.dtype, options=options)
     tens = torch.from_numpy(pack_tensors(w.tensors(seed=0))).to(dev)
     cfg0 = torch.from_numpy(initial_configs(n, n_sites, w.phys_dim, seed=rank)).to(dev)
     ustream = uniform_stream(n, n_sites, seed=1000 * rank)
@@ -324,7 +339,7 @@ def run_ours(args, rank, world, local_rank):
     unfused = unfused_rate(eng, tens, cfg, args, barrier) if not args.no_unfused else None
 
     # ---------------- end-to-end through the public API, host buffers ----------------
-    e2e_value, h2d, d2h = e2e_public_api(w, n, rank, dev, ustream, args, barrier)
+    e2e_value, h2d, d2h = e2e_public_api(w, n, rank, dev, ustream, args, barrier, options)
     if world > 1:
         t = torch.tensor([n * args.steps / e2e_value], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -371,6 +386,7 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
                    "phys_dim": w.phys_dim, "strategy": f"{w.strategy}({w.chi})", "model": w.model,
                    "chains_per_gpu": n, "global_chains": n * world, "parallelism": f"replicas x{world}",
+                   "launch_options": options or "engine default",
                    "l2": "inputs larger than L2 (bottom-env cache "
                          f"{eng.cache_bytes(n) / 1e9:.2f} GB read+written per step)"},
         "roofline": roofline,

@@ -80,11 +80,14 @@ class PEPS:
     dtypes the complex64 engine.  ``lib``
     selects an engine library other than the in-tree CUDA build (a ctypes
     handle bound by ``vmc_gb300._abi.bind``); by default the CUDA build is
-    required.
+    required.  ``engine_options``: the plan's launch configuration (a
+    vmc_plan_options dict, or "auto" for the autotuner's winner on this GPU);
+    None takes the engine's default.
     """
 
     def __init__(self, *, rngs=0, shape, bond_dim, phys_dim=2, contraction_strategy=None,
-                 dtype=torch.float32, device=None, tensors=None, lib=None):
+                 dtype=torch.float32, device=None, tensors=None, lib=None, engine_options=None):
+        self.engine_options = engine_options if engine_options in (None, "auto") else dict(engine_options)
         self.shape = (int(shape[0]), int(shape[1]))
         self.bond_dim = int(bond_dim)
         self.phys_dim = int(phys_dim)
@@ -152,7 +155,7 @@ class PEPS:
             sname, chi, n_sweeps = _engine_strategy(self.strategy)
             eng = PEPSEngine(self.shape, self.bond_dim, min(chi, 1 << 20), self.phys_dim, sname, n_sweeps,
                              operator=operator, device=self.device, lib=self._lib,
-                             dtype="complex64" if self.is_complex else "float32")
+                             dtype="complex64" if self.is_complex else "float32", options=self.engine_options)
             self._engines[key] = (eng, operator)
             return eng
         return eng[0]
