@@ -93,3 +93,27 @@ def test_qr_solve_both_min_norm_branches_match_oracle(emu_lib, m, n, rank, cplx)
     xr, mr = osr.qr_solve(osr.Jacobian(O), dv)
     assert met["rank"] == mr["rank"]
     assert np.linalg.norm(x.numpy() - xr) <= 1e-9 * np.linalg.norm(xr)
+
+
+@pytest.mark.parametrize("m,n", [(40, 90), (90, 40)], ids=["wide", "tall"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_qr_solve_graded_spectrum(emu_lib, m, n, cplx):
+    """Singular values spread over eight decades (rank 30, kept whole by the default rcond): the
+    minimum-norm x from the QR of R^H matches the oracle and the pseudo-inverse solution."""
+    from oracle import sr as osr
+    from vmc_gb300 import qgt as gq
+    from vmc_gb300.preconditioners import _qr_solve
+
+    rng = np.random.default_rng(m * n + cplx)
+    rank = 30
+    u = np.linalg.qr(_rand(rng, (m, rank), cplx))[0]
+    v = np.linalg.qr(_rand(rng, (n, rank), cplx))[0]
+    O = (u * np.logspace(0, -8, rank)) @ v.conj().T
+    dv = _rand(rng, (m,), cplx)
+    x, met = _qr_solve(gq.Jacobian(torch.as_tensor(O)), torch.as_tensor(dv), None, True, lib=emu_lib)
+    xr, mr = osr.qr_solve(osr.Jacobian(O), dv)
+    assert met["rank"] == mr["rank"]
+    oc = O - O.mean(axis=0, keepdims=True)
+    xp = np.linalg.pinv(oc, rcond=1e-12) @ dv
+    assert np.linalg.norm(x.numpy() - xr) <= 1e-6 * np.linalg.norm(xr)
+    assert np.linalg.norm(x.numpy() - xp) <= 1e-6 * np.linalg.norm(xp)

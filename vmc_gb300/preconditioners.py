@@ -101,44 +101,44 @@ def _qr_solve(jac: Jacobian, dv, rcond, min_norm, lib=None):
     dvd = dv.to(device=o.device, dtype=dt)
     r, piv, y = qr_pivoted(oc, dvd, lib=lib)
     y = y[:, 0]
-    # matrix_rank(r): R's singular values are those of the k x k triangle of a QR of R^H (no
-    # squaring, unlike R R^H), so the SVD runs on k x k instead of k x n
-    rt = torch.linalg.qr(r.mH, mode="r")[1] if r.shape[1] > r.shape[0] else r
+    k, n_red = r.shape
+    # One Householder QR of R^H (n x k), R^H = Q T, serves both the rank and the solve: R = T^H Q^H has
+    # T's singular values (an SVD of the k x k triangle instead of the k x n trapezoid, with no squaring
+    # as R R^H would), and the minimum-norm solution of R[:rank] z = y1 is z = Q [T11^-H y1; 0] with
+    # T11 = T[:rank, :rank], since R[:rank]^H = Q[:, :rank] T11
+    qa = tau = None
+    if n_red > k:
+        qa, tau = torch.geqrf(r.mH)
+        rt = qa[:k].triu()
+    else:
+        rt = r
     eps = torch.finfo(torch.float64).eps
     rtol = max(r.shape) * eps if rcond is None else rcond
     if rt.is_cuda and rt.numel():
-        # cuSOLVER's QR-iteration SVD (gesvd): robust on the rank-deficient triangles that repeated
-        # samples produce, and faster here than svdvals' default driver (8.8 s against 12.1 s at
-        # 4096 x 4096); the approximate gesvda does not converge on them
-        sv = torch.linalg.svd(rt, full_matrices=False, driver="gesvd")[1]
+        # singular values only, by cuSOLVER's QR-iteration SVD (gesvd): robust on the rank-deficient
+        # triangles that repeated samples produce (the approximate gesvda does not converge on them)
+        sv = torch.linalg.svdvals(rt, driver="gesvd")
     else:
         sv = torch.linalg.svdvals(rt)
     smax = sv.max() if sv.numel() else torch.zeros((), dtype=torch.float64, device=o.device)
     tol = rtol * smax
     rank = int((sv > tol).sum())  # the reference's int(matrix_rank(r)) also reads it on the host
-    n_red = r.shape[1]
     n2 = n_red - rank
     x = torch.zeros(n_red, dtype=dt, device=o.device)
     if rank:
-        r11, r12, y1 = r[:rank, :rank], r[:rank, rank:], y[:rank, None]
+        y1 = y[:rank, None]
         if min_norm and n2 > 0:
-            # minimum-norm z = (z1, z2) of z1 + B z2 = a, a = R11^-1 y1, B = R11^-1 R12.  The reference
-            # solves (B^H B + I) z2 = B^H a (n2 x n2); by the push-through identity the same z is
-            # z1 = (I + B B^H)^-1 a, z2 = B^H z1 (rank x rank): the smaller system is solved.
-            a = torch.linalg.solve_triangular(r11, y1, upper=True)
-            bm = torch.linalg.solve_triangular(r11, r12, upper=True)
-            if n2 > rank:
-                chol, _ = torch.linalg.cholesky_ex(bm @ bm.mH + torch.eye(rank, dtype=dt, device=o.device))
-                x1 = torch.cholesky_solve(a, chol)
-                x2 = bm.mH @ x1
-            else:
-                chol, _ = torch.linalg.cholesky_ex(bm.mH @ bm + torch.eye(n2, dtype=dt, device=o.device))
-                x2 = torch.cholesky_solve(bm.mH @ a, chol)
-                x1 = a - bm @ x2
+            # the reference's z1 + B z2 = a, a = R11^-1 y1, B = R11^-1 R12, minimising |z|, is the
+            # minimum-norm solution of [R11 R12] z = y1
+            if qa is None:
+                qa, tau = torch.geqrf(r.mH)
+            w = torch.zeros((n_red, 1), dtype=dt, device=o.device)
+            w[:rank] = torch.linalg.solve_triangular(qa[:rank, :rank].triu().mH, y1, upper=False)
+            z = torch.ormqr(qa, tau, w, left=True, transpose=False)
         else:
-            x1 = torch.linalg.solve_triangular(r11, y1, upper=True)
-            x2 = torch.zeros((n2, 1), dtype=dt, device=o.device)
-        x[piv] = torch.cat([x1, x2])[:, 0]
+            z = torch.zeros((n_red, 1), dtype=dt, device=o.device)
+            z[:rank] = torch.linalg.solve_triangular(r[:rank, :rank], y1, upper=True)
+        x[piv] = z[:, 0]
     rhs = oc.mH @ dvd
     resid = oc.mH @ (oc @ x) - rhs
     err = (torch.linalg.norm(resid) ** 2 / torch.linalg.norm(rhs) ** 2).item()
