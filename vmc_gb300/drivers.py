@@ -19,12 +19,30 @@ from .sampling import _sample_counts, _trim_samples, make_mc_sampler
 
 logger = logging.getLogger(__name__)
 
-__all__ = ["TDVPDriver", "Integrator", "Euler", "RK4", "TimeUnit", "RealTimeUnit", "ImaginaryTimeUnit"]
+__all__ = ["TDVPDriver", "Integrator", "Euler", "RK4", "TimeUnit", "RealTimeUnit", "ImaginaryTimeUnit", "EnergyStats"]
 
 
 def _add_scaled(base, delta, scale):
     """src/vmc/utils/utils.py:60-65."""
     return [[b + scale * d for b, d in zip(rb, rd)] for rb, rd in zip(base, delta)]
+
+
+class EnergyStats(dict):
+    """Statistics of the last step's local energies (tdvp.py:226, netket.stats.statistics): ``mean``,
+    ``variance`` and ``error_of_mean``, read as attributes (``driver.energy.mean.real``, as the
+    reference's examples do) or as keys."""
+
+    def __getattr__(self, name):
+        try:
+            return self[name]
+        except KeyError:
+            raise AttributeError(name) from None
+
+    @classmethod
+    def of(cls, e: torch.Tensor) -> "EnergyStats":
+        mean = e.mean()
+        var = float((e - mean).abs().pow(2).mean())
+        return cls(mean=mean.item(), variance=var, error_of_mean=math.sqrt(var / e.numel()))
 
 
 class Integrator:
@@ -155,10 +173,7 @@ class TDVPDriver:
         self._sampler_configuration = carry[1]
         self._model.tensors = self._tensors
         self.step_count += n_steps
-        mean = e.mean()
-        var = float((e - mean).abs().pow(2).mean())
-        self._loss_stats = {"mean": mean.item(), "variance": var,
-                            "error_of_mean": math.sqrt(var / e.numel())}
+        self._loss_stats = EnergyStats.of(e)
         self.residual_error = metrics.get("residual_error")
 
     # ------------------------------------------------------------ checkpoint
@@ -197,7 +212,7 @@ class TDVPDriver:
         self._model.tensors = self._tensors
         self._sampler_configuration = state["sampler_configuration"].to(dev, torch.int32).clone()
         self._gen.set_state(state["generator_state"])
-        self._loss_stats = None if state["loss_stats"] is None else dict(state["loss_stats"])
+        self._loss_stats = None if state["loss_stats"] is None else EnergyStats(state["loss_stats"])
 
     def save(self, path) -> None:
         torch.save(self.state_dict(), path)

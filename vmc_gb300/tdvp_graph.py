@@ -20,12 +20,11 @@ two give the same bits.
 from __future__ import annotations
 
 import ctypes as ct
-import math
 
 import torch
 
 from . import _abi
-from .drivers import Euler, RealTimeUnit, RK4, TimeUnit
+from .drivers import EnergyStats, Euler, RealTimeUnit, RK4, TimeUnit
 from .engine import SweepResult
 from .lowering import params_per_site
 from .preconditioners import DirectSolve, SRPreconditioner, _direct_solve, reorder_updates
@@ -189,9 +188,7 @@ class GraphTDVPDriver:
         self._eng.raise_on_status()
         self._model.tensors = self._model.unpack(self._theta.clone())
         e = self._E.reshape(-1)[:self.n_samples]
-        mean = e.mean()
-        var = float((e - mean).abs().pow(2).mean())
-        self._loss_stats = {"mean": mean.item(), "variance": var, "error_of_mean": math.sqrt(var / e.numel())}
+        self._loss_stats = EnergyStats.of(e)
 
     # ------------------------------------------------------------------ state
     @property
@@ -237,5 +234,5 @@ class GraphTDVPDriver:
         self._theta.copy_(state["theta"].to(self._dev))
         self._configs.copy_(state["sampler_configuration"].to(self._dev))
         self._counter.fill_(int(state["counter"]))
-        self._loss_stats = None if state["loss_stats"] is None else dict(state["loss_stats"])
+        self._loss_stats = None if state["loss_stats"] is None else EnergyStats(state["loss_stats"])
         self._model.tensors = self._model.unpack(self._theta.clone())
