@@ -78,14 +78,14 @@ def _store(key: str, entry: dict) -> None:
 
 
 def _time_candidate(options, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator, device, lib,
-                    waves, reps, seed=0):
+                    waves, reps, seed=0, n_chains=None):
     from .engine import PEPSEngine
     from .lowering import pack_tensors
     from .synthetic import initial_configs, random_tensors
 
     eng = PEPSEngine(shape, bond_dim, chi, phys_dim, strategy, n_sweeps, operator=operator, device=device,
                      lib=lib, dtype=dtype, options=options)
-    n = max(1, waves * eng.resident_chains)
+    n = int(n_chains) if n_chains else max(1, waves * eng.resident_chains)
     n_sites = shape[0] * shape[1]
     T = random_tensors(shape, bond_dim, phys_dim=phys_dim, seed=seed,
                        dtype=np.complex128 if dtype == "complex64" else np.float64)
@@ -120,8 +120,11 @@ def _time_candidate(options, shape, bond_dim, chi, phys_dim, strategy, n_sweeps,
 
 
 def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32", operator=None,
-         device=None, lib=None, candidates=None, waves=1, reps=1, store=True) -> dict:
-    """Time every candidate on this problem; returns {"options", "samples_per_s", "candidates"}."""
+         device=None, lib=None, candidates=None, waves=1, reps=1, store=True, n_chains=None) -> dict:
+    """Time every candidate on this problem; returns {"options", "samples_per_s", "candidates"}.
+    ``n_chains``: chains per timed sweep (the run's own count); None times ``waves`` full waves of each
+    candidate's resident chains.  One wave favours configurations whose extra resident chains only pay
+    off within a wave, so a table meant for a given run size is best tuned at that size."""
     from .operators import heisenberg
 
     shape = (int(shape[0]), int(shape[1]))
@@ -132,7 +135,7 @@ def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="
     results = []
     for cand in candidates or CANDIDATES:
         rate = _time_candidate(cand, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op, device, lib,
-                               waves, reps)
+                               waves, reps, n_chains=n_chains)
         results.append({"options": dict(cand), "samples_per_s": rate})
     best = max(results, key=lambda r: r["samples_per_s"])
     entry = {"options": best["options"], "samples_per_s": best["samples_per_s"], "candidates": results}
@@ -168,12 +171,21 @@ def main(argv=None) -> None:
                                                        "heis8x8_D5_chi25", "tfim10x10_D4_chi16_c64",
                                                        "heis12x12_D6_chi36", "heis16x16_D6_chi48"])
     ap.add_argument("--out", default=str(SHIPPED))
+    ap.add_argument("--chains", type=int, default=-1,
+                    help="chains per timed sweep: -1 the workload's own count when one sweep of it stays under "
+                         "about 20 s, else one wave; 0 one wave; N > 0 exactly N")
     args = ap.parse_args(argv)
     table = _load(args.out)
     dev = torch.device("cuda")
     for name in args.workloads:
         w = WORKLOADS[name]
-        entry = tune(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype, w.operator(), dev, store=False)
+        n = args.chains
+        if n < 0:
+            # about 2.4 TFLOP/s of algorithmic work is what one GB300 sustains on these plans
+            n = w.n_chains if (w.flops_per_sample() or 0) * w.n_chains < 20 * 2.4e12 else 0
+        entry = tune(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype, w.operator(), dev, store=False,
+                     n_chains=n or None)
+        entry["chains"] = n or "one wave"
         table[_key(dev, w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype)] = entry
         print(json.dumps({"workload": name, **entry}), flush=True)
         Path(args.out).write_text(json.dumps(table, indent=1, sort_keys=True))

@@ -607,10 +607,30 @@ __device__ inline void fill_ones_row(const DevPlan& P, float* row) {
   __syncthreads();
 }
 
+// op element (re, im) of a real or complex operator table
+__device__ __forceinline__ void op_elem(const float* table, size_t e, double* re, double* im) {
+  const float* x = elem(table, e);
+  *re = x[0];
+  *im = kCplx ? (double)x[1] : 0.0;
+}
+
+// Pairs (p, q), as bit p*d + q, whose coefficient in column `col` of the d^2 x d^2 two-site operator
+// `op` (element (j, col) at j*d*d + col) is nonzero: the only amplitudes psi(p, q) that E_loc uses.
+// For a Heisenberg bond with parallel spins that is the configuration's own pair alone.
+__device__ __forceinline__ unsigned nonzero_pairs(const float* op, int d, int col) {
+  unsigned m = 0;
+  for (int j = 0; j < d * d; ++j) {
+    double re, im;
+    op_elem(op, (size_t)j * d * d + col, &re, &im);
+    if (re != 0.0 || im != 0.0) m |= 1u << j;
+  }
+  return m;
+}
+
 // Right environments of one row: R[q][c] for c = C-1..0 (R_c covers columns
-// > c).  With open_q, R_c is produced for every spin q of site c+1
-// (renv[q][c]); otherwise only for its current spin (renv[spin][c] and also
-// stored at renv[0][c]... the caller reads renv_cur()).
+// > c), at renv[q][c] for the current spin q of site c+1 (read through
+// renv_cur()).  With open_q, also for every other q that the horizontal term
+// of the bond (c, c+1) meets with a nonzero coefficient.
 __device__ __noinline__ void right_envs(const DevPlan& P, const Slot& S, Shared& sh, const float* perm,
                                        const float* top, const int* tbond, const float* bot, const int* bbond, int row,
                                        const int* spins, bool open_q) {
@@ -635,8 +655,16 @@ __device__ __noinline__ void right_envs(const DevPlan& P, const Slot& S, Shared&
     const float* Rin = S.renv + ((size_t)qin * C + c) * P.ES;
     const double lin_c = S.rl[(size_t)qin * C + c];
     renv_step1(T, Rin, X1, ta, U, tb, Rb, bb);
+    // R_{c-1}^(q) for the configuration's spin of site c and, when the bond (c-1, c) carries a term, for
+    // every q that meets a nonzero coefficient of its operator
+    unsigned qm = 0;
+    if (open_q && P.horiz_mask[row * (C - 1) + c - 1]) {
+      const unsigned jm = nonzero_pairs(elem(P.horiz, (size_t)(row * (C - 1) + c - 1) * P.d * P.d * P.d * P.d),
+                                        P.d, spins[c - 1] * P.d + spins[c]);
+      for (int p = 0; p < P.d; ++p) qm |= (jm >> (p * P.d)) & ((1u << P.d) - 1u);
+    }
     for (int q = 0; q < P.d; ++q) {
-      if (!open_q && q != spins[c]) continue;
+      if (q != spins[c] && !((qm >> q) & 1u)) continue;
       float* Rout = S.renv + ((size_t)q * C + (c - 1)) * P.ES;
       renv_step23(X1, perm_of(P, perm, s, P_RENV, q), B, X2, Rout, ta, U, Rb, bb, Lb, V, ba);
       const double lg = cta_normalize(Rout, ta * Lb * ba * kEs, sh.red);
@@ -722,13 +750,6 @@ __device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Sha
 // Estimate of one row (energy.py:158-205): gradient envs, one-site and
 // horizontal energies.  `oscale` = exp(lt + lb - logamp) * sign(amp).
 // ---------------------------------------------------------------------------
-// op element (re, im) of a real or complex operator table
-__device__ __forceinline__ void op_elem(const float* table, size_t e, double* re, double* im) {
-  const float* x = elem(table, e);
-  *re = x[0];
-  *im = kCplx ? (double)x[1] : 0.0;
-}
-
 // energy += (ar + i ai) * (br + i bi) * (cr + i ci)
 __device__ __forceinline__ void acc3(double* energy, double ar, double ai, double br, double bi, double cr,
                                      double ci) {
@@ -797,10 +818,16 @@ __device__ __noinline__ void estimate_row(const DevPlan& P, const Slot& S, Share
       const int cur1 = spins[c + 1];
       const size_t op0 = (size_t)(row * (C - 1) + c) * P.d * P.d * P.d * P.d;
       const int col = cur * P.d + cur1;
+      const unsigned jm = nonzero_pairs(elem(P.horiz, op0), P.d, col);
       for (int p = 0; p < P.d; ++p) {
+        // L'^(p) for the configuration's own spin (the next environment) and for every p with a nonzero
+        // coefficient; psi(p, q) only where the coefficient is nonzero
+        const unsigned qm = (jm >> (p * P.d)) & ((1u << P.d) - 1u);
+        if (p != cur && qm == 0) continue;
         float* Lp = S.lenv + (size_t)(1 + p) * P.ES;
         lenv_step23(Y1, perm_of(P, perm, s, P_LENV, p), B, Y2, Lp, ba, tb, Lb, U, Rb, V, bb);
         for (int q = 0; q < P.d; ++q) {
+          if (!((qm >> q) & 1u)) continue;
           const float* Rq = S.renv + ((size_t)q * C + c) * P.ES;
           double pi = 0.0;
           const double pr = elem_dot(Lp, Rq, n_env, sh.red, &pi);
@@ -885,12 +912,19 @@ __device__ __noinline__ void vertical_energy(const DevPlan& P, const Slot& S, Sh
     const float* T = top + (size_t)c * P.TS;
     const float* B = bot + (size_t)c * P.TS;
     const float* Rc = S.r2 + (size_t)c * P.E2S;
-    const bool vt = P.vert_mask[r * C + c];
+    const int s_cur = sp0[c];
+    // pairs (p, q) with a nonzero coefficient in the configuration's column of the bond operator; when
+    // that is the configuration's own pair alone (a Heisenberg bond with parallel spins), psi comes from
+    // the slices the environment update forms anyway
+    const unsigned jm = P.vert_mask[r * C + c]
+                            ? nonzero_pairs(elem(P.vert, (size_t)(r * C + c) * d * d * d * d), d, s_cur * d + sp1[c])
+                            : 0u;
+    const bool vt = jm != 0;
+    const bool own_only = jm == (1u << (s_cur * d + sp1[c]));
     const bool last = (c == C - 1);
     if (!vt && last) break;
     double psi[kMaxPhys * kMaxPhys], psi_im[kMaxPhys * kMaxPhys];  // standard plans only: d <= kMaxPhys
     for (int i = 0; i < d * d; ++i) psi[i] = psi_im[i] = 0.0;
-    const int s_cur = sp0[c];
     const int sz0 = ssize(P, s0), sz1 = ssize(P, s1);
     const int vstride = (int)(vb[2] - vb[1]) / kEs;  // buffer spacing in elements
     for (int b0 = 0; b0 < tb; b0 += P.vchunk) {
@@ -901,7 +935,7 @@ __device__ __noinline__ void vertical_energy(const DevPlan& P, const Slot& S, Sh
                          two(Lb1 * ba, U, nb * Lb * U), two(nb, 1, Lb * U), Lb * Lb1 * ba, U * nb, ta));
       // Q2[p][e][b][rr][x][v] = sum_{l,u} Q1[x][e][b][l][u] A[p](u,v,l,rr); with a vertical term every
       // p at once (the spin slices of A are contiguous, the buffers vb[1+p] equally spaced)
-      if (vt) {
+      if (vt && !own_only) {
         gemm(make_gemm(Q1, lin(Lb * U), 1, perm_of(P, perm, s0, P_LENV, 0), two(Rb * V, sz0, 1), Rb * V,
                            vb[1], two(ba * nb, V, Rb * Lb1 * V), three(Rb, V, vstride, Lb1 * V, 1),
                            Lb1 * ba * nb, d * Rb * V, Lb * U));
@@ -916,19 +950,34 @@ __device__ __noinline__ void vertical_energy(const DevPlan& P, const Slot& S, Sh
                            two(V1, nb * Rb * V1 * Rb1, Rb1), three(Rb, Rb1, Rb * V1 * Rb1, V1 * Rb1, 1), ba * V1,
                            nb * Rb * Rb1, bb));
         const int q2n = Lb1 * ba * nb * Rb * V;
-        // Vq[e][b][rr][x][v] = sum_{w,y} A'[q][x][v][w][y] W2[e][b][rr][w][y], every q in one GEMM
-        gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, 0), two(Lb1 * V, sz1, V1 * Rb1), 1, W2, lin(V1 * Rb1), 1,
-                           vb[1 + d], two(Lb1 * V, vstride, 1), lin(Lb1 * V), d * Lb1 * V, ba * nb * Rb, V1 * Rb1));
-        // psi(p, q) += <Q2[p], Vq> for all d*d pairs in one pass and one reduction
-        if (kCplx) {
-          for (int pp = 0; pp < d; ++pp)
-            for (int q = 0; q < d; ++q) {
-              double im = 0.0;
-              psi[pp * d + q] += cta_cdot(vb[1 + pp], vb[1 + d + q], q2n, sh.red, &im);
-              psi_im[pp * d + q] += im;
-            }
+        if (own_only) {
+          // Vq for q = the configuration's spin only; psi(cur, cur1) += <Q2[cur], Vq>
+          const int q = sp1[c];
+          gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, q), lin(V1 * Rb1), 1, W2, lin(V1 * Rb1), 1, vb[1 + d + q],
+                             lin(1), lin(Lb1 * V), Lb1 * V, ba * nb * Rb, V1 * Rb1));
+          if (kCplx) {
+            double im = 0.0;
+            psi[s_cur * d + q] += cta_cdot(vb[1 + s_cur], vb[1 + d + q], q2n, sh.red, &im);
+            psi_im[s_cur * d + q] += im;
+          } else {
+            psi[s_cur * d + q] += cta_dot(vb[1 + s_cur], vb[1 + d + q], q2n, sh.red);
+          }
         } else {
-          cta_dots_all(vb + 1, vb + 1 + d, d, q2n, psi, sh.red);
+          // Vq[e][b][rr][x][v] = sum_{w,y} A'[q][x][v][w][y] W2[e][b][rr][w][y], every q in one GEMM
+          gemm(make_gemm(perm_of(P, perm, s1, P_ZIPT, 0), two(Lb1 * V, sz1, V1 * Rb1), 1, W2, lin(V1 * Rb1), 1,
+                             vb[1 + d], two(Lb1 * V, vstride, 1), lin(Lb1 * V), d * Lb1 * V, ba * nb * Rb,
+                             V1 * Rb1));
+          // psi(p, q) += <Q2[p], Vq> for all d*d pairs in one pass and one reduction
+          if (kCplx) {
+            for (int pp = 0; pp < d; ++pp)
+              for (int q = 0; q < d; ++q) {
+                double im = 0.0;
+                psi[pp * d + q] += cta_cdot(vb[1 + pp], vb[1 + d + q], q2n, sh.red, &im);
+                psi_im[pp * d + q] += im;
+              }
+          } else {
+            cta_dots_all(vb + 1, vb + 1 + d, d, q2n, psi, sh.red);
+          }
         }
       }
       if (!last) {
