@@ -98,7 +98,9 @@ vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys
  *   smem_kb      dynamic shared memory per CTA for the truncation arena and
  *                the 1-row intermediates, 0..52 KB; -1: 52 (0: all in the
  *                CTA's workspace slot, L1-cached)
- *   tile_policy  register tiles of the CTA GEMMs: 0 default, 1 smaller, 2 larger
+ *   tile_policy  register tiles of the CTA GEMMs: 0 default, 1 smaller, 2 larger, 3 real GEMMs of at
+ *                least 16 x 8 x 8 on the tensor cores (3xTF32, FP32 accuracy; faster from D = 6, chi = 36
+ *                on), the rest as 0
  * vmc_peps_plan uses the defaults, overridden by the VMC_THREADS, VMC_SMEM_KB
  * and VMC_TILE_POLICY environment variables when set; vmc_peps_plan_ex with
  * options ignores the environment.

@@ -45,3 +45,28 @@ def test_tune_then_auto(cuda_device, tmp_path, monkeypatch):
     eng = PEPSEngine((6, 6), 4, 16, 2, "ZipUp", operator=hamiltonian("heisenberg", (6, 6)), device=cuda_device,
                      options="auto")
     assert eng.options == entry["options"]
+
+
+@pytest.mark.parametrize("threads", [128, 256])
+def test_tensor_core_policy_at_large_bonds(cuda_device, threads):
+    """tile_policy 3 (3xTF32 tensor-core GEMMs) where its GEMMs engage: 4x4, D=6, chi=36 against the FP64
+    oracle, with the bars of an active truncation (the FFMA tiles give a median of 3e-6 and a maximum of
+    8e-5 on these samples)."""
+    shape, D, chi = (4, 4), 6, 36
+    H = hamiltonian("heisenberg", shape)
+    T, cfg, _ = make_case(shape, D, 6, seed=21)
+    eng = PEPSEngine(shape, D, chi, 2, "ZipUp", operator=H, device=cuda_device,
+                     options={"threads": threads, "smem_kb": -1, "tile_policy": 3})
+    tens = torch.from_numpy(pack_tensors(T)).to(cuda_device)
+    c = torch.from_numpy(cfg).to(cuda_device)
+    la, sg, O = eng.amp_grad(tens, c)
+    E = eng.local_energy(tens, c, la, sg)
+    torch.cuda.synchronize()
+    eng.raise_on_status()
+    model = oracle.PEPS(fp32(T), shape, D, strategy=oracle.ZipUp(chi))
+    amp, grads, _ = oracle.value_and_grad(model, cfg)
+    assert_parity(np.abs((sg * torch.exp(la)).cpu().numpy() / amp - 1), True)
+    o_ref = grads / amp[:, None]
+    assert_parity(np.linalg.norm(O.cpu().numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
+    e_ref = oracle.local_estimate(model, cfg, H, amp)
+    assert_parity(np.abs(E.cpu().numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)

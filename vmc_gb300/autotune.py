@@ -34,6 +34,8 @@ CANDIDATES = [
     {"threads": 64, "smem_kb": 0, "tile_policy": 0},
     {"threads": 64, "smem_kb": 0, "tile_policy": 2},
     {"threads": 64, "smem_kb": 20, "tile_policy": 0},
+    {"threads": 128, "smem_kb": -1, "tile_policy": 3},
+    {"threads": 256, "smem_kb": -1, "tile_policy": 3},
 ]
 
 _LOCK = threading.Lock()

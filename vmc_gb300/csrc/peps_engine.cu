@@ -253,7 +253,7 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
   if (!shape || !out_plan) return VMC_ERR_INVALID;
   if (opts && (opts->threads != 0 && (opts->threads < 64 || opts->threads > kThreads || opts->threads % 32 != 0)))
     return VMC_ERR_INVALID;
-  if (opts && (opts->tile_policy < 0 || opts->tile_policy > 2 || opts->smem_kb < -1)) return VMC_ERR_INVALID;
+  if (opts && (opts->tile_policy < 0 || opts->tile_policy > 3 || opts->smem_kb < -1)) return VMC_ERR_INVALID;
   *out_plan = nullptr;
   const int R = shape->n_rows, C = shape->n_cols;
   if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
@@ -376,7 +376,7 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
     P.threads = opts ? (opts->threads ? opts->threads : kDefaultThreads)
                      : th ? std::max(64, std::min(kThreads, std::atoi(th))) : kDefaultThreads;
     const char* tp = opts ? nullptr : std::getenv("VMC_TILE_POLICY");
-    P.tile_policy = opts ? opts->tile_policy : tp ? std::max(0, std::min(2, std::atoi(tp))) : 0;
+    P.tile_policy = opts ? opts->tile_policy : tp ? std::max(0, std::min(3, std::atoi(tp))) : 0;
   }
   long long budget = kMaxArenaSmemBytes;
   if (opts) {

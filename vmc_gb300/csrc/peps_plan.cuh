@@ -198,12 +198,14 @@ struct KernelSet {
                      int32_t* next, int32_t* status);
 };
 namespace rk { const KernelSet& kernels(); }  // real FP32 elements
+namespace rt { const KernelSet& kernels(); }  // real FP32 elements, tensor-core GEMMs (tile_policy 3)
 namespace ck { const KernelSet& kernels(); }  // complex64 elements
 namespace gr { const KernelSet& kernels(); }  // gauge-invariant plans, real FP32
 namespace gc { const KernelSet& kernels(); }  // gauge-invariant plans, complex64
 inline const KernelSet& kernels_of(const DevPlan& P) {
   if (P.gi) return P.es == 2 ? gc::kernels() : gr::kernels();
-  return P.es == 2 ? ck::kernels() : rk::kernels();
+  if (P.es == 2) return ck::kernels();
+  return P.tile_policy == 3 ? rt::kernels() : rk::kernels();
 }
 
 }  // namespace vmc
