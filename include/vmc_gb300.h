@@ -300,7 +300,8 @@ vmc_status vmc_peps_local_energy(const vmc_plan* plan, void* stream, const float
  *                                               are outputs; out_O, out_gap optional)
  *   VMC_JOB_LOCAL_ENERGY vmc_peps_local_energy (logamp, sign are inputs; out_E)
  * Fields a kind does not use are ignored.  Every plan of a batch has the same
- * element type and CTA size.  Each chain's results are bit-identical to the
+ * element type, CTA size and kernel (standard or gauge-invariant; tile policy 3
+ * or not), else VMC_ERR_UNSUPPORTED.  Each chain's results are bit-identical to the
  * single call's: the same device code runs every chain.  CTAs take
  * (job, chain) items from a device counter, jobs in decreasing order of cost
  * per chain, so the lattices that take longest start first.

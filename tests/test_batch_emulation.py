@@ -130,6 +130,12 @@ def test_malformed_batches_return_status_codes(emu_lib):
     # mixed element types
     assert run([good, ceng.amp_grad_job(ctens, ccfg)]) == _abi.VMC_ERR_UNSUPPORTED
     assert emu_lib.vmc_batch_workspace_size(_job_array([good, ceng.amp_grad_job(ctens, ccfg)]), 2) == 0
+    # the same lattice on the tensor-core kernel (tile policy 3) cannot share the launch
+    shape, D, chi, strategy, model, _ = JOBS[0]
+    teng = PEPSEngine(shape, D, chi, 2, strategy, operator=hamiltonian(model, shape), device="cpu", lib=emu_lib,
+                      options={"threads": 128, "smem_kb": -1, "tile_policy": 3})
+    assert run([good, teng.amp_grad_job(tens, cfg)]) == _abi.VMC_ERR_UNSUPPORTED
+    assert emu_lib.vmc_batch_workspace_size(_job_array([teng.amp_grad_job(tens, cfg)] * 2), 2) > 0
     # a sweep without uniforms, an unknown kind
     bad = eng.sweep_job(tens, cfg.clone(), u, eng.init_cache(tens, cfg.clone()))
     bad.uniforms = None
