@@ -193,7 +193,7 @@ def test_config2_shape_within_fp32_tolerance(emu_lib):
                                               ("ZipUp", 6, {"VMC_SMEM_KB": "0"}), ("Variational", 6, {}),
                                               ("NoTruncation", 16, {})])
 def test_stale_memory_never_reaches_the_results(emu_lib, strategy, chi, env, monkeypatch):
-    """Workspace, cache and (in this build, always) shared memory start as NaN: every value the
+    """Workspace, cache and (in the host-emulation build, always) shared memory start as NaN: every value the
     kernel reads must have been written first, so the outputs equal those of a zeroed run."""
     for k, v in env.items():
         monkeypatch.setenv(k, v)
