@@ -29,7 +29,7 @@ def _check(emu_lib, a, b):
 
 
 @pytest.mark.parametrize("cplx", [False, True])
-@pytest.mark.parametrize("m,n", [(7, 5), (5, 9), (12, 30), (30, 12), (1, 4), (4, 1), (40, 40)])
+@pytest.mark.parametrize("m,n", [(7, 5), (5, 9), (12, 30), (30, 12), (1, 4), (4, 1), (40, 40), (300, 60), (229, 100)])
 def test_matches_lapack_geqp3(emu_lib, m, n, cplx):
     rng = np.random.default_rng(m * 100 + n + cplx)
     a = _rand(rng, (m, n), cplx) * rng.uniform(0.1, 10.0, n)  # distinct column scales
