@@ -70,3 +70,23 @@ def test_shipped_table_is_the_fallback(emu_lib, tmp_path, monkeypatch):
     monkeypatch.setattr(at, "SHIPPED", shipped)
     assert tuned_options((3, 3), 2, 4, lib=emu_lib) == CANDIDATES[4]
     assert not (tmp_path / "empty.json").exists()  # nothing was tuned
+
+
+def test_shipped_table_entries_are_valid_candidates(emu_lib):
+    """Every winner in the shipped GB300 table is one of the candidates, and each candidate it lists was a
+    valid plan configuration (vmc_peps_plan_ex accepts it)."""
+    from vmc_gb300.autotune import SHIPPED
+
+    table = json.loads(SHIPPED.read_text())
+    assert table
+    shape = _abi.VmcShape(3, 3)
+    for key, entry in table.items():
+        assert entry["options"] in CANDIDATES, key
+        assert entry["samples_per_s"] == max(c["samples_per_s"] for c in entry["candidates"]), key
+        for cand in entry["candidates"]:
+            o = _abi.VmcPlanOptions(cand["options"]["threads"], cand["options"]["smem_kb"],
+                                    cand["options"]["tile_policy"])
+            plan = ct.c_void_p()
+            assert emu_lib.vmc_peps_plan_ex(ct.byref(shape), 2, 4, 2, 0, 1, 2, ct.byref(o), ct.byref(plan)) == \
+                _abi.VMC_OK, (key, cand)
+            emu_lib.vmc_plan_destroy(plan)
