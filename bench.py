@@ -234,15 +234,9 @@ def e2e_public_api(w, n, rank, dev, ustream, args, barrier, options=None):
 def shipped_options(w):
     """The launch configuration the shipped GB300 autotune table holds for this workload, or None (the
     engine's default) when the table has no entry for it."""
-    import json
+    from vmc_gb300 import autotune
 
-    import torch
-
-    from vmc_gb300.autotune import SHIPPED, _key
-
-    key = _key(torch.device("cuda"), w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype)
-    hit = json.loads(SHIPPED.read_text()).get(key)
-    return dict(hit["options"]) if hit else None
+    return autotune.shipped_options(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype)
 
 
 def unfused_rate(eng, tens, cfg, args, barrier):

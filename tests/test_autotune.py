@@ -90,3 +90,14 @@ def test_shipped_table_entries_are_valid_candidates(emu_lib):
             assert emu_lib.vmc_peps_plan_ex(ct.byref(shape), 2, 4, 2, 0, 1, 2, ct.byref(o), ct.byref(plan)) == \
                 _abi.VMC_OK, (key, cand)
             emu_lib.vmc_plan_destroy(plan)
+
+
+def test_shipped_options_lookup(monkeypatch):
+    from vmc_gb300 import autotune
+
+    assert autotune.shipped_options((8, 8), 4, 16, device="cpu") is None  # no table for the host build
+    monkeypatch.setattr(autotune, "_device_name", lambda device: "NVIDIA GB300")
+    table = json.loads(autotune.SHIPPED.read_text())
+    want = table["NVIDIA GB300|16x16|D6|chi48|d2|ZipUp|sweeps2|float32"]["options"]
+    assert autotune.shipped_options((16, 16), 6, 48, device="cpu") == want
+    assert autotune.shipped_options((5, 7), 3, 9, device="cpu") is None

@@ -20,7 +20,7 @@ from pathlib import Path
 import numpy as np
 import torch
 
-__all__ = ["CANDIDATES", "cache_path", "tune", "tuned_options"]
+__all__ = ["CANDIDATES", "cache_path", "shipped_options", "tune", "tuned_options"]
 
 # (threads, smem_kb, tile_policy); smem_kb -1 = the 52 KB default, 0 = all buffers in the slot
 CANDIDATES = [
@@ -145,6 +145,15 @@ def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="
         with _LOCK:
             _store(_key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype), entry)
     return entry
+
+
+def shipped_options(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32",
+                    device=None):
+    """The winner the shipped table holds for this problem on this GPU, or None (no tuning, no local cache)."""
+    device = torch.device(device if device is not None else "cuda")
+    hit = _load(SHIPPED).get(_key(device, (int(shape[0]), int(shape[1])), bond_dim, chi, phys_dim, strategy, n_sweeps,
+                                  dtype))
+    return dict(hit["options"]) if hit else None
 
 
 def tuned_options(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32", operator=None,
