@@ -89,26 +89,52 @@ const char* vmc_status_string(vmc_status s);
 vmc_status vmc_peps_plan(const vmc_shape* shape, int bond_dim, int chi, int phys_dim,
                          int dtype, int strategy, int n_sweeps, vmc_plan** out_plan);
 
+/* Arithmetic of a plan (vmc_plan_options.precision). */
+enum {
+  /* every contraction, truncation and stored tensor in FP32 */
+  VMC_PRECISION_FP32 = 0,
+  /* the boundary-MPS chain -- zip-up theta, its truncation and the stored
+   * boundary tensors that feed the next row's zip -- in FP64; environments,
+   * Metropolis ratios, gradients and energies in FP32.  Real ZipUp and
+   * NoTruncation plans.  Truncated amplitudes are ill-conditioned (the kept
+   * subspace moves by the relative perturbation of theta divided by the
+   * relative singular-value gap at the cut), so FP32 storage on the chain
+   * alone puts the batch-mean energy ~1e-4 off the FP64 result at 8x8, D=4,
+   * chi=16; this tier brings it to ~1e-7. */
+  VMC_PRECISION_MIXED = 1
+};
+
 /*
- * Launch configuration of a plan -- what the autotuner (vmc_gb300.autotune)
- * picks per (lattice, D, chi, dtype, strategy).  No reference counterpart
- * (XLA picks its own kernels).  Every choice computes the same quantities;
- * they differ in FP32 rounding only (GEMM and reduction order).
+ * Options of a plan -- the launch configuration the autotuner
+ * (vmc_gb300.autotune) picks per (lattice, D, chi, dtype, strategy), and the
+ * arithmetic.  No reference counterpart (XLA picks its own kernels).  A
+ * zero-initialised struct except smem_kb = -1 gives the defaults, which is
+ * what vmc_peps_plan uses; nothing is read from the environment.
  *   threads      CTA size, a multiple of 32 in [64, 256]; 0: 128
  *   smem_kb      dynamic shared memory per CTA for the truncation arena and
- *                the 1-row intermediates, 0..52 KB; -1: 52 (0: all in the
- *                CTA's workspace slot, L1-cached)
+ *                the 1-row intermediates, 0..52 KB (FP32) or 0..200 KB
+ *                (mixed precision); -1: the precision's default (0: all in
+ *                the CTA's workspace slot, L1-cached)
  *   tile_policy  register tiles of the CTA GEMMs: 0 default, 1 smaller, 2 larger, 3 real GEMMs of at
  *                least 16 x 8 x 8 on the tensor cores (3xTF32, FP32 accuracy; faster from D = 6, chi = 36
  *                on), the rest as 0
- * vmc_peps_plan uses the defaults, overridden by the VMC_THREADS, VMC_SMEM_KB
- * and VMC_TILE_POLICY environment variables when set; vmc_peps_plan_ex with
- * options ignores the environment.
+ *   precision    VMC_PRECISION_FP32 or VMC_PRECISION_MIXED
+ *   trunc_method 0: Gram matrix + tridiagonal eigensolver; 1: one-sided
+ *                Jacobi on theta (real FP32 plans; a cross-check of 0)
+ *   vchunk       bond values per vertical-energy chunk; 0: all at once
+ *   vert_smem    1: vertical-energy buffers in the shared-memory arena,
+ *                chunked to fit; 0: in the workspace slot
+ * Every choice but precision computes the same quantities and differs in
+ * FP32 rounding only (GEMM and reduction order).
  */
 typedef struct {
   int threads;
   int smem_kb;
   int tile_policy;
+  int precision;
+  int trunc_method;
+  int vchunk;
+  int vert_smem;
 } vmc_plan_options;
 vmc_status vmc_peps_plan_ex(const vmc_shape* shape, int bond_dim, int chi, int phys_dim, int dtype,
                             int strategy, int n_sweeps, const vmc_plan_options* options,
@@ -263,9 +289,15 @@ vmc_status vmc_peps_amp_grad(const vmc_plan* plan, void* stream, const float* te
  * launched.  Chains are then processed by as many CTAs as fit, so results are
  * identical to vmc_peps_amp_grad's but throughput drops for large plans.
  *
+ * The array is a static device variable of this library: it takes 64 MiB of
+ * device memory in every CUDA context that loads the library, whether or not
+ * this entry point is ever called.
+ *
  * The first call on a device looks up the array's address on the current
  * device (cudaGetSymbolAddress) and caches it; make that first call before any
- * stream capture begins.  Nothing in the scratch needs to start at zero: the
+ * stream capture begins.  The cached address belongs to the device's primary
+ * context: after cudaDeviceReset (or anything else that destroys and recreates
+ * that context) the process must not call this entry point again.  Nothing in the scratch needs to start at zero: the
  * kernels write every word before reading it.  All calls on a device share
  * the one array, so calls that overlap in time (different streams or threads)
  * race on it and corrupt each other's results: serialise them.  The call
@@ -342,6 +374,22 @@ typedef struct {
 size_t vmc_batch_workspace_size(const vmc_peps_job* jobs, int n_jobs);
 vmc_status vmc_peps_batch(const vmc_peps_job* jobs, int n_jobs, void* stream, void* workspace,
                           size_t workspace_bytes, int32_t* status_dev);
+
+/*
+ * The same batch with an explicit buffer placement.  Shared memory and L1
+ * share one array per SM, so a batch runs all its plans either with their
+ * own placement (VMC_BATCH_LAYOUT_PLAN: truncation arena and 1-row
+ * intermediates in shared memory where they fit) or with every buffer in
+ * the CTA's workspace slot (VMC_BATCH_LAYOUT_SLOT), which leaves the whole
+ * array to L1 for plans too large for shared memory.  VMC_BATCH_LAYOUT_AUTO
+ * (what vmc_peps_batch does) takes the slot placement when plans whose arena
+ * lives in the slot carry more than half of the batch's work.  The placement
+ * moves data, not arithmetic: results are the same bits either way.
+ */
+enum { VMC_BATCH_LAYOUT_AUTO = -1, VMC_BATCH_LAYOUT_PLAN = 0, VMC_BATCH_LAYOUT_SLOT = 1 };
+size_t vmc_batch_workspace_size_ex(const vmc_peps_job* jobs, int n_jobs, int layout);
+vmc_status vmc_peps_batch_ex(const vmc_peps_job* jobs, int n_jobs, int layout, void* stream, void* workspace,
+                             size_t workspace_bytes, int32_t* status_dev);
 
 /*
  * Column-pivoted Householder QR, A P = Q R, in FP64 (complex_elements = 0) or

@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import numpy as np
+import torch
 
 from oracle import peps as oracle
 from vmc_gb300.operators import heisenberg, transverse_field_ising
@@ -89,3 +90,37 @@ def assert_parity(rel_errors, truncating, median_tol=TRUNC_MEDIAN_TOL, max_tol=T
     else:
         assert np.median(rel_errors) < median_tol, np.median(rel_errors)
         assert np.max(rel_errors) < max_tol, np.max(rel_errors)
+
+
+# Accuracy bars against the FP64 oracle for the mixed-precision tier (FP64
+# boundary-MPS chain, FP32 contractions elsewhere).  "E" is the batch-mean
+# local energy; its error is taken relative to the energy scale mean|E_loc|,
+# because for a random PEPS the batch mean itself sits near zero (8x8 D=4:
+# mean 0.33 against mean|E_loc| 15), which would inflate a plain relative
+# error by the cancellation.  "O" is the Frobenius norm over the batch.
+E_BAR = 1e-5
+O_BAR = 1e-4
+# FP64 chain: the amplitude is the FP64 contraction of FP64 boundary tensors
+MIXED_AMP_TOL = 1e-9
+
+
+def accuracy(res, c2, ctx, le):
+    """Errors of one engine sweep against the oracle's, over the chains whose configurations agree."""
+    cfg = res.configs.cpu().numpy()
+    same = np.all(cfg == c2, axis=1)
+    amp = (res.sign * torch.exp(res.logamp)).cpu().numpy()
+    ra = np.abs(amp[same] / ctx.amp[same] - 1)
+    e, e_ref = res.E.cpu().numpy()[same], le.local_estimate[same]
+    o, o_ref = res.O.cpu().numpy()[same], le.local_log_derivatives[same]
+    de = np.abs(e - e_ref)
+    return {
+        "chains": int(len(cfg)), "same_configs": float(same.mean()),
+        "logpsi_abs_max": float(np.max(np.abs(np.log1p(amp[same] / ctx.amp[same] - 1)))),
+        "amp_rel_median": float(np.median(ra)), "amp_rel_max": float(np.max(ra)),
+        "eloc_rel_median": float(np.median(de / np.maximum(1.0, np.abs(e_ref)))),
+        "eloc_rel_max": float(np.max(de / np.maximum(1.0, np.abs(e_ref)))),
+        "e_mean_scaled": float(abs(e.mean() - e_ref.mean()) / np.abs(e_ref).mean()),
+        "e_mean_rel": float(abs(e.mean() - e_ref.mean()) / abs(e_ref.mean())),
+        "o_frob": float(np.linalg.norm(o - o_ref) / np.linalg.norm(o_ref)),
+        "min_gap": float(np.min(res.gap.cpu().numpy())) if res.gap is not None else None,
+    }

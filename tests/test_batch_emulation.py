@@ -174,15 +174,14 @@ def test_recomputing_sweeps_equal_init_cache_then_sweep(emu_lib, full):
 
 
 @pytest.mark.parametrize("layout", ["slot", "shared"])
-def test_either_batch_layout_gives_the_single_call_bits(emu_lib, layout, monkeypatch):
+def test_either_batch_layout_gives_the_single_call_bits(emu_lib, layout):
     """The batch runs every plan either with its shared-memory buffer placement or with all buffers
     in the CTA slot (chosen by cost share); the placement moves data, not arithmetic."""
-    monkeypatch.setenv("VMC_BATCH_LAYOUT", layout)
     cases = [_setup(emu_lib, spec, seed=80 + i) for i, spec in enumerate(JOBS)]
     refs, jobs = [], []
     for eng, tens, cfg, u in cases:
         cache = eng.init_cache(tens, cfg.clone())
         refs.append(eng.sweep(tens, cfg.clone(), u, cache.clone()))
         jobs.append(eng.sweep_job(tens, cfg.clone(), u, cache))
-    for ref, out in zip(refs, PEPSBatch().run(jobs)):
+    for ref, out in zip(refs, PEPSBatch().run(jobs, layout=layout)):
         _assert_same_bits(ref, out)

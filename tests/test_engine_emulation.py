@@ -19,8 +19,8 @@ from vmc_gb300.lowering import pack_tensors
 from vmc_gb300.operators import LocalHamiltonian, OneSiteTerm, HorizontalTwoSiteTerm, VerticalTwoSiteTerm, DiagonalTerm
 
 
-def _engine(emu_lib, shape, D, chi, strategy, H, d=2):
-    return PEPSEngine(shape, D, chi, d, strategy, operator=H, device="cpu", lib=emu_lib)
+def _engine(emu_lib, shape, D, chi, strategy, H, d=2, options=None):
+    return PEPSEngine(shape, D, chi, d, strategy, operator=H, device="cpu", lib=emu_lib, options=options)
 
 
 def _sweep(eng, T, cfg, u, full=False, deltas=None):
@@ -106,17 +106,15 @@ def test_amp_grad_and_local_energy_match_oracle(emu_lib):
     assert_parity(np.abs(e - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
 
 
-@pytest.mark.parametrize("env", [{"VMC_VCHUNK": "1", "VMC_VERT_SMEM": "1"}, {"VMC_TRUNCATION": "jacobi"}, {"VMC_SMEM_KB": "0"},
-                                 {"VMC_SMEM_KB": "24"}, {"VMC_TILE_POLICY": "1"}, {"VMC_TILE_POLICY": "2"}],
+@pytest.mark.parametrize("opts", [{"vchunk": 1, "vert_smem": 1}, {"trunc_method": "jacobi"}, {"smem_kb": 0},
+                                  {"smem_kb": 24}, {"tile_policy": 1}, {"tile_policy": 2}],
                          ids=["chunk1", "jacobi", "all-global", "mat-global", "small-tiles", "large-tiles"])
-def test_alternative_engine_paths_match_oracle(emu_lib, env, monkeypatch):
+def test_alternative_engine_paths_match_oracle(emu_lib, opts):
     """Chunked vertical energy, the Jacobi truncation and the global-memory fallbacks agree with the oracle."""
-    for k, v in env.items():
-        monkeypatch.setenv(k, v)
     shape, D, chi = (4, 4), 3, 6
     H = hamiltonian("heisenberg", shape)
     T, cfg, u = make_case(shape, D, 4, seed=21)
-    eng = _engine(emu_lib, shape, D, chi, "ZipUp", H)
+    eng = _engine(emu_lib, shape, D, chi, "ZipUp", H, options=opts)
     res, _, _ = _sweep(eng, T, cfg, u)
     c2, ctx, le = oracle_sweep(fp32(T), shape, D, "ZipUp", chi, H, cfg, u)
     assert np.array_equal(res.configs.numpy(), c2)
@@ -189,21 +187,21 @@ def test_config2_shape_within_fp32_tolerance(emu_lib):
         assert abs(res.E.numpy()[i] - le.local_estimate[i]) < tol * max(1.0, abs(le.local_estimate[i])) * 10
 
 
-@pytest.mark.parametrize("strategy,chi,env", [("ZipUp", 6, {}), ("ZipUp", 6, {"VMC_TRUNCATION": "jacobi"}),
-                                              ("ZipUp", 6, {"VMC_SMEM_KB": "0"}), ("Variational", 6, {}),
-                                              ("NoTruncation", 16, {})])
-def test_stale_memory_never_reaches_the_results(emu_lib, strategy, chi, env, monkeypatch):
+@pytest.mark.parametrize("strategy,chi,opts", [("ZipUp", 6, None), ("ZipUp", 6, {"trunc_method": "jacobi"}),
+                                               ("ZipUp", 6, {"smem_kb": 0}), ("Variational", 6, None),
+                                               ("NoTruncation", 16, None), ("ZipUp", 6, {"precision": "mixed"}),
+                                               ("ZipUp", 6, {"precision": "mixed", "smem_kb": 200}),
+                                               ("NoTruncation", 16, {"precision": "mixed"})])
+def test_stale_memory_never_reaches_the_results(emu_lib, strategy, chi, opts):
     """Workspace, cache and (in the host-emulation build, always) shared memory start as NaN: every value the
     kernel reads must have been written first, so the outputs equal those of a zeroed run."""
-    for k, v in env.items():
-        monkeypatch.setenv(k, v)
     shape, D = (4, 4), 3
     H = hamiltonian("heisenberg", shape)
     T, cfg, u = make_case(shape, D, 4, seed=11)
     tens = torch.from_numpy(pack_tensors(T))
     outs = []
     for fill in (0.0, float("nan")):
-        eng = _engine(emu_lib, shape, D, chi, strategy, H)
+        eng = _engine(emu_lib, shape, D, chi, strategy, H, options=opts)
         ws = eng.workspace(cfg.shape[0])
         ws[: (ws.numel() // 4) * 4].view(torch.float32).fill_(fill)
         cache = eng.new_cache(cfg.shape[0])

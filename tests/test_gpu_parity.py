@@ -33,8 +33,8 @@ CASES = [
 ]
 
 
-def _run(device, shape, D, chi, strategy, H, T, cfg, u, full=False):
-    eng = PEPSEngine(shape, D, chi, 2, strategy, operator=H, device=device)
+def _run(device, shape, D, chi, strategy, H, T, cfg, u, full=False, options=None):
+    eng = PEPSEngine(shape, D, chi, 2, strategy, operator=H, device=device, options=options)
     tens = torch.from_numpy(pack_tensors(T)).to(device)
     c = torch.from_numpy(cfg.copy()).to(device)
     cache = eng.init_cache(tens, c)
@@ -116,16 +116,14 @@ def test_amp_grad_and_local_energy_match_oracle(cuda_device):
     assert_parity(np.abs(e.cpu().numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref)), True)
 
 
-@pytest.mark.parametrize("env", [{"VMC_VCHUNK": "1", "VMC_VERT_SMEM": "1"}, {"VMC_TRUNCATION": "jacobi"}, {"VMC_SMEM_KB": "0"},
-                                 {"VMC_SMEM_KB": "24"}, {"VMC_THREADS": "256", "VMC_SMEM_KB": "96"}],
+@pytest.mark.parametrize("opts", [{"vchunk": 1, "vert_smem": 1}, {"trunc_method": "jacobi"}, {"smem_kb": 0},
+                                  {"smem_kb": 24}, {"threads": 256, "smem_kb": 96}],
                          ids=["chunk1", "jacobi", "all-global", "mat-global", "256-threads"])
-def test_alternative_engine_paths(cuda_device, env, monkeypatch):
-    for k, v in env.items():
-        monkeypatch.setenv(k, v)
+def test_alternative_engine_paths(cuda_device, opts):
     shape, D, chi = (4, 4), 3, 6
     H = hamiltonian("heisenberg", shape)
     T, cfg, u = make_case(shape, D, 32, seed=21)
-    res = _run(cuda_device, shape, D, chi, "ZipUp", H, T, cfg, u)
+    res = _run(cuda_device, shape, D, chi, "ZipUp", H, T, cfg, u, options=opts)
     c2, ctx, le = oracle_sweep(fp32(T), shape, D, "ZipUp", chi, H, cfg, u)
     _compare(res, c2, ctx, le, True)
 

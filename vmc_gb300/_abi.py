@@ -20,6 +20,9 @@ VMC_ERR_SCRATCH = 7
 VMC_DTYPE_F32 = 0
 VMC_DTYPE_C64 = 1
 
+VMC_PRECISION_FP32 = 0
+VMC_PRECISION_MIXED = 1
+
 VMC_STRATEGY_NO_TRUNCATION = 0
 VMC_STRATEGY_ZIP_UP = 1
 VMC_STRATEGY_DENSITY_MATRIX = 2
@@ -33,6 +36,9 @@ VMC_JOB_SWEEP = 1
 VMC_JOB_AMP_GRAD = 2
 VMC_JOB_LOCAL_ENERGY = 3
 VMC_MAX_BATCH_JOBS = 16
+VMC_BATCH_LAYOUT_AUTO = -1
+VMC_BATCH_LAYOUT_PLAN = 0
+VMC_BATCH_LAYOUT_SLOT = 1
 
 
 class VmcShape(ct.Structure):
@@ -45,8 +51,25 @@ _SZ = ct.c_size_t
 
 
 class VmcPlanOptions(ct.Structure):
-    """vmc_plan_options: a plan's launch configuration."""
-    _fields_ = [("threads", _I), ("smem_kb", _I), ("tile_policy", _I)]
+    """vmc_plan_options: a plan's launch configuration and arithmetic."""
+    _fields_ = [("threads", _I), ("smem_kb", _I), ("tile_policy", _I), ("precision", _I), ("trunc_method", _I),
+                ("vchunk", _I), ("vert_smem", _I)]
+
+
+PRECISIONS = {"fp32": VMC_PRECISION_FP32, "mixed": VMC_PRECISION_MIXED}
+TRUNC_METHODS = {"gram": 0, "jacobi": 1}
+
+
+def plan_options(options) -> VmcPlanOptions:
+    """A vmc_plan_options from a dict (threads, smem_kb, tile_policy, precision, trunc_method, vchunk,
+    vert_smem); precision is "fp32" / "mixed" (or 0 / 1), trunc_method "gram" / "jacobi" (or 0 / 1)."""
+    o = dict(options)
+    prec = o.get("precision", VMC_PRECISION_FP32)
+    prec = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
+    tm = o.get("trunc_method", 0)
+    tm = TRUNC_METHODS[tm] if isinstance(tm, str) else int(tm)
+    return VmcPlanOptions(int(o.get("threads", 0)), int(o.get("smem_kb", -1)), int(o.get("tile_policy", 0)), prec,
+                          tm, int(o.get("vchunk", 0)), int(o.get("vert_smem", 0)))
 
 
 class VmcPepsJob(ct.Structure):
@@ -80,6 +103,8 @@ SIGNATURES = {
     "vmc_peps_local_energy": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _P]),
     "vmc_batch_workspace_size": (_SZ, [ct.POINTER(VmcPepsJob), _I]),
     "vmc_peps_batch": (_I, [ct.POINTER(VmcPepsJob), _I, _P, _P, _SZ, _P]),
+    "vmc_batch_workspace_size_ex": (_SZ, [ct.POINTER(VmcPepsJob), _I, _I]),
+    "vmc_peps_batch_ex": (_I, [ct.POINTER(VmcPepsJob), _I, _I, _P, _P, _SZ, _P]),
     "vmc_uniforms": (_I, [_P, _P, ct.c_int64, ct.c_uint64, _P]),
     "vmc_qr_pivoted_workspace_size": (_SZ, [_I]),
     "vmc_qr_pivoted": (_I, [_P, _I, _P, ct.c_int64, _I, _I, _I, _P, _P, _P, _SZ]),

@@ -1,0 +1,262 @@
+// chain_f64.cuh -- the boundary-MPS chain of mixed-precision plans in FP64.
+//
+// Included by peps_device.cuh inside the real-element namespace of the
+// mixed-precision kernel (VMC_CHAIN_F64).  Every tensor a boundary MPS is
+// built from -- the zip-up carry, theta = carry . m . w, its Gram matrix, the
+// eigensolver, the kept vectors and the stored boundary tensors that feed the
+// next row's zip -- is FP64.  Each new boundary tensor is also written as an
+// FP32 copy for the environments, Metropolis ratios, gradients and energies,
+// which stay FP32.
+//
+// Why: ZipUp keeps the top-chi singular subspace of theta at every cut
+// (strategy.py:128-150).  At 8x8, D=4, chi=16 the relative gap
+// (s_chi - s_chi+1) / s_chi at the smallest cut of a sample is below 1e-2 for
+// nearly every sample and reaches 2e-4, and the kept subspace moves by the
+// relative perturbation of theta divided by that gap.  FP32 storage of any
+// tensor on the chain perturbs theta by ~6e-8 and moves amplitudes and
+// energies by up to 1e-2; with the chain in FP64 and everything else FP32 the
+// error against the FP64 oracle falls to ~1e-7 in the batch-mean energy.
+#pragma once
+
+struct ArenaD {
+  double* mat;
+  double* G;
+  double* Y;
+  EigScratchT<double> eig;
+};
+
+// Layout mirrored by arena_doubles() in peps_plan.cuh.
+__device__ inline ArenaD make_arena_d(const DevPlan& P, double* p) {
+  ArenaD a;
+  const int nmax = P.nmax, ld = P.nmax | 1, kmax = P.kmax;
+  a.mat = p; p += al32((long long)nmax * ld);
+  a.G = p; p += al32((long long)nmax * ld);
+  a.Y = p; p += al32((long long)nmax * kmax);
+  a.eig.S = p; p += al32((long long)kmax * kmax);
+  a.eig.lu = p; p += al32(4LL * kmax * nmax);
+  a.eig.sw = reinterpret_cast<unsigned char*>(p); p += al32(((long long)kmax * nmax + 7) / 8);
+  a.eig.d = p; p += al32(nmax);
+  a.eig.e = p; p += al32(nmax);
+  a.eig.e2 = p; p += al32(nmax);
+  a.eig.tau = p; p += al32(nmax);
+  a.eig.v = p; p += al32(nmax);
+  a.eig.p = p; p += al32(nmax);
+  a.eig.lam = p; p += al32(nmax + 1);
+  a.eig.cvec = p; p += al32(2LL * nmax);
+  a.eig.part = p; p += al32(nmax + 64);
+  a.eig.flag = reinterpret_cast<int*>(p); p += 32;
+  a.eig.yr = nullptr;
+  return a;
+}
+
+// FP64 counterpart of cta_normalize: rescale x[0..n) by the power of two that
+// brings max|x| into [0.5, 1); returns the log of the factor taken out.
+__device__ inline double cta_normalize_d(double* x, int n, double* red) {
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[i]));
+#ifndef VMC_HOST_EMULATION
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+#endif
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = m;
+  __syncthreads();
+  m = 0.0;
+  for (int w = 0; w < nw; ++w) m = fmax(m, red[w]);
+  __syncthreads();
+  if (!(m > 0.0) || !isfinite(m)) return 0.0;
+  int e = 0;
+  frexp(m, &e);
+  e = e < -1000 ? -1000 : (e > 1000 ? 1000 : e);
+  if (e == 0) return 0.0;
+  const double sc = ldexp(1.0, -e);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= sc;
+  __syncthreads();
+  return (double)e * 0.69314718055994530942;
+}
+
+// dst32[i] = (float)src[i]: the FP32 copy a boundary tensor's consumers read.
+__device__ inline void cta_round_copy(float* dst, const double* src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = (float)src[i];
+  __syncthreads();
+}
+
+__device__ inline void fill_ones_row_d(const DevPlan& P, double* row) {
+  for (int c = threadIdx.x; c < P.C; c += blockDim.x) row[(size_t)c * P.TS] = 1.0;
+  __syncthreads();
+}
+
+// The FP64 buffers of one chain's boundary-MPS chain: rows, carries and Z1
+// carved from the slot's FP64 region (layout mirrored by chain_f64_doubles()
+// in peps_plan.cuh), the arena at `arena` (shared memory or the slot's arena
+// region).
+struct ChainD {
+  double* row[2];  // current and next boundary MPS (C tensors at stride TS)
+  double* carry[2];
+  double* z1;
+  ArenaD ar;
+};
+
+__device__ inline ChainD make_chain_d(const DevPlan& P, double* p, double* arena) {
+  ChainD c;
+  for (int i = 0; i < 2; ++i) { c.row[i] = p; p += al32((long long)P.C * P.TS); }
+  for (int i = 0; i < 2; ++i) { c.carry[i] = p; p += al32(P.SCR); }
+  c.z1 = p;
+  c.ar = make_arena_d(P, arena);
+  return c;
+}
+
+// Boundary-MPS row application (strategy.py:118-150, contraction.py:59-65) in
+// FP64: src and dst hold C tensors at stride TS; dst32 receives the FP32
+// copy of dst.  Returns the sum of the log-norms divided out of the new
+// tensors.  *min_gap receives the smallest relative eigen-gap
+// (l_k - l_{k+1}) / l_k of theta theta^T at a truncating cut.  ZipUp and
+// NoTruncation.
+__device__ __noinline__ double apply_row_hp(const DevPlan& P, Shared& sh, const float* perm, const double* src,
+                                            const int* bin, double* dst, float* dst32, const int* bout, int row,
+                                            const int* spins, bool from_below, const ChainD& ch, float* min_gap) {
+  const int C = P.C;
+  const ArenaD& ar = ch.ar;
+  double logsum = 0.0;
+  double* carry = ch.carry[0];
+  double* carry_next = ch.carry[1];
+  double* Z1 = ch.z1;
+  if (threadIdx.x == 0) carry[0] = 1.0;
+  __syncthreads();
+  int kc = 1;
+  for (int c = 0; c < C; ++c) {
+    const int s = site_id(P, row, c);
+    const int U = P.sdim[4 * s], V = P.sdim[4 * s + 1], Lb = P.sdim[4 * s + 2], Rb = P.sdim[4 * s + 3];
+    const int pin = from_below ? V : U;
+    const int pout = from_below ? U : V;
+    const float* Ap = perm_of(P, perm, s, from_below ? P_ZIPB : P_ZIPT, spins[c]);
+    const int din = bin[c], dn = bin[c + 1];
+    const double* m = src + (size_t)c * P.TS;
+    double* out = dst + (size_t)c * P.TS;
+    float* out32 = dst32 + (size_t)c * P.TS;
+    if (P.strategy == VMC_STRATEGY_NO_TRUNCATION) {
+      // out[d][l][q][r'][w] = sum_p m[d][p][r'] A(p, q, l, w)
+      const int ncol = dn * Rb;
+      cta_gemm_x(make_gemm_x(m, two(dn, pin * dn, 1), dn, Ap, three(pout, Rb, pin * pout * Rb, Rb, 1), pout * Rb,
+                             out, two(dn, Lb * pout * ncol, Rb), three(pout, Rb, pout * ncol, ncol, 1), din * dn,
+                             Lb * pout * Rb, pin));
+      const int n_el = din * Lb * pout * ncol;
+      logsum += cta_normalize_d(out, n_el, sh.red);
+      cta_round_copy(out32, out, n_el);
+      continue;
+    }
+    // Z1[k][l][p][r'] = sum_d carry[k][l][d] m[d][p][r']
+    cta_gemm_x(make_gemm_x(static_cast<const double*>(carry), lin(din), 1, m, lin(1), pin * dn, Z1, lin(pin * dn),
+                           lin(1), kc * Lb, pin * dn, din));
+    const int mrows = kc * pout;
+    const int ncols = dn * Rb;
+    if (c == C - 1) {
+      // last site: untruncated, out[k][q][(r',w)]
+      cta_gemm_x(make_gemm_x(static_cast<const double*>(Z1), two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb,
+                             out, two(dn, pout * ncols, Rb), two(Rb, ncols, 1), kc * dn, pout * Rb, Lb * pin));
+      const int n_el = mrows * ncols;
+      logsum += cta_normalize_d(out, n_el, sh.red);
+      cta_round_copy(out32, out, n_el);
+      break;
+    }
+    const int kout = bout[c + 1];
+    // theta as a row-major matrix: mat[(k,q)][(r',w)], odd leading dimension
+    const int ldm = ncols | 1;
+    double* mat = ar.mat;
+    cta_gemm_x(make_gemm_x(static_cast<const double*>(Z1), two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat,
+                           two(dn, pout * ldm, Rb), two(Rb, ldm, 1), kc * dn, pout * Rb, Lb * pin));
+    if (mrows <= ncols && kout >= mrows) {
+      // every row direction is kept: U = I, carry = theta
+      for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) out[e] = (e / mrows == e % mrows) ? 1.0 : 0.0;
+      for (int e = threadIdx.x; e < mrows * ncols; e += blockDim.x) {
+        const int i = e / ncols, col = e % ncols;
+        carry_next[(size_t)i * ncols + (col % Rb) * dn + col / Rb] = mat[(size_t)i * ldm + col];
+      }
+      __syncthreads();
+    } else if (mrows > ncols && kout >= ncols) {
+      // every column is kept: U = Q of the leading kout columns (an orthonormal basis of the column
+      // space, exact for rank-deficient theta), carry = Q^T theta
+      cta_householder_q<double>(mat, mrows, kout, ldm, 1, out, kout, 1, ar.G, kout | 1, ar.eig.tau);
+      cta_gemm_x(make_gemm_x(static_cast<const double*>(out), lin(1), kout, static_cast<const double*>(mat), lin(1),
+                             ldm, carry_next, lin(ncols), two(Rb, 1, dn), kout, ncols, mrows));
+    } else {
+      // ---- Gram + tridiagonal eigensolver on the smaller side, all FP64 ----
+      const bool rows_side = mrows <= ncols;
+      const int nG = rows_side ? mrows : ncols;
+      const int ldg = nG | 1;
+      const double* cm = mat;
+      if (rows_side)  // G = theta theta^T
+        cta_gemm_x(make_gemm_x(cm, lin(ldm), 1, cm, lin(ldm), 1, ar.G, lin(ldg), lin(1), nG, nG, ncols));
+      else  // G = theta^T theta
+        cta_gemm_x(make_gemm_x(cm, lin(1), ldm, cm, lin(1), ldm, ar.G, lin(ldg), lin(1), nG, nG, mrows));
+      cta_sym_topk<double>(ar.G, nG, ldg, kout, ar.Y, kout, ar.eig, sh.red);
+      if (threadIdx.x == 0 && kout < nG) {
+        const double lk = ar.eig.lam[kout - 1], lk1 = ar.eig.lam[kout];
+        const float gap = lk > 0.0 ? (float)((lk - lk1) / lk) : 0.f;
+        if (gap < *min_gap) *min_gap = gap;
+      }
+      if (rows_side) {
+        for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) out[e] = ar.Y[e];
+        __syncthreads();
+      } else {
+        // U = theta V / |theta V| column-wise
+        cta_gemm_x(make_gemm_x(cm, lin(ldm), 1, static_cast<const double*>(ar.Y), lin(1), kout, out, lin(kout),
+                               lin(1), mrows, kout, ncols));
+        double* nrm = ar.eig.cvec;
+        for (int t = threadIdx.x; t < kout; t += blockDim.x) {
+          double a = 0.0;
+          for (int i = 0; i < mrows; ++i) a = fma(out[(size_t)i * kout + t], out[(size_t)i * kout + t], a);
+          nrm[t] = a;
+        }
+        __syncthreads();
+        double smax = 0.0;
+        for (int t = 0; t < kout; ++t) smax = fmax(smax, nrm[t]);
+        for (int e = threadIdx.x; e < mrows * kout; e += blockDim.x) {
+          const double s2 = nrm[e % kout];
+          out[e] *= (s2 > 1e-60 * smax && s2 > 0.0) ? 1.0 / sqrt(s2) : 0.0;
+        }
+        __syncthreads();
+      }
+      // carry'[k'][w][r'] = sum_i U[i][k'] theta[i][(r',w)]
+      cta_gemm_x(make_gemm_x(static_cast<const double*>(out), lin(1), kout, cm, lin(1), ldm, carry_next, lin(ncols),
+                             two(Rb, 1, dn), kout, ncols, mrows));
+    }
+    logsum += cta_normalize_d(carry_next, kout * ncols, sh.red);
+    logsum += cta_normalize_d(out, mrows * kout, sh.red);
+    cta_round_copy(out32, out, mrows * kout);
+    double* t = carry;
+    carry = carry_next;
+    carry_next = t;
+    kc = kout;
+  }
+  return logsum;
+}
+
+// contract_bottom (contraction.py:30-35) of an FP64 boundary row: log|psi|
+// and *sign_or_phase the sign.  One thread, FP64.
+__device__ __noinline__ double contract_bottom_d(const DevPlan& P, const double* row, const int* bonds, Shared& sh,
+                                                 double* tmp, double* sign_out) {
+  if (threadIdx.x == 0) {
+    double* v = tmp;
+    double* w = tmp + kMaxVec;
+    v[0] = 1.0;
+    for (int c = 0; c < P.C; ++c) {
+      const int l = bonds[c], r = bonds[c + 1];
+      const double* t = row + (size_t)c * P.TS;
+      for (int j = 0; j < r; ++j) {
+        double a = 0.0;
+        for (int i = 0; i < l; ++i) a = fma(v[i], t[(size_t)i * r + j], a);
+        w[j] = a;
+      }
+      for (int j = 0; j < r; ++j) v[j] = w[j];
+    }
+    sh.bcast[0] = v[0];
+  }
+  __syncthreads();
+  const double vr = sh.bcast[0];
+  __syncthreads();
+  *sign_out = vr < 0 ? -1.0 : 1.0;
+  return vr == 0.0 ? -INFINITY : log(fabs(vr));
+}

@@ -329,6 +329,114 @@ __device__ inline Gemm make_gemm(const float* A, IMap am, int sak, const float* 
 }
 
 // ---------------------------------------------------------------------------
+// FP64-accumulating CTA GEMM for the boundary-MPS chain of mixed-precision
+// plans: A is FP64, B is FP64 or FP32 (the site tensors), C is FP64.  Same
+// index maps and thread-tile interleaving as the FP32 GEMM above.
+// ---------------------------------------------------------------------------
+template <typename TA, typename TB>
+struct GemmX {
+  const TA* A;
+  const TB* B;
+  double* C;
+  int M, N, K;
+  IMap am;
+  int sak;
+  IMap bn;
+  int sbk;
+  IMap cm, cn;
+  double alpha;
+  int accumulate;
+};
+
+template <typename TA, typename TB>
+__device__ inline GemmX<TA, TB> make_gemm_x(const TA* A, IMap am, int sak, const TB* B, IMap bn, int sbk,
+                                             double* C, IMap cm, IMap cn, int M, int N, int K, double alpha = 1.0,
+                                             int accumulate = 0) {
+  GemmX<TA, TB> g;
+  g.A = A; g.B = B; g.C = C; g.M = M; g.N = N; g.K = K;
+  g.am = am; g.sak = sak; g.bn = bn; g.sbk = sbk; g.cm = cm; g.cn = cn;
+  g.alpha = alpha; g.accumulate = accumulate;
+  return g;
+}
+
+template <typename TA, typename TB, int TM, int TN>
+__device__ __forceinline__ void gemm_tiles_x(const GemmX<TA, TB>& g) {
+  const int tiles_m = (g.M + TM - 1) / TM;
+  const int tiles_n = (g.N + TN - 1) / TN;
+  const int n_tiles = tiles_m * tiles_n;
+  for (int t = threadIdx.x; t < n_tiles; t += blockDim.x) {
+    const int tn = t % tiles_n;
+    const int tm = t / tiles_n;
+    int aoff[TM], boff[TN];
+    bool mv[TM], nv[TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      int m = tm + i * tiles_m;
+      mv[i] = m < g.M;
+      aoff[i] = imap(g.am, mv[i] ? m : 0);
+    }
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      int n = tn + j * tiles_n;
+      nv[j] = n < g.N;
+      boff[j] = imap(g.bn, nv[j] ? n : 0);
+    }
+    double acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) acc[i][j] = 0.0;
+    for (int k = 0; k < g.K; ++k) {
+      double a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = (double)g.A[aoff[i] + k * g.sak];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = (double)g.B[boff[j] + k * g.sbk];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      if (!mv[i]) continue;
+      const int co = imap(g.cm, tm + i * tiles_m);
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        if (!nv[j]) continue;
+        double* dst = g.C + co + imap(g.cn, tn + j * tiles_n);
+        const double v = g.alpha * acc[i][j];
+        *dst = g.accumulate ? (*dst + v) : v;
+      }
+    }
+  }
+}
+
+// CTA-wide FP64 GEMM; ends with a barrier.
+template <typename TA, typename TB>
+__device__ inline void cta_gemm_x(const GemmX<TA, TB>& g) {
+  const int work = g.M * g.N;
+  const int nt = blockDim.x;
+  if (g.M >= 4 && g.N >= 4 && work >= nt * 16) {
+    gemm_tiles_x<TA, TB, 4, 4>(g);
+  } else if (g.M >= 2 && g.N >= 2 && work >= nt * 4) {
+    gemm_tiles_x<TA, TB, 2, 2>(g);
+  } else {
+    gemm_tiles_x<TA, TB, 1, 1>(g);
+  }
+  __syncthreads();
+}
+
+// S (k x k) = Y^T Y for the n x k matrix Y (row stride ldy), in Y's precision.
+__device__ inline void cta_gram_t(float* Y, int n, int k, int ldy, float* S) {
+  cta_gemm(make_gemm(Y, lin(1), ldy, Y, lin(1), ldy, S, lin(k), lin(1), k, k, n));
+}
+__device__ inline void cta_gram_t(double* Y, int n, int k, int ldy, double* S) {
+  cta_gemm_x(make_gemm_x(static_cast<const double*>(Y), lin(1), ldy, static_cast<const double*>(Y), lin(1), ldy, S,
+                         lin(k), lin(1), k, k, n));
+}
+
+// ---------------------------------------------------------------------------
 // Reductions (result broadcast to all threads).  `red` is >= 32 doubles of
 // shared scratch.
 // ---------------------------------------------------------------------------

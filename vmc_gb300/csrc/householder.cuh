@@ -23,8 +23,9 @@ namespace vmc {
 // dimension ldh, odd for conflict-free column access) and tau (k floats) are
 // scratch; Q must alias neither A nor H.  One warp builds each reflector, the
 // warps share the trailing columns; 3 barriers per column.
-__device__ inline void cta_householder_q(const float* A, int m, int k, int ars, int acs, float* Q, int qrs, int qcs,
-                                         float* H, int ldh, float* tau) {
+template <typename T>
+__device__ inline void cta_householder_q(const T* A, int m, int k, int ars, int acs, T* Q, int qrs, int qcs,
+                                         T* H, int ldh, T* tau) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int nl = nt < 32 ? nt : 32;
   const int lane = tid % nl, warp = tid / nl, nwarps = nt / nl;
@@ -35,21 +36,21 @@ __device__ inline void cta_householder_q(const float* A, int m, int k, int ars, 
   __syncthreads();
   for (int j = 0; j < k; ++j) {
     if (warp == 0) {
-      float xn = 0.f;
+      T xn = T(0.);
       for (int i = j + 1 + lane; i < m; i += nl) {
-        const float x = H[(size_t)i * ldh + j];
-        xn = fmaf(x, x, xn);
+        const T x = H[(size_t)i * ldh + j];
+        xn = vfma(x, x, xn);
       }
-      xn = warp_sum_f(xn);
-      const float alpha = H[(size_t)j * ldh + j];
-      float t = 0.f, beta = alpha, sc = 0.f;
-      if (xn > 0.f) {
-        beta = -copysignf(sqrtf(fmaf(alpha, alpha, xn)), alpha);
+      xn = warp_sum_t(xn);
+      const T alpha = H[(size_t)j * ldh + j];
+      T t = T(0.), beta = alpha, sc = T(0.);
+      if (xn > T(0.)) {
+        beta = -vcopysign(vsqrt(vfma(alpha, alpha, xn)), alpha);
         t = (beta - alpha) / beta;
-        sc = 1.f / (alpha - beta);
+        sc = T(1.) / (alpha - beta);
       }
       warp_sync();
-      if (t != 0.f)
+      if (t != T(0.))
         for (int i = j + 1 + lane; i < m; i += nl) H[(size_t)i * ldh + j] *= sc;
       if (lane == 0) {
         H[(size_t)j * ldh + j] = beta;
@@ -57,16 +58,16 @@ __device__ inline void cta_householder_q(const float* A, int m, int k, int ars, 
       }
     }
     __syncthreads();
-    const float t = tau[j];
-    if (t != 0.f) {
+    const T t = tau[j];
+    if (t != T(0.)) {
       for (int c = j + 1 + warp; c < k; c += nwarps) {
-        float w = 0.f;
-        for (int i = j + 1 + lane; i < m; i += nl) w = fmaf(H[(size_t)i * ldh + j], H[(size_t)i * ldh + c], w);
-        w = t * (warp_sum_f(w) + H[(size_t)j * ldh + c]);
+        T w = T(0.);
+        for (int i = j + 1 + lane; i < m; i += nl) w = vfma(H[(size_t)i * ldh + j], H[(size_t)i * ldh + c], w);
+        w = t * (warp_sum_t(w) + H[(size_t)j * ldh + c]);
         warp_sync();
         if (lane == 0) H[(size_t)j * ldh + c] -= w;
         for (int i = j + 1 + lane; i < m; i += nl)
-          H[(size_t)i * ldh + c] = fmaf(-w, H[(size_t)i * ldh + j], H[(size_t)i * ldh + c]);
+          H[(size_t)i * ldh + c] = vfma(-w, H[(size_t)i * ldh + j], H[(size_t)i * ldh + c]);
       }
     }
     __syncthreads();
@@ -74,22 +75,22 @@ __device__ inline void cta_householder_q(const float* A, int m, int k, int ars, 
   // Q = H_0 H_1 ... H_{k-1} [I_k; 0]; H_j leaves columns c < j at e_c
   for (int e = tid; e < m * k; e += nt) {
     const int i = e / k, c = e - i * k;
-    Q[(size_t)i * qrs + (size_t)c * qcs] = (i == c) ? 1.f : 0.f;
+    Q[(size_t)i * qrs + (size_t)c * qcs] = (i == c) ? T(1.) : T(0.);
   }
   __syncthreads();
   for (int j = k - 1; j >= 0; --j) {
-    const float t = tau[j];
-    if (t != 0.f) {
+    const T t = tau[j];
+    if (t != T(0.)) {
       for (int c = j + warp; c < k; c += nwarps) {
-        float w = 0.f;
+        T w = T(0.);
         for (int i = j + 1 + lane; i < m; i += nl)
-          w = fmaf(H[(size_t)i * ldh + j], Q[(size_t)i * qrs + (size_t)c * qcs], w);
-        w = t * (warp_sum_f(w) + Q[(size_t)j * qrs + (size_t)c * qcs]);
+          w = vfma(H[(size_t)i * ldh + j], Q[(size_t)i * qrs + (size_t)c * qcs], w);
+        w = t * (warp_sum_t(w) + Q[(size_t)j * qrs + (size_t)c * qcs]);
         warp_sync();
         if (lane == 0) Q[(size_t)j * qrs + (size_t)c * qcs] -= w;
         for (int i = j + 1 + lane; i < m; i += nl)
           Q[(size_t)i * qrs + (size_t)c * qcs] =
-              fmaf(-w, H[(size_t)i * ldh + j], Q[(size_t)i * qrs + (size_t)c * qcs]);
+              vfma(-w, H[(size_t)i * ldh + j], Q[(size_t)i * qrs + (size_t)c * qcs]);
       }
     }
     __syncthreads();

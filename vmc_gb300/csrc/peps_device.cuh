@@ -607,6 +607,13 @@ __device__ inline void fill_ones_row(const DevPlan& P, float* row) {
   __syncthreads();
 }
 
+#ifndef VMC_CHAIN_F64
+#define VMC_CHAIN_F64 0
+#endif
+#if VMC_CHAIN_F64
+#include "chain_f64.cuh"
+#endif
+
 // op element (re, im) of a real or complex operator table
 __device__ __forceinline__ void op_elem(const float* table, size_t e, double* re, double* im) {
   const float* x = elem(table, e);
@@ -1049,7 +1056,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   float* dyn_smem = emu_dyn_smem(P.arena_in_smem ? P.arena_floats : 0);
   std::memset(&sh, 0xff, sizeof(sh));
 #else
-  extern __shared__ float dyn_smem[];
+  extern __shared__ __align__(16) float dyn_smem[];
 #endif
   const int mode = J.mode, n_chains = J.n_chains, full_gradient = J.full_gradient;
   const float* tensors = J.tensors;
@@ -1067,7 +1074,12 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   float* out_gap = J.out_gap;
   Slot S = make_slot(P, slot_base);
   if (threadIdx.x == 0) g_tile_policy = P.tile_policy;  // read by cta_gemm after the next barrier
+#if VMC_CHAIN_F64
+  // the FP64 chain's arena takes the place of the FP32 truncation arena
+  const ChainD ch = make_chain_d(P, S.h64, reinterpret_cast<double*>(P.arena_in_smem ? dyn_smem : S.arena));
+#else
   const Arena ar = make_arena(P, P.arena_in_smem ? dyn_smem : S.arena, S.arena);
+#endif
   if (P.onerow_in_smem) {
     // the 1-row environment GEMM intermediates are never live during a truncation
     for (int i = 0; i < 4; ++i) S.scr[3 + i] = dyn_smem + (size_t)i * P.scr1;
@@ -1092,12 +1104,23 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
     float* b = cache_row(P, cache, ce, R - 1);
     fill_ones_row(P, b);
     if (threadIdx.x == 0) lb[R - 1] = 0.0;
+#if VMC_CHAIN_F64
+    int hc = 0;
+    fill_ones_row_d(P, ch.row[0]);
+#endif
     for (int r = R - 1; r >= 1; --r) {
       for (int c = threadIdx.x; c < C; c += blockDim.x) sh.spins[0][c] = cfg[r * C + c];
       __syncthreads();
+#if VMC_CHAIN_F64
+      const double ls = apply_row_hp(P, sh, perm, ch.row[hc], bbonds(P, r), ch.row[hc ^ 1],
+                                     cache_row(P, cache, ce, r - 1), bbonds(P, r - 1), r, sh.spins[0], true, ch,
+                                     &min_gap);
+      hc ^= 1;
+#else
       const double ls = apply_row(P, S, sh, perm, cache_row(P, cache, ce, r), bbonds(P, r),
                                   cache_row(P, cache, ce, r - 1), bbonds(P, r - 1), r, sh.spins[0], true, ar,
                                   &min_gap);
+#endif
       if (threadIdx.x == 0) lb[r - 1] = lb[r] + ls;
       __syncthreads();
     }
@@ -1108,6 +1131,10 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   // ---------------- top-down pass: transition or forward ----------------
   VMC_TSTART(tchain);
   float min_margin = INFINITY;
+#if VMC_CHAIN_F64
+  int ht = 0;
+  fill_ones_row_d(P, ch.row[0]);
+#endif
   fill_ones_row(P, S.topc);
   if (threadIdx.x == 0) S.lt[0] = 0.0;
   __syncthreads();
@@ -1124,15 +1151,26 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
       __syncthreads();
     }
     VMC_TSTART(tz);
+#if VMC_CHAIN_F64
+    const double ls = apply_row_hp(P, sh, perm, ch.row[ht], tbonds(P, r), ch.row[ht ^ 1],
+                                   S.topc + (size_t)(r + 1) * C * P.TS, tbonds(P, r + 1), r, sh.spins[0], false, ch,
+                                   &min_gap);
+    ht ^= 1;
+#else
     const double ls = apply_row(P, S, sh, perm, top, tbonds(P, r), S.topc + (size_t)(r + 1) * C * P.TS,
                                 tbonds(P, r + 1), r, sh.spins[0], false, ar, &min_gap);
+#endif
     VMC_TSTOP(tz, PH_T_ZIP);
     if (threadIdx.x == 0) S.lt[r + 1] = S.lt[r] + ls;
     __syncthreads();
   }
   double sgn = 1.0;
+#if VMC_CHAIN_F64
+  double logamp = S.lt[R] + contract_bottom_d(P, ch.row[ht], tbonds(P, R), sh, ch.z1, &sgn);
+#else
   double logamp = S.lt[R] + contract_bottom(P, S.topc + (size_t)R * C * P.TS, tbonds(P, R), sh,
                                            reinterpret_cast<double*>(S.scr[0]), &sgn);
+#endif
   if (mode == MODE_ENERGY) {
     logamp = logamp_io[chain];
     sgn = sign_io[chain];
@@ -1167,6 +1205,10 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   double* lbc = (mode == MODE_SWEEP) ? cache_logs(P, cache, ce_n, ce) : nullptr;
   double lb_cur = 0.0, lb_prev = 0.0;
   int ib_cur = 0, ib_prev = 1, ib_next = 2;
+#if VMC_CHAIN_F64
+  int hb = 0;
+  fill_ones_row_d(P, ch.row[0]);
+#endif
   fill_ones_row(P, S.brow[ib_cur]);
   for (int r = R - 1; r >= 0; --r) {
     for (int c = threadIdx.x; c < C; c += blockDim.x) {
@@ -1194,8 +1236,14 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
     }
     if (r > 0) {
       VMC_TSTART(tb);
+#if VMC_CHAIN_F64
+      const double ls = apply_row_hp(P, sh, perm, ch.row[hb], bbonds(P, r), ch.row[hb ^ 1], S.brow[ib_next],
+                                     bbonds(P, r - 1), r, sh.spins[0], true, ch, &min_gap);
+      hb ^= 1;
+#else
       const double ls = apply_row(P, S, sh, perm, bcur, bbonds(P, r), S.brow[ib_next], bbonds(P, r - 1), r,
                                   sh.spins[0], true, ar, &min_gap);
+#endif
       VMC_TSTOP(tb, PH_B_ZIP);
       lb_prev = lb_cur;
       lb_cur = lb_cur + ls;

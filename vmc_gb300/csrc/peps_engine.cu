@@ -254,6 +254,15 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
   if (opts && (opts->threads != 0 && (opts->threads < 64 || opts->threads > kThreads || opts->threads % 32 != 0)))
     return VMC_ERR_INVALID;
   if (opts && (opts->tile_policy < 0 || opts->tile_policy > 3 || opts->smem_kb < -1)) return VMC_ERR_INVALID;
+  if (opts && (opts->precision < VMC_PRECISION_FP32 || opts->precision > VMC_PRECISION_MIXED ||
+               opts->trunc_method < 0 || opts->trunc_method > 1 || opts->vchunk < 0 || opts->vert_smem < 0))
+    return VMC_ERR_INVALID;
+  const int precision = opts ? opts->precision : VMC_PRECISION_FP32;
+  // the FP64 chain exists for real ZipUp / NoTruncation plans with the Gram eigensolver and FFMA tiles
+  if (precision == VMC_PRECISION_MIXED &&
+      (dtype != VMC_DTYPE_F32 || gi_N > 0 || strategy == VMC_STRATEGY_VARIATIONAL || opts->trunc_method != 0 ||
+       opts->tile_policy == 3))
+    return VMC_ERR_UNSUPPORTED;
   *out_plan = nullptr;
   const int R = shape->n_rows, C = shape->n_cols;
   if (R < 1 || C < 1 || C > kMaxCols || bond_dim < 1 || phys_dim < 1 || chi < 1) return VMC_ERR_INVALID;
@@ -365,38 +374,32 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
   E2S *= es;
   P.nmax = (int)(chimax * D);
   P.kmax = (int)std::min<long long>(chi, chimax * D);
-  {
-    const char* tm = std::getenv("VMC_TRUNCATION");
-    // the one-sided Jacobi cross-check exists for real elements only
-    P.trunc_method = (tm && std::strcmp(tm, "jacobi") == 0 && es == 1) ? 1 : 0;
-  }
-  {
-    // explicit options (an autotuned choice) or, without them, the VMC_* environment
-    const char* th = opts ? nullptr : std::getenv("VMC_THREADS");
-    P.threads = opts ? (opts->threads ? opts->threads : kDefaultThreads)
-                     : th ? std::max(64, std::min(kThreads, std::atoi(th))) : kDefaultThreads;
-    const char* tp = opts ? nullptr : std::getenv("VMC_TILE_POLICY");
-    P.tile_policy = opts ? opts->tile_policy : tp ? std::max(0, std::min(3, std::atoi(tp))) : 0;
-  }
-  long long budget = kMaxArenaSmemBytes;
-  if (opts) {
-    if (opts->smem_kb >= 0) budget = std::min<long long>(opts->smem_kb, kMaxArenaSmemBytes / 1024) * 1024LL;
-  } else if (const char* kb = std::getenv("VMC_SMEM_KB")) {
-    budget = std::max(0, std::atoi(kb)) * 1024LL;
-  }
+  // the one-sided Jacobi cross-check exists for real elements only
+  P.trunc_method = (opts && opts->trunc_method == 1 && es == 1) ? 1 : 0;
+  P.chain64 = precision == VMC_PRECISION_MIXED;
+  P.threads = (opts && opts->threads) ? opts->threads : kDefaultThreads;
+  P.tile_policy = opts ? opts->tile_policy : 0;
+  // shared memory per CTA: the FP64 arena of a mixed plan is twice the FP32 one
+  const long long smem_cap = P.chain64 ? kMaxArenaSmemBytesF64 : kMaxArenaSmemBytes;
+  long long budget = P.chain64 ? kDefaultArenaSmemBytesF64 : kMaxArenaSmemBytes;
+  if (opts && opts->smem_kb >= 0) budget = std::min<long long>(opts->smem_kb * 1024LL, smem_cap);
+  const int opt_vchunk = opts ? opts->vchunk : 0;
+  const int opt_vert_smem = opts ? opts->vert_smem : 0;
   // Buffer placement for a shared-memory budget (bytes per CTA): truncation
   // arena, 1-row intermediates and vertical-energy buffers go to shared memory
   // when they fit, else to the CTA's workspace slot.
   auto lay_out = [&](DevPlan& Q, long long budget) {
     const long long mat_floats = al64(es * Q.nmax * (Q.nmax | 1));
-    const long long trunc_all = arena_floats(Q.nmax, Q.kmax, Q.trunc_method, Q.es);
+    // a mixed plan's arena holds FP64 values: two floats each
+    const long long trunc_all =
+        Q.chain64 ? 2 * arena_doubles(Q.nmax, Q.kmax) : arena_floats(Q.nmax, Q.kmax, Q.trunc_method, Q.es);
     Q.arena_in_smem = 0;
     Q.mat_in_smem = 1;  // "theta lives inside the arena" (arena itself may be global)
     Q.arena_floats = trunc_all;
     if (trunc_all * 4 <= budget) {
       Q.arena_in_smem = 1;
       Q.mat_in_smem = 1;
-    } else if ((trunc_all - mat_floats) * 4 <= budget && Q.trunc_method == 0) {
+    } else if (!Q.chain64 && (trunc_all - mat_floats) * 4 <= budget && Q.trunc_method == 0) {
       Q.arena_in_smem = 1;
       Q.mat_in_smem = 0;
       Q.arena_floats = trunc_all - mat_floats;
@@ -408,16 +411,15 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
       const long long nbuf = 1 + 2LL * d;
       long long ch = (budget / 4) / (nbuf * unit);
       ch = std::max(1LL, std::min(ch, chimax));
-      if (const char* vc = std::getenv("VMC_VCHUNK")) ch = std::max(1LL, std::min(ch, (long long)std::atoi(vc)));
+      if (opt_vchunk > 0) ch = std::max(1LL, std::min(ch, (long long)opt_vchunk));
       Q.vchunk = (int)ch;
       Q.vbuf = (int)al64(ch * unit);
       // The vertical-energy buffers live in (L1-cached) global scratch with the
       // whole bond range in one chunk: fewer, larger GEMMs beat shared-memory
       // chunks of a few bond values (measured +5 % at 8x8, D=4, chi=16).
-      // VMC_VERT_SMEM=1 puts them in the shared-memory arena, chunked.
+      // The vert_smem option puts them in the shared-memory arena, chunked.
       Q.vert_in_smem = 0;
-      if (const char* vs = std::getenv("VMC_VERT_SMEM"))
-        if (std::atoi(vs) != 0 && !Q.gi && Q.arena_in_smem && nbuf * Q.vbuf * 4 <= budget) Q.vert_in_smem = 1;
+      if (opt_vert_smem != 0 && !Q.gi && Q.arena_in_smem && nbuf * Q.vbuf * 4 <= budget) Q.vert_in_smem = 1;
     }
     Q.onerow_in_smem = 0;
     if (Q.arena_in_smem && std::max(Q.arena_floats, 4LL * Q.scr1) * 4 <= budget) {
@@ -438,7 +440,8 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
                     al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
                     2 * al64(E2S) +
                     (Q.arena_in_smem ? (Q.mat_in_smem ? 0 : mat_floats) : al64(Q.arena_floats)) +
-                    (long long)Q.n_scr * al64(SCR) + al64(2LL * C * Q.VS);
+                    (long long)Q.n_scr * al64(SCR) + al64(2LL * C * Q.VS) +
+                    (Q.chain64 ? 2 * chain_f64_doubles(C, TS, SCR) : 0);
   };
   lay_out(P, budget);
   // The same plan with everything in the slot (no dynamic shared memory): an
@@ -750,9 +753,10 @@ static bool job_valid(const vmc_peps_job& j) {
   }
 }
 
-static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout* L) {
+static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, int layout, BatchLayout* L) {
   if (!jobs || n_jobs < 1) return VMC_ERR_INVALID;
   if (n_jobs > VMC_MAX_BATCH_JOBS) return VMC_ERR_UNSUPPORTED;
+  if (layout < VMC_BATCH_LAYOUT_AUTO || layout > VMC_BATCH_LAYOUT_SLOT) return VMC_ERR_INVALID;
   size_t off = 64;  // the item counter
   long long total = 0;
   double cost[VMC_MAX_BATCH_JOBS];
@@ -767,8 +771,7 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, BatchLayout
     w_all += cost[i] * jobs[i].n_chains;
     if (!P.arena_in_smem) w_slot += cost[i] * jobs[i].n_chains;
   }
-  L->slot_layout = w_slot > 0.5 * w_all;
-  if (const char* bl = std::getenv("VMC_BATCH_LAYOUT")) L->slot_layout = std::strcmp(bl, "slot") == 0;
+  L->slot_layout = layout == VMC_BATCH_LAYOUT_AUTO ? w_slot > 0.5 * w_all : layout == VMC_BATCH_LAYOUT_SLOT;
   for (int i = 0; i < n_jobs; ++i) {
     const vmc_peps_job& j = jobs[i];
     const DevPlan& P = L->slot_layout ? j.plan->hpg : j.plan->hp;
@@ -849,16 +852,25 @@ static vmc_status launch_batch(const vmc_peps_job* jobs, const BatchLayout& L, v
 
 extern "C" {
 
-size_t vmc_batch_workspace_size(const vmc_peps_job* jobs, int n_jobs) {
+size_t vmc_batch_workspace_size_ex(const vmc_peps_job* jobs, int n_jobs, int layout) {
   BatchLayout L;
-  return batch_layout(jobs, n_jobs, &L) == VMC_OK ? L.bytes : 0;
+  return batch_layout(jobs, n_jobs, layout, &L) == VMC_OK ? L.bytes : 0;
+}
+
+size_t vmc_batch_workspace_size(const vmc_peps_job* jobs, int n_jobs) {
+  return vmc_batch_workspace_size_ex(jobs, n_jobs, VMC_BATCH_LAYOUT_AUTO);
 }
 
 vmc_status vmc_peps_batch(const vmc_peps_job* jobs, int n_jobs, void* stream, void* workspace,
                           size_t workspace_bytes, int32_t* status_dev) {
+  return vmc_peps_batch_ex(jobs, n_jobs, VMC_BATCH_LAYOUT_AUTO, stream, workspace, workspace_bytes, status_dev);
+}
+
+vmc_status vmc_peps_batch_ex(const vmc_peps_job* jobs, int n_jobs, int layout, void* stream, void* workspace,
+                             size_t workspace_bytes, int32_t* status_dev) {
   if (!workspace || !status_dev) return VMC_ERR_INVALID;
   BatchLayout L;
-  const vmc_status st = batch_layout(jobs, n_jobs, &L);
+  const vmc_status st = batch_layout(jobs, n_jobs, layout, &L);
   if (st != VMC_OK) return st;
   if (L.total == 0) return VMC_OK;
   if (workspace_bytes < L.bytes) return VMC_ERR_WORKSPACE;

@@ -37,6 +37,9 @@ constexpr float kJacobiTol = 5e-7f;  // stop when every |a_p.a_q| <= tol |a_p||a
 constexpr int kJacobiSweeps = 16;
 // dynamic shared memory per chain; 52 KB keeps 4 chains of 128 threads on an SM
 constexpr long long kMaxArenaSmemBytes = 52 * 1024;
+// mixed precision: largest and default dynamic shared memory per CTA for the FP64 arena
+constexpr long long kMaxArenaSmemBytesF64 = 200 * 1024;
+constexpr long long kDefaultArenaSmemBytesF64 = 52 * 1024;
 enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4, P_VRB = 5 };
 enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3 };
 
@@ -49,6 +52,7 @@ struct DevPlan {
   int TS, ES, E2S, SCR, MM;  // buffer sizes (floats)
   int nmax, kmax;         // largest truncation matrix side / kept bond
   int trunc_method;       // 0: Gram + tridiagonal eigensolver, 1: one-sided Jacobi
+  int chain64;            // mixed precision: the boundary-MPS chain in FP64 (chain_f64.cuh), the rest FP32
   int arena_in_smem;      // truncation arena in dynamic shared memory
   int mat_in_smem;        // theta matrix inside the arena (else in a separate global slot region)
   int threads;            // CTA size of the fused kernel
@@ -106,10 +110,12 @@ struct Slot {
   float* l2[2];  // E2S
   float* arena;  // truncation arena when it does not fit shared memory
   float* venv;   // Variational: left envs C*VS, then right envs C*VS
+  double* h64;   // mixed precision: the FP64 boundary-MPS chain (chain_f64_doubles doubles), else null
   float* scr[11 + 2 * kMaxPhys + 5];  // n_scr = 11 + 2 kMaxPhys buffers (GI plans use the first 12)
 };
 
 __host__ __device__ inline long long al64(long long n) { return (n + 63) & ~63LL; }
+__host__ __device__ inline long long al32(long long n) { return (n + 31) & ~31LL; }
 __host__ __device__ inline int min_i(int a, int b) { return a < b ? a : b; }
 
 __device__ inline Slot make_slot(const DevPlan& P, float* base) {
@@ -128,6 +134,7 @@ __device__ inline Slot make_slot(const DevPlan& P, float* base) {
                                     : al64(P.arena_floats);
   for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
   s.venv = p; p += al64(2LL * P.C * P.VS);
+  s.h64 = P.chain64 ? reinterpret_cast<double*>(p) : nullptr;
   return s;
 }
 
@@ -148,6 +155,21 @@ __host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_
          al64((long long)kmax * kmax) + al64(4LL * kmax * nmax) + al64(((long long)kmax * nmax + 3) / 4) +
          3 * al64(nmax) + 3 * al64((long long)es * nmax) + al64(nmax + 1) + al64(2LL * es * nmax) +
          al64(nmax + 64) + 64 + (es == 2 ? al64((long long)nmax * kmax) : 0);
+}
+
+// Doubles of the FP64 truncation arena of a mixed-precision plan (layout:
+// make_arena_d in chain_f64.cuh).
+__host__ __device__ inline long long arena_doubles(int nmax, int kmax) {
+  const int ld = nmax | 1;
+  return 2 * al32((long long)nmax * ld) + al32((long long)nmax * kmax) + al32((long long)kmax * kmax) +
+         al32(4LL * kmax * nmax) + al32(((long long)kmax * nmax + 7) / 8) + 6 * al32(nmax) + al32(nmax + 1) +
+         al32(2LL * nmax) + al32(nmax + 64) + 32;
+}
+// Doubles of the FP64 chain buffers in a slot (make_chain_d): two boundary
+// rows, two carries and the Z1 intermediate.  The FP64 arena takes the place
+// of the FP32 one (shared memory or the slot's arena region).
+__host__ __device__ inline long long chain_f64_doubles(int C, long long TS, long long SCR) {
+  return 2 * al32((long long)C * TS) + 3 * al32(SCR);
 }
 
 // Arguments of one job: the chains of one plan in one mode.
@@ -199,12 +221,14 @@ struct KernelSet {
 };
 namespace rk { const KernelSet& kernels(); }  // real FP32 elements
 namespace rt { const KernelSet& kernels(); }  // real FP32 elements, tensor-core GEMMs (tile_policy 3)
+namespace rm { const KernelSet& kernels(); }  // real, mixed precision: FP64 boundary-MPS chain
 namespace ck { const KernelSet& kernels(); }  // complex64 elements
 namespace gr { const KernelSet& kernels(); }  // gauge-invariant plans, real FP32
 namespace gc { const KernelSet& kernels(); }  // gauge-invariant plans, complex64
 inline const KernelSet& kernels_of(const DevPlan& P) {
   if (P.gi) return P.es == 2 ? gc::kernels() : gr::kernels();
   if (P.es == 2) return ck::kernels();
+  if (P.chain64) return rm::kernels();
   return P.tile_policy == 3 ? rt::kernels() : rk::kernels();
 }
 

@@ -16,6 +16,7 @@
 
 #include "device_common.cuh"
 #include "phase_timers.cuh"
+#include "scalar.cuh"
 
 namespace vmc {
 
@@ -40,8 +41,9 @@ __device__ __forceinline__ void warp_sync() {
 // `v`, `p` are n floats of scratch; `part` holds >= 64 floats.
 // Per column: 3 barriers; the matrix-vector product uses `rg` threads per row
 // and the rank-2 update a 2-D thread grid (no integer division).
-__device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, float* e, float* tau, float* v,
-                                          float* p, float* part) {
+template <typename T>
+__device__ inline void cta_tridiagonalize(T* A, int n, int lda, T* d, T* e, T* tau, T* v,
+                                          T* p, T* part) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = (nt + 31) >> 5;
   if (n == 1) {
@@ -61,108 +63,108 @@ __device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, fl
   const int gy = nt / gx;
   const int ux = tid % gx, uy = tid / gx;
   {
-    float s = 0.f;
-    for (int i = 2 + tid; i < n; i += nt) s = fmaf(A[(size_t)i * lda], A[(size_t)i * lda], s);
-    s = warp_sum_f(s);
+    T s = T(0.);
+    for (int i = 2 + tid; i < n; i += nt) s = vfma(A[(size_t)i * lda], A[(size_t)i * lda], s);
+    s = warp_sum_t(s);
     if (lane == 0) part[warp] = s;
   }
   __syncthreads();
   for (int j = 0; j < n - 2; ++j) {
     const int m = n - j - 1;
-    float xn2 = 0.f;
+    T xn2 = T(0.);
     for (int w = 0; w < nwarps; ++w) xn2 += part[w];
-    const float alpha = A[(size_t)(j + 1) * lda + j];
-    float tj = 0.f, beta = alpha, scal = 0.f;
-    if (xn2 > 0.f) {
-      beta = -copysignf(sqrtf(alpha * alpha + xn2), alpha);
+    const T alpha = A[(size_t)(j + 1) * lda + j];
+    T tj = T(0.), beta = alpha, scal = T(0.);
+    if (xn2 > T(0.)) {
+      beta = -vcopysign(vsqrt(alpha * alpha + xn2), alpha);
       tj = (beta - alpha) / beta;
-      scal = 1.f / (alpha - beta);
+      scal = T(1.) / (alpha - beta);
     }
     // column j stays unscaled until barrier (2): the matrix-vector product
     // below rebuilds v from it, so v needs no barrier of its own
-    const float* colj = A + (size_t)(j + 1) * lda + j;
-    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? 1.f : colj[(size_t)i * lda] * scal;
+    const T* colj = A + (size_t)(j + 1) * lda + j;
+    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? T(1.) : colj[(size_t)i * lda] * scal;
     if (tid == 0) {
       d[j] = A[(size_t)j * lda + j];
       e[j] = beta;
       tau[j] = tj;
     }
-    float* As = A + (size_t)(j + 1) * lda + (j + 1);
-    if (tj == 0.f) {
+    T* As = A + (size_t)(j + 1) * lda + (j + 1);
+    if (tj == T(0.)) {
       __syncthreads();  // v visible
-      float s = 0.f;
-      for (int i = 2 + tid; i < m; i += nt) s = fmaf(As[(size_t)i * lda], As[(size_t)i * lda], s);
-      s = warp_sum_f(s);
+      T s = T(0.);
+      for (int i = 2 + tid; i < m; i += nt) s = vfma(As[(size_t)i * lda], As[(size_t)i * lda], s);
+      s = warp_sum_t(s);
       if (lane == 0) part[warp] = s;
       __syncthreads();
       continue;
     }
     // p = tau * A_sub v, rg threads per row; partial p.v per warp
-    float pv = 0.f;
+    T pv = T(0.);
     for (int i = rrow; i < m; i += nrow_thr) {
-      const float* row = As + (size_t)i * lda;
-      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+      const T* row = As + (size_t)i * lda;
+      T s0 = T(0.), s1 = T(0.), s2 = T(0.), s3 = T(0.);
       int l = rlane;
       for (; l + 3 * rg < m; l += 4 * rg) {
-        const float a0 = row[l], a1 = row[l + rg], a2 = row[l + 2 * rg], a3 = row[l + 3 * rg];
-        const float b0 = l == 0 ? 1.f : colj[(size_t)l * lda] * scal;
-        const float b1 = colj[(size_t)(l + rg) * lda] * scal;
-        const float b2 = colj[(size_t)(l + 2 * rg) * lda] * scal;
-        const float b3 = colj[(size_t)(l + 3 * rg) * lda] * scal;
-        s0 = fmaf(a0, b0, s0);
-        s1 = fmaf(a1, b1, s1);
-        s2 = fmaf(a2, b2, s2);
-        s3 = fmaf(a3, b3, s3);
+        const T a0 = row[l], a1 = row[l + rg], a2 = row[l + 2 * rg], a3 = row[l + 3 * rg];
+        const T b0 = l == 0 ? T(1.) : colj[(size_t)l * lda] * scal;
+        const T b1 = colj[(size_t)(l + rg) * lda] * scal;
+        const T b2 = colj[(size_t)(l + 2 * rg) * lda] * scal;
+        const T b3 = colj[(size_t)(l + 3 * rg) * lda] * scal;
+        s0 = vfma(a0, b0, s0);
+        s1 = vfma(a1, b1, s1);
+        s2 = vfma(a2, b2, s2);
+        s3 = vfma(a3, b3, s3);
       }
-      for (; l < m; l += rg) s0 = fmaf(row[l], l == 0 ? 1.f : colj[(size_t)l * lda] * scal, s0);
-      float s = (s0 + s1) + (s2 + s3);
+      for (; l < m; l += rg) s0 = vfma(row[l], l == 0 ? T(1.) : colj[(size_t)l * lda] * scal, s0);
+      T s = (s0 + s1) + (s2 + s3);
 #ifndef VMC_HOST_EMULATION
       for (int o = rg / 2; o > 0; o >>= 1) s += __shfl_xor_sync(rmask, s, o, rg);
 #endif
-      const float pi = tj * s;
+      const T pi = tj * s;
       if (rlane == 0) {
         p[i] = pi;
-        pv = fmaf(pi, i == 0 ? 1.f : colj[(size_t)i * lda] * scal, pv);
+        pv = vfma(pi, i == 0 ? T(1.) : colj[(size_t)i * lda] * scal, pv);
       }
     }
-    pv = warp_sum_f(pv);
+    pv = warp_sum_t(pv);
     if (lane == 0) part[32 + warp] = pv;
     __syncthreads();  // (2) p and v visible
     // store the reflector in column j (nothing reads column j any more)
     for (int i = 1 + tid; i < m; i += nt) A[(size_t)(j + 1 + i) * lda + j] = v[i];
-    float ptv = 0.f;
+    T ptv = T(0.);
     for (int w = 0; w < nwarps; ++w) ptv += part[32 + w];
-    const float K = 0.5f * tj * ptv;
+    const T K = T(0.5) * tj * ptv;
     // A_sub -= v w^T + w v^T, w = p - K v
-    float s = 0.f;
+    T s = T(0.);
     // columns l = l0 + q*gx (q < 4) of this thread: v_l, w_l kept in registers
     for (int l0 = ux; l0 < m; l0 += 4 * gx) {
-      float vl[4], wl[4];
+      T vl[4], wl[4];
       int nl = 0;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int l = l0 + q * gx;
-        vl[q] = l < m ? v[l] : 0.f;
-        wl[q] = l < m ? p[l] - K * vl[q] : 0.f;
+        vl[q] = l < m ? v[l] : T(0.);
+        wl[q] = l < m ? p[l] - K * vl[q] : T(0.);
         nl += l < m;
       }
       for (int i = uy; i < m; i += gy) {
-        const float vi = v[i], wi = p[i] - K * vi;
-        float* arow = As + (size_t)i * lda;
-        float a[4];
+        const T vi = v[i], wi = p[i] - K * vi;
+        T* arow = As + (size_t)i * lda;
+        T a[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) a[q] = q < nl ? arow[l0 + q * gx] : 0.f;
+        for (int q = 0; q < 4; ++q) a[q] = q < nl ? arow[l0 + q * gx] : T(0.);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           if (q < nl) {
-            const float nv = a[q] - vi * wl[q] - wi * vl[q];
+            const T nv = a[q] - vi * wl[q] - wi * vl[q];
             arow[l0 + q * gx] = nv;
-            if (l0 + q * gx == 0 && i >= 2) s = fmaf(nv, nv, s);
+            if (l0 + q * gx == 0 && i >= 2) s = vfma(nv, nv, s);
           }
         }
       }
     }
-    s = warp_sum_f(s);
+    s = warp_sum_t(s);
     if (lane == 0) part[warp] = s;
     __syncthreads();  // (3) trailing matrix updated
   }
@@ -176,37 +178,39 @@ __device__ inline void cta_tridiagonalize(float* A, int n, int lda, float* d, fl
 }
 
 // Number of eigenvalues of T (d, e2 = e^2) smaller than x.
-__device__ __forceinline__ int sturm_count(const float* d, const float* e2, int n, float x, float pivmin) {
-  float q = d[0] - x;
-  if (fabsf(q) < pivmin) q = -pivmin;
-  int cnt = q < 0.f;
+template <typename T>
+__device__ __forceinline__ int sturm_count(const T* d, const T* e2, int n, T x, T pivmin) {
+  T q = d[0] - x;
+  if (vabs(q) < pivmin) q = -pivmin;
+  int cnt = q < T(0.);
 #pragma unroll 4
   for (int i = 1; i < n; ++i) {
-    q = (d[i] - x) - __fdividef(e2[i - 1], q);
-    if (fabsf(q) < pivmin) q = -pivmin;
-    cnt += q < 0.f;
+    q = (d[i] - x) - vfdiv(e2[i - 1], q);
+    if (vabs(q) < pivmin) q = -pivmin;
+    cnt += q < T(0.);
   }
   return cnt;
 }
 
 // The kk largest eigenvalues of T, descending, into lam[0..kk-1].
 // e2 receives e^2 (n-1 floats of scratch).  Returns the Gershgorin scale |T|.
-__device__ inline float cta_top_eigenvalues(const float* d, const float* e, float* e2, int n, int kk, float* lam) {
+template <typename T>
+__device__ inline T cta_top_eigenvalues(const T* d, const T* e, T* e2, int n, int kk, T* lam) {
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int i = tid; i < n - 1; i += nt) e2[i] = e[i] * e[i];
   __syncthreads();
-  float lo = 3.4e38f, hi = -3.4e38f, e2max = 0.f;
+  T lo = Tol<T>::big, hi = -Tol<T>::big, e2max = T(0.);
   for (int i = 0; i < n; ++i) {
-    const float r = (i > 0 ? fabsf(e[i - 1]) : 0.f) + (i < n - 1 ? fabsf(e[i]) : 0.f);
-    lo = fminf(lo, d[i] - r);
-    hi = fmaxf(hi, d[i] + r);
-    if (i < n - 1) e2max = fmaxf(e2max, e2[i]);
+    const T r = (i > 0 ? vabs(e[i - 1]) : T(0.)) + (i < n - 1 ? vabs(e[i]) : T(0.));
+    lo = vmin(lo, d[i] - r);
+    hi = vmax(hi, d[i] + r);
+    if (i < n - 1) e2max = vmax(e2max, e2[i]);
   }
-  const float tnorm = fmaxf(fabsf(lo), fabsf(hi));
-  const float pivmin = 1e-30f * fmaxf(1.f, e2max);
-  const float span = hi - lo;
-  lo -= 1e-6f * span + 1e-30f;
-  hi += 1e-6f * span + 1e-30f;
+  const T tnorm = vmax(vabs(lo), vabs(hi));
+  const T pivmin = T(1e-30) * vmax(T(1.), e2max);
+  const T span = hi - lo;
+  lo -= T(1e-6) * span + T(1e-30);
+  hi += T(1e-6) * span + T(1e-30);
   // lanes per eigenvalue: 8 (9-way multisection) unless fewer lanes let every
   // wanted eigenvalue run in one round
   int G = nt >= 8 ? 8 : 1;
@@ -222,25 +226,25 @@ __device__ inline float cta_top_eigenvalues(const float* d, const float* e, floa
     const int t = rd * ngroups + tid / G;
     const bool valid = t < kk && tid / G < ngroups;
     const int idx = n - 1 - (valid ? t : 0);
-    float a = lo, b = hi;
-    const int max_it = npts >= 7 ? 14 : (npts >= 3 ? 20 : (npts >= 2 ? 26 : 64));
+    T a = lo, b = hi;
+    const int max_it = Tol<T>::bisect_iter_scale * (npts >= 7 ? 14 : (npts >= 3 ? 20 : (npts >= 2 ? 26 : 64)));
     for (int it = 0; it < max_it; ++it) {
-      const float step = (b - a) / (float)(npts + 1);
+      const T step = (b - a) / T(npts + 1);
       int pred = 0;
-      if (l < npts) pred = sturm_count(d, e2, n, a + (float)(l + 1) * step, pivmin) <= idx;
+      if (l < npts) pred = sturm_count(d, e2, n, a + T(l + 1) * step, pivmin) <= idx;
 #ifdef VMC_HOST_EMULATION
       const unsigned bits = (unsigned)pred;
 #else
       const unsigned bits = (__ballot_sync(gmask, pred) >> base) & ((1u << G) - 1u);
 #endif
       const int L = __popc(bits);
-      const float na = (L == 0) ? a : a + (float)L * step;
-      const float nb = (L == npts) ? b : a + (float)(L + 1) * step;
+      const T na = (L == 0) ? a : a + T(L) * step;
+      const T nb = (L == npts) ? b : a + T(L + 1) * step;
       a = na;
       b = nb;
-      if (b - a <= 2.5e-7f * fmaxf(fabsf(a), fabsf(b)) + pivmin) break;
+      if (b - a <= Tol<T>::bisect_rtol * vmax(vabs(a), vabs(b)) + pivmin) break;
     }
-    if (valid && l == 0) lam[t] = 0.5f * (a + b);
+    if (valid && l == 0) lam[t] = T(0.5) * (a + b);
   }
   __syncthreads();
   return tnorm;
@@ -252,31 +256,32 @@ __device__ inline float cta_top_eigenvalues(const float* d, const float* e, floa
 // If n_orth > 0, every iterate is orthogonalised against the n_orth vectors
 // `orth` (stride xs, column offset 1 apart) -- used for clusters of nearly
 // equal eigenvalues.
-__device__ inline void tri_inverse_iteration(const float* d, const float* e, int n, float lam, float tnorm, float* x,
-                                             int xs, float* u0, float* u1, float* u2, float* mul,
-                                             unsigned char* sw, unsigned seed, const float* orth = nullptr,
+template <typename T>
+__device__ inline void tri_inverse_iteration(const T* d, const T* e, int n, T lam, T tnorm, T* x,
+                                             int xs, T* u0, T* u1, T* u2, T* mul,
+                                             unsigned char* sw, unsigned seed, const T* orth = nullptr,
                                              int n_orth = 0) {
-  const float tiny = 1.2e-7f * fmaxf(tnorm, 1e-30f);
-  float al = d[0] - lam;
-  float be = n > 1 ? e[0] : 0.f;
+  const T tiny = Tol<T>::inv_tiny * vmax(tnorm, T(1e-30));
+  T al = d[0] - lam;
+  T be = n > 1 ? e[0] : T(0.);
 #pragma unroll 4
   for (int i = 0; i < n - 1; ++i) {
-    const float c = e[i];
-    const float a1 = d[i + 1] - lam;
-    const float b1 = (i + 1 < n - 1) ? e[i + 1] : 0.f;
-    if (fabsf(al) >= fabsf(c)) {
-      float piv = al;
-      if (fabsf(piv) < tiny) piv = copysignf(tiny, piv == 0.f ? 1.f : piv);
-      const float m = c / piv;
+    const T c = e[i];
+    const T a1 = d[i + 1] - lam;
+    const T b1 = (i + 1 < n - 1) ? e[i + 1] : T(0.);
+    if (vabs(al) >= vabs(c)) {
+      T piv = al;
+      if (vabs(piv) < tiny) piv = vcopysign(tiny, piv == T(0.) ? T(1.) : piv);
+      const T m = c / piv;
       sw[i] = 0;
       u0[i] = piv;
       u1[i] = be;
-      u2[i] = 0.f;
+      u2[i] = T(0.);
       mul[i] = m;
       al = a1 - m * be;
       be = b1;
     } else {
-      const float m = al / c;
+      const T m = al / c;
       sw[i] = 1;
       u0[i] = c;
       u1[i] = a1;
@@ -286,23 +291,23 @@ __device__ inline void tri_inverse_iteration(const float* d, const float* e, int
       be = -m * b1;
     }
   }
-  if (fabsf(al) < tiny) al = copysignf(tiny, al == 0.f ? 1.f : al);
+  if (vabs(al) < tiny) al = vcopysign(tiny, al == T(0.) ? T(1.) : al);
   u0[n - 1] = al;
   // the back substitution reads these (times zero) at i = n-1: they must not hold stale data
-  u1[n - 1] = 0.f;
-  u2[n - 1] = 0.f;
+  u1[n - 1] = T(0.);
+  u2[n - 1] = T(0.);
   // start vector: deterministic pseudo-random entries in [0.5, 1.5)
   unsigned h = seed * 2654435761u + 12345u;
   for (int i = 0; i < n; ++i) {
     h = h * 1664525u + 1013904223u;
-    x[(size_t)i * xs] = 0.5f + (float)(h >> 8) * (1.f / 16777216.f);
+    x[(size_t)i * xs] = T(0.5) + T(h >> 8) * T(1.0 / 16777216.0);
   }
-  for (int iter = 0; iter < 2; ++iter) {
+  for (int iter = 0; iter < Tol<T>::inv_iters; ++iter) {
     // forward: apply the row operations to the right-hand side (in x)
-    float act = x[0];
+    T act = x[0];
     #pragma unroll 4
     for (int i = 0; i < n - 1; ++i) {
-      const float r1 = x[(size_t)(i + 1) * xs];
+      const T r1 = x[(size_t)(i + 1) * xs];
       if (!sw[i]) {
         x[(size_t)i * xs] = act;
         act = r1 - mul[i] * act;
@@ -313,56 +318,57 @@ __device__ inline void tri_inverse_iteration(const float* d, const float* e, int
     }
     x[(size_t)(n - 1) * xs] = act;
     // back substitution
-    float xn1 = 0.f, xn2 = 0.f, amax = 0.f;
+    T xn1 = T(0.), xn2 = T(0.), amax = T(0.);
     #pragma unroll 4
     for (int i = n - 1; i >= 0; --i) {
-      const float xi = (x[(size_t)i * xs] - u1[i] * xn1 - u2[i] * xn2) / u0[i];
+      const T xi = (x[(size_t)i * xs] - u1[i] * xn1 - u2[i] * xn2) / u0[i];
       x[(size_t)i * xs] = xi;
       xn2 = xn1;
       xn1 = xi;
-      amax = fmaxf(amax, fabsf(xi));
+      amax = vmax(amax, vabs(xi));
     }
-    const float sc = amax > 0.f ? 1.f / amax : 1.f;
+    const T sc = amax > T(0.) ? T(1.) / amax : T(1.);
     for (int i = 0; i < n; ++i) x[(size_t)i * xs] *= sc;
     for (int o = 0; o < n_orth; ++o) {
-      const float* y = orth + o;
-      float dot = 0.f, yy = 0.f;
+      const T* y = orth + o;
+      T dot = T(0.), yy = T(0.);
       for (int i = 0; i < n; ++i) {
-        dot = fmaf(y[(size_t)i * xs], x[(size_t)i * xs], dot);
-        yy = fmaf(y[(size_t)i * xs], y[(size_t)i * xs], yy);
+        dot = vfma(y[(size_t)i * xs], x[(size_t)i * xs], dot);
+        yy = vfma(y[(size_t)i * xs], y[(size_t)i * xs], yy);
       }
-      const float c = yy > 0.f ? dot / yy : 0.f;
+      const T c = yy > T(0.) ? dot / yy : T(0.);
       for (int i = 0; i < n; ++i) x[(size_t)i * xs] -= c * y[(size_t)i * xs];
     }
   }
-  float nrm = 0.f;
-  for (int i = 0; i < n; ++i) nrm = fmaf(x[(size_t)i * xs], x[(size_t)i * xs], nrm);
-  const float sc = nrm > 0.f ? 1.f / sqrtf(nrm) : 0.f;
+  T nrm = T(0.);
+  for (int i = 0; i < n; ++i) nrm = vfma(x[(size_t)i * xs], x[(size_t)i * xs], nrm);
+  const T sc = nrm > T(0.) ? T(1.) / vsqrt(nrm) : T(0.);
   for (int i = 0; i < n; ++i) x[(size_t)i * xs] *= sc;
 }
 
 // Orthonormalise the k columns of Y (n x k, row stride ldy) by CholQR: S = Y^T Y,
 // S = R^T R (warp 0), Y <- Y R^-1.  Returns false if S is numerically singular.
-__device__ inline bool cta_cholqr(float* Y, int n, int k, int ldy, float* S, int* flag) {
+template <typename T>
+__device__ inline bool cta_cholqr(T* Y, int n, int k, int ldy, T* S, int* flag) {
   const int tid = threadIdx.x;
-  cta_gemm(make_gemm(Y, lin(1), ldy, Y, lin(1), ldy, S, lin(k), lin(1), k, k, n));
+  cta_gram_t(Y, n, k, ldy, S);
   if (tid == 0) *flag = 0;
   __syncthreads();
   const int nl = blockDim.x < 32 ? blockDim.x : 32;
   if (tid < 32) {
     for (int j = 0; j < k; ++j) {
-      const float sjj = S[j * k + j];
-      if (!(sjj > 1e-10f)) {
+      const T sjj = S[j * k + j];
+      if (!(sjj > Tol<T>::chol_min)) {
         if (tid == 0) *flag = 1;
         break;
       }
-      const float rjj = sqrtf(sjj);
+      const T rjj = vsqrt(sjj);
       warp_sync();
       for (int c = j + 1 + tid; c < k; c += nl) S[j * k + c] /= rjj;
       if (tid == 0) S[j * k + j] = rjj;
       warp_sync();
       for (int c = j + 1 + tid; c < k; c += nl) {
-        const float rjc = S[j * k + c];
+        const T rjc = S[j * k + c];
         for (int i = j + 1; i <= c; ++i) S[i * k + c] -= S[j * k + i] * rjc;
       }
       warp_sync();
@@ -372,9 +378,9 @@ __device__ inline bool cta_cholqr(float* Y, int n, int k, int ldy, float* S, int
   if (*flag) return false;
   // Y <- Y R^-1, one row per thread
   for (int i = tid; i < n; i += blockDim.x) {
-    float* y = Y + (size_t)i * ldy;
+    T* y = Y + (size_t)i * ldy;
     for (int t = 0; t < k; ++t) {
-      float v = y[t];
+      T v = y[t];
       for (int s = 0; s < t; ++s) v -= y[s] * S[s * k + t];
       y[t] = v / S[t * k + t];
     }
@@ -384,27 +390,29 @@ __device__ inline bool cta_cholqr(float* Y, int n, int k, int ldy, float* S, int
 }
 
 // Modified Gram-Schmidt fallback (serial over columns, parallel over rows).
-__device__ inline void cta_mgs(float* Y, int n, int k, int ldy, double* red) {
+template <typename T>
+__device__ inline void cta_mgs(T* Y, int n, int k, int ldy, double* red) {
   for (int t = 0; t < k; ++t) {
     for (int s = 0; s < t; ++s) {
       double dot = 0.0;
       for (int i = threadIdx.x; i < n; i += blockDim.x) dot += (double)Y[(size_t)i * ldy + s] * Y[(size_t)i * ldy + t];
       dot = cta_sum(dot, red);
-      for (int i = threadIdx.x; i < n; i += blockDim.x) Y[(size_t)i * ldy + t] -= (float)dot * Y[(size_t)i * ldy + s];
+      for (int i = threadIdx.x; i < n; i += blockDim.x) Y[(size_t)i * ldy + t] -= T(dot) * Y[(size_t)i * ldy + s];
       __syncthreads();
     }
     double nn = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) nn += (double)Y[(size_t)i * ldy + t] * Y[(size_t)i * ldy + t];
     nn = cta_sum(nn, red);
-    const float sc = nn > 0.0 ? (float)(1.0 / sqrt(nn)) : 0.f;
+    const T sc = nn > 0.0 ? T(1.0 / sqrt(nn)) : T(0.);
     for (int i = threadIdx.x; i < n; i += blockDim.x) Y[(size_t)i * ldy + t] *= sc;
     __syncthreads();
   }
 }
 
 // Apply Q = H_0 ... H_{n-3} to Y (n x k):  Y <- Q Y.
-__device__ inline void cta_back_transform(const float* A, int n, int lda, const float* tau, float* Y, int k, int ldy,
-                                          float* cvec) {
+template <typename T>
+__device__ inline void cta_back_transform(const T* A, int n, int lda, const T* tau, T* Y, int k, int ldy,
+                                          T* cvec) {
   const int tid = threadIdx.x, nt = blockDim.x;
   int g = nt / (k > 0 ? k : 1);
   if (g > 32) g = 32;
@@ -418,7 +426,7 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
   while (gx * 2 <= k && gx * 2 <= nt) gx *= 2;
   const int gy = nt / gx;
   const int ux = tid % gx, uy = tid / gx;
-  float* cv2 = cvec + k;
+  T* cv2 = cvec + k;
   int j = n - 3;
   // pairs: Y <- H_{j-1} H_j Y in one reduction and one update.  With
   // a = v_j^T Y, b = v_{j-1}^T Y and sg = v_{j-1}^T v_j:
@@ -426,19 +434,19 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
   //   Y -= v_j c_j^T + v_{j-1} c_{j-1}^T.
   // Rows are indexed from j (v_{j-1}[j] = 1, v_j[j] = 0, v_j[j+1] = 1).
   for (; j >= 1; j -= 2) {
-    const float t1 = tau[j], t0 = tau[j - 1];
-    if (t1 == 0.f && t0 == 0.f) continue;
+    const T t1 = tau[j], t0 = tau[j - 1];
+    if (t1 == T(0.) && t0 == T(0.)) continue;
     const int m = n - j;
     for (int t = grp; t < k; t += ngroups) {
-      float a = 0.f, b = 0.f, sg = 0.f;
+      T a = T(0.), b = T(0.), sg = T(0.);
       for (int i = lig; i < m; i += g) {
         const int row = j + i;
-        const float y = Y[(size_t)row * ldy + t];
-        const float vb = (i == 0) ? 1.f : A[(size_t)row * lda + (j - 1)];
-        const float va = (i == 0) ? 0.f : ((i == 1) ? 1.f : A[(size_t)row * lda + j]);
-        a = fmaf(va, y, a);
-        b = fmaf(vb, y, b);
-        sg = fmaf(va, vb, sg);
+        const T y = Y[(size_t)row * ldy + t];
+        const T vb = (i == 0) ? T(1.) : A[(size_t)row * lda + (j - 1)];
+        const T va = (i == 0) ? T(0.) : ((i == 1) ? T(1.) : A[(size_t)row * lda + j]);
+        a = vfma(va, y, a);
+        b = vfma(vb, y, b);
+        sg = vfma(va, vb, sg);
       }
 #ifndef VMC_HOST_EMULATION
       for (int o = g / 2; o > 0; o >>= 1) {
@@ -448,7 +456,7 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
       }
 #endif
       if (lig == 0) {
-        const float cj = t1 * a;
+        const T cj = t1 * a;
         cvec[t] = cj;
         cv2[t] = t0 * (b - sg * cj);
       }
@@ -456,22 +464,22 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
     __syncthreads();
     for (int i = uy; i < m; i += gy) {
       const int row = j + i;
-      const float vb = (i == 0) ? 1.f : A[(size_t)row * lda + (j - 1)];
-      const float va = (i == 0) ? 0.f : ((i == 1) ? 1.f : A[(size_t)row * lda + j]);
-      float* yrow = Y + (size_t)row * ldy;
+      const T vb = (i == 0) ? T(1.) : A[(size_t)row * lda + (j - 1)];
+      const T va = (i == 0) ? T(0.) : ((i == 1) ? T(1.) : A[(size_t)row * lda + j]);
+      T* yrow = Y + (size_t)row * ldy;
       for (int t = ux; t < k; t += gx) yrow[t] -= va * cvec[t] + vb * cv2[t];
     }
     __syncthreads();
   }
   // a last unpaired reflector (j == 0)
   for (; j >= 0; --j) {
-    const float tj = tau[j];
-    if (tj == 0.f) continue;
+    const T tj = tau[j];
+    if (tj == T(0.)) continue;
     const int m = n - j - 1;
     for (int t = grp; t < k; t += ngroups) {
-      float s = 0.f;
+      T s = T(0.);
       for (int i = lig; i < m; i += g)
-        s = fmaf(i == 0 ? 1.f : A[(size_t)(j + 1 + i) * lda + j], Y[(size_t)(j + 1 + i) * ldy + t], s);
+        s = vfma(i == 0 ? T(1.) : A[(size_t)(j + 1 + i) * lda + j], Y[(size_t)(j + 1 + i) * ldy + t], s);
 #ifndef VMC_HOST_EMULATION
       for (int o = g / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, g);
 #endif
@@ -479,8 +487,8 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
     }
     __syncthreads();
     for (int i = uy; i < m; i += gy) {
-      const float vi = (i == 0) ? 1.f : A[(size_t)(j + 1 + i) * lda + j];
-      float* yrow = Y + (size_t)(j + 1 + i) * ldy;
+      const T vi = (i == 0) ? T(1.) : A[(size_t)(j + 1 + i) * lda + j];
+      T* yrow = Y + (size_t)(j + 1 + i) * ldy;
       for (int t = ux; t < k; t += gx) yrow[t] -= vi * cvec[t];
     }
     __syncthreads();
@@ -489,14 +497,16 @@ __device__ inline void cta_back_transform(const float* A, int n, int lda, const 
 }
 
 // Scratch for cta_sym_topk (all pointers into shared or global memory).
-struct EigScratch {
-  float *d, *e, *e2, *tau, *v, *p, *lam, *cvec, *part;
-  float* yr;               // complex solves: real n*k eigenvectors of T before the back-transform
-  float* S;                // k*k
-  float* lu;               // k * 4 * n
+template <typename T>
+struct EigScratchT {
+  T *d, *e, *e2, *tau, *v, *p, *lam, *cvec, *part;
+  T* yr;               // complex solves: real n*k eigenvectors of T before the back-transform
+  T* S;                // k*k
+  T* lu;               // k * 4 * n
   unsigned char* sw;       // k * n
   int* flag;
 };
+using EigScratch = EigScratchT<float>;
 
 // Y (n x k, row stride ldy) <- orthonormal basis of the dominant k-dimensional
 // invariant subspace of the symmetric matrix G (destroyed).  lam[0..kk-1]
@@ -504,14 +514,15 @@ struct EigScratch {
 // Y (n x k, real, row stride ldy) <- orthonormal eigenvectors of the k
 // largest eigenvalues of the tridiagonal (w.d, w.e); w.lam receives the
 // min(k+1, n) largest eigenvalues.
-__device__ inline void tri_topk_vectors(int n, int k, float* Y, int ldy, const EigScratch& w, double* red) {
+template <typename T>
+__device__ inline void tri_topk_vectors(int n, int k, T* Y, int ldy, const EigScratchT<T>& w, double* red) {
   VMC_TSTART(t1);
   const int kk = k + 1 <= n ? k + 1 : n;
-  const float tnorm = cta_top_eigenvalues(w.d, w.e, w.e2, n, kk, w.lam);
+  const T tnorm = cta_top_eigenvalues(w.d, w.e, w.e2, n, kk, w.lam);
   VMC_TSTOP(t1, PH_BISECT);
   VMC_TSTART(t2);
   for (int t = threadIdx.x; t < k; t += blockDim.x) {
-    float* lu = w.lu + (size_t)t * 4 * n;
+    T* lu = w.lu + (size_t)t * 4 * n;
     tri_inverse_iteration(w.d, w.e, n, w.lam[t], tnorm, Y + t, ldy, lu, lu + n, lu + 2 * n, lu + 3 * n,
                           w.sw + (size_t)t * n, 977u * (unsigned)t + 1u);
   }
@@ -521,8 +532,8 @@ __device__ inline void tri_topk_vectors(int n, int k, float* Y, int ldy, const E
   if (threadIdx.x == 0) {
     int start = 0;
     for (int t = 1; t < k; ++t) {
-      if (w.lam[t - 1] - w.lam[t] < 1e-3f * tnorm) {
-        float* lu = w.lu + (size_t)t * 4 * n;
+      if (w.lam[t - 1] - w.lam[t] < Tol<T>::cluster * tnorm) {
+        T* lu = w.lu + (size_t)t * 4 * n;
         tri_inverse_iteration(w.d, w.e, n, w.lam[t], tnorm, Y + t, ldy, lu, lu + n, lu + 2 * n, lu + 3 * n,
                               w.sw + (size_t)t * n, 977u * (unsigned)t + 1u, Y + start, t - start);
       } else {
@@ -540,7 +551,8 @@ __device__ inline void tri_topk_vectors(int n, int k, float* Y, int ldy, const E
   VMC_TSTOP(t3, PH_CHOLQR);
 }
 
-__device__ inline void cta_sym_topk(float* G, int n, int ldg, int k, float* Y, int ldy, const EigScratch& w,
+template <typename T>
+__device__ inline void cta_sym_topk(T* G, int n, int ldg, int k, T* Y, int ldy, const EigScratchT<T>& w,
                                     double* red) {
   VMC_TSTART(t0);
   cta_tridiagonalize(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);

@@ -53,10 +53,12 @@ class PEPSEngine:
     """Plan + workspace for one (shape, D, chi, d, strategy, operator)."""
 
     def __init__(self, shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, operator=None,
-                 device=None, lib=None, dtype="float32", options=None):
-        """``options``: the plan's launch configuration -- None (defaults, or the VMC_* environment), a
-        dict with keys threads / smem_kb / tile_policy (vmc_plan_options), or "auto" for the
-        autotuned choice of this (lattice, D, chi, dtype, strategy) from vmc_gb300.autotune."""
+                 device=None, lib=None, dtype="float32", options=None, precision=None):
+        """``options``: the plan's launch configuration -- None (defaults), a dict with keys threads /
+        smem_kb / tile_policy / precision / trunc_method / vchunk / vert_smem (vmc_plan_options), or
+        "auto" for the autotuned choice of this (lattice, D, chi, dtype, strategy, precision) from
+        vmc_gb300.autotune.  ``precision``: "fp32" (default) or "mixed" -- the boundary-MPS chain in
+        FP64, everything else FP32 (overrides the options' precision)."""
         self.shape = (int(shape[0]), int(shape[1]))
         self.complex = str(dtype).replace("torch.", "") in ("complex64", "complex128")
         # dtypes of this engine's parameters / O_k and of E_loc
@@ -88,10 +90,12 @@ class PEPSEngine:
             options = tuned_options(self.shape, self.bond_dim, self.chi, self.phys_dim, strategy, n_sweeps,
                                     "complex64" if self.complex else "float32", operator=operator,
                                     device=self.device, lib=lib)
+        if precision is not None:
+            options = dict(options or {})
+            options["precision"] = precision
         self.options = None if options is None else dict(options)
         dt = _abi.VMC_DTYPE_C64 if self.complex else _abi.VMC_DTYPE_F32
-        o = None if options is None else _abi.VmcPlanOptions(
-            int(options.get("threads", 0)), int(options.get("smem_kb", -1)), int(options.get("tile_policy", 0)))
+        o = None if options is None else _abi.plan_options(options)
         with torch.cuda.device(self.device) if self.device.type == "cuda" else _null():
             st = self._make_plan(lib, _abi.VmcShape(*self.shape), dt, sid, int(n_sweeps), o, plan)
         _abi.check(lib, st, "vmc_peps_plan")
@@ -390,16 +394,23 @@ class PEPSBatch:
             self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
         return eng0.lib, eng0
 
-    def run(self, jobs):
+    LAYOUTS = {None: _abi.VMC_BATCH_LAYOUT_AUTO, "auto": _abi.VMC_BATCH_LAYOUT_AUTO,
+               "plan": _abi.VMC_BATCH_LAYOUT_PLAN, "shared": _abi.VMC_BATCH_LAYOUT_PLAN,
+               "slot": _abi.VMC_BATCH_LAYOUT_SLOT}
+
+    def run(self, jobs, layout=None):
+        """``layout``: buffer placement of the launch -- None / "auto" (by cost share), "plan" (each
+        plan's shared-memory placement) or "slot" (every buffer in the CTA's workspace slot)."""
         lib, eng0 = self._setup(jobs)
+        lay = self.LAYOUTS[layout]
         arr = (_abi.VmcPepsJob * len(jobs))(*[j.c_struct() for j in jobs])
-        need = int(lib.vmc_batch_workspace_size(arr, len(jobs)))
+        need = int(lib.vmc_batch_workspace_size_ex(arr, len(jobs), lay))
         if need == 0:
             raise ValueError("invalid batch (missing buffers, or plans of different element type or CTA size)")
         if self._ws is None or self._ws.numel() < need:
             self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
-        st = lib.vmc_peps_batch(arr, len(jobs), eng0._stream(), _vp(self._ws), self._ws.numel(),
-                                _vp(self._status))
+        st = lib.vmc_peps_batch_ex(arr, len(jobs), lay, eng0._stream(), _vp(self._ws), self._ws.numel(),
+                                   _vp(self._status))
         _abi.check(lib, st, "vmc_peps_batch")
         return [j.out for j in jobs]
 
