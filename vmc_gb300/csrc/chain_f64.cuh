@@ -147,6 +147,7 @@ __device__ __noinline__ double apply_row_hp(const DevPlan& P, Shared& sh, const 
       cta_round_copy(out32, out, n_el);
       continue;
     }
+    VMC_TSTART(tth);
     // Z1[k][l][p][r'] = sum_d carry[k][l][d] m[d][p][r']
     cta_gemm_x(make_gemm_x(static_cast<const double*>(carry), lin(din), 1, m, lin(1), pin * dn, Z1, lin(pin * dn),
                            lin(1), kc * Lb, pin * dn, din));
@@ -167,6 +168,7 @@ __device__ __noinline__ double apply_row_hp(const DevPlan& P, Shared& sh, const 
     double* mat = ar.mat;
     cta_gemm_x(make_gemm_x(static_cast<const double*>(Z1), two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat,
                            two(dn, pout * ldm, Rb), two(Rb, ldm, 1), kc * dn, pout * Rb, Lb * pin));
+    VMC_TSTOP(tth, PH_THETA);
     if (mrows <= ncols && kout >= mrows) {
       // every row direction is kept: U = I, carry = theta
       for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) out[e] = (e / mrows == e % mrows) ? 1.0 : 0.0;
@@ -187,10 +189,12 @@ __device__ __noinline__ double apply_row_hp(const DevPlan& P, Shared& sh, const 
       const int nG = rows_side ? mrows : ncols;
       const int ldg = nG | 1;
       const double* cm = mat;
+      VMC_TSTART(tg);
       if (rows_side)  // G = theta theta^T
         cta_gemm_x(make_gemm_x(cm, lin(ldm), 1, cm, lin(ldm), 1, ar.G, lin(ldg), lin(1), nG, nG, ncols));
       else  // G = theta^T theta
         cta_gemm_x(make_gemm_x(cm, lin(1), ldm, cm, lin(1), ldm, ar.G, lin(ldg), lin(1), nG, nG, mrows));
+      VMC_TSTOP(tg, PH_GRAM);
       cta_sym_topk<double>(ar.G, nG, ldg, kout, ar.Y, kout, ar.eig, sh.red);
       if (threadIdx.x == 0 && kout < nG) {
         const double lk = ar.eig.lam[kout - 1], lk1 = ar.eig.lam[kout];
@@ -220,8 +224,10 @@ __device__ __noinline__ double apply_row_hp(const DevPlan& P, Shared& sh, const 
         __syncthreads();
       }
       // carry'[k'][w][r'] = sum_i U[i][k'] theta[i][(r',w)]
+      VMC_TSTART(tc);
       cta_gemm_x(make_gemm_x(static_cast<const double*>(out), lin(1), kout, cm, lin(1), ldm, carry_next, lin(ncols),
                              two(Rb, 1, dn), kout, ncols, mrows));
+      VMC_TSTOP(tc, PH_CARRY);
     }
     logsum += cta_normalize_d(carry_next, kout * ncols, sh.red);
     logsum += cta_normalize_d(out, mrows * kout, sh.red);

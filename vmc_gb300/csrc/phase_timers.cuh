@@ -10,7 +10,7 @@ namespace vmc {
 // of every CTA accumulates clock64() deltas.  Off in the product build.
 enum Phase { PH_T_RENV = 0, PH_T_METRO, PH_T_ZIP, PH_JACOBI, PH_E_RENV, PH_E_LEFT, PH_E_VERT, PH_B_ZIP, PH_CHAIN,
              PH_GRAM, PH_TRIDIAG, PH_BISECT, PH_INVIT, PH_CHOLQR, PH_BACK, PH_CARRY, PH_V_RIGHT, PH_V_LEFT,
-             PH_COUNT };
+             PH_THETA, PH_COUNT };
 #if defined(VMC_PHASE_TIMERS) && !defined(VMC_HOST_EMULATION)
 static __device__ unsigned long long g_phase[PH_COUNT];
 #define VMC_TSTART(v) long long v = clock64()

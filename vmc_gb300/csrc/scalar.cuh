@@ -45,7 +45,7 @@ struct Tol<double> {
   static constexpr double inv_tiny = 2.3e-16;
   static constexpr double chol_min = 1e-24;
   static constexpr double cluster = 1e-6;
-  static constexpr int inv_iters = 3;
+  static constexpr int inv_iters = 2;
 };
 
 __device__ __forceinline__ float warp_sum_t(float v) {

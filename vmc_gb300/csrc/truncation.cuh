@@ -508,17 +508,138 @@ struct EigScratchT {
 };
 using EigScratch = EigScratchT<float>;
 
-// Y (n x k, row stride ldy) <- orthonormal basis of the dominant k-dimensional
-// invariant subspace of the symmetric matrix G (destroyed).  lam[0..kk-1]
-// receives the kk = min(k+1, n) largest eigenvalues.
-// Y (n x k, real, row stride ldy) <- orthonormal eigenvectors of the k
-// largest eigenvalues of the tridiagonal (w.d, w.e); w.lam receives the
-// min(k+1, n) largest eigenvalues.
+// The kk largest eigenvalues of the tridiagonal in w (descending, into w.lam);
+// returns the Gershgorin scale |T|.
+__device__ inline float top_eigenvalues(const EigScratchT<float>& w, int n, int kk) {
+  return cta_top_eigenvalues(w.d, w.e, w.e2, n, kk, w.lam);
+}
+
+// High 32 bits of an FP64 value: its sign and exponent, tested with integer
+// instructions (FP64 compares also issue to the FP64 pipe).
+__device__ __forceinline__ int hi_word(double x) {
+#ifdef VMC_HOST_EMULATION
+  long long b;
+  std::memcpy(&b, &x, 8);
+  return (int)(b >> 32);
+#else
+  return __double2hiint(x);
+#endif
+}
+__device__ __forceinline__ int exp_bits(int hi) { return (hi >> 20) & 0x7ff; }
+
+// Characteristic polynomial of the leading principal submatrices of T at x:
+// p_i = det(T_i - x I) = (d_{i-1} - x) p_{i-1} - e2_{i-2} p_{i-2}, with its
+// x-derivative when want_deriv.  Returns the number of eigenvalues of T below
+// x (sign changes along p_0..p_n); *f and *fp receive p_n and p_n' scaled by
+// one common power of two.  A minor within ~2^-930 of its predecessor is
+// replaced by -2^-930 times it (the ratio form's pivmin guard), and the pair
+// is rescaled by 2^-/+600 to stay in range.  No divisions: FP64 division costs
+// many FP64 multiply-adds.
+template <bool want_deriv>
+__device__ __forceinline__ int char_poly(const double* d, const double* e2, int n, double x, double* f, double* fp) {
+  double a = 1.0, b = d[0] - x, ap = 0.0, bp = -1.0;
+  if (exp_bits(hi_word(b)) < 1023 - 930) b = -0x1p-930;
+  int cnt = hi_word(b) < 0;
+  for (int i = 1; i < n; ++i) {
+    const double dmx = d[i] - x;
+    double c = fma(dmx, b, -e2[i - 1] * a);
+    if (want_deriv) {
+      const double cp = fma(dmx, bp, -fma(e2[i - 1], ap, b));
+      ap = bp;
+      bp = cp;
+    }
+    const int hb = hi_word(b);
+    int hc = hi_word(c);
+    if (exp_bits(hc) + 930 < exp_bits(hb)) {
+      c = -0x1p-930 * b;
+      hc = hi_word(c);
+    }
+    cnt += (hc < 0) != (hb < 0);
+    a = b;
+    b = c;
+    const int eb = exp_bits(hc);
+    if (eb > 1023 + 600 || (eb < 1023 - 600 && exp_bits(hi_word(a)) < 1023 - 600)) {
+      const double sc = eb > 1023 ? 0x1p-600 : 0x1p600;
+      a *= sc;
+      b *= sc;
+      if (want_deriv) {
+        ap *= sc;
+        bp *= sc;
+      }
+    }
+  }
+  *f = b;
+  *fp = bp;
+  return cnt;
+}
+
+// FP64 eigenvalues for the boundary-MPS chain of mixed-precision plans.  FP32
+// multisection on the rounded tridiagonal gives each eigenvalue to a few FP32
+// ulps of |T|; from that start a Newton iteration on p_n, guarded by the
+// bracket that the same recurrence's Sturm count maintains (a step leaving
+// the bracket bisects instead), converges to 1e-13 |T| in a few evaluations.
+// The bracket starts at +-4e-6 |T| around the FP32 value and widens to the
+// Gershgorin interval if its counts disagree.  w.v and w.p (free between the
+// tridiagonalisation and the back-transform) hold the FP32 copies.
+__device__ inline double top_eigenvalues(const EigScratchT<double>& w, int n, int kk) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  float* d32 = reinterpret_cast<float*>(w.v);
+  float* e32 = d32 + n;
+  float* e2_32 = reinterpret_cast<float*>(w.p);
+  float* lam32 = e2_32 + n;
+  for (int i = tid; i < n; i += nt) {
+    d32[i] = (float)w.d[i];
+    if (i < n - 1) {
+      e32[i] = (float)w.e[i];
+      w.e2[i] = w.e[i] * w.e[i];
+    }
+  }
+  __syncthreads();
+  cta_top_eigenvalues(d32, e32, e2_32, n, kk, lam32);
+  double lo = 1.7e308, hi = -1.7e308;
+  for (int i = 0; i < n; ++i) {
+    const double r = (i > 0 ? fabs(w.e[i - 1]) : 0.0) + (i < n - 1 ? fabs(w.e[i]) : 0.0);
+    lo = fmin(lo, w.d[i] - r);
+    hi = fmax(hi, w.d[i] + r);
+  }
+  const double tnorm = fmax(fabs(lo), fabs(hi));
+  // Near a root the evaluated p_n / p_n' carries rounding noise well above
+  // 1e-13 |T|, so Newton stops at 1e-11 |T|: two inverse-iteration steps then
+  // leave (1e-11 |T| / gap)^2 of a neighbouring eigenvector in the vector, and
+  // the eigen-gaps at the cuts stay above ~1e-6 |T|.
+  const double span = hi - lo, tol = 1e-11 * tnorm + 1e-280;
+  lo -= 1e-12 * span + 1e-280;
+  hi += 1e-12 * span + 1e-280;
+  for (int t = tid; t < kk; t += nt) {
+    const int idx = n - 1 - t;  // the eigenvalue with idx others below it: count(a) <= idx < count(b)
+    const double c = (double)lam32[t], delta = 4e-6 * tnorm;
+    double a = c - delta, b = c + delta, f, fp;
+    if (!(a > lo) || char_poly<false>(w.d, w.e2, n, a, &f, &fp) > idx) a = lo;
+    if (!(b < hi) || char_poly<false>(w.d, w.e2, n, b, &f, &fp) <= idx) b = hi;
+    double x = fmin(fmax(c, a), b);
+    for (int it = 0; it < 64; ++it) {
+      const int cx = char_poly<true>(w.d, w.e2, n, x, &f, &fp);
+      if (cx <= idx)
+        a = x;
+      else
+        b = x;
+      double xn = (fp != 0.0) ? x - f / fp : 0.5 * (a + b);
+      if (!(xn > a && xn < b)) xn = 0.5 * (a + b);
+      const bool done = fabs(xn - x) <= tol || b - a <= tol;
+      x = xn;
+      if (done) break;
+    }
+    w.lam[t] = x;
+  }
+  __syncthreads();
+  return tnorm;
+}
+
 template <typename T>
 __device__ inline void tri_topk_vectors(int n, int k, T* Y, int ldy, const EigScratchT<T>& w, double* red) {
   VMC_TSTART(t1);
   const int kk = k + 1 <= n ? k + 1 : n;
-  const T tnorm = cta_top_eigenvalues(w.d, w.e, w.e2, n, kk, w.lam);
+  const T tnorm = top_eigenvalues(w, n, kk);
   VMC_TSTOP(t1, PH_BISECT);
   VMC_TSTART(t2);
   for (int t = threadIdx.x; t < k; t += blockDim.x) {
