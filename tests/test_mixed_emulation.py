@@ -40,7 +40,7 @@ CASES = [
 
 @pytest.mark.parametrize("shape,D,chi,strategy,model", CASES)
 @pytest.mark.parametrize("full", [False, True])
-@pytest.mark.parametrize("smem_kb", [-1, 200], ids=["arena-in-slot", "arena-in-smem"])
+@pytest.mark.parametrize("smem_kb", [0, -1, 200], ids=["arena-in-slot", "default-budget", "arena-in-smem"])
 def test_mixed_sweep_matches_oracle(emu_lib, shape, D, chi, strategy, model, full, smem_kb):
     H = hamiltonian(model, shape)
     T, cfg, u = make_case(shape, D, 6, seed=D + chi)

@@ -25,15 +25,18 @@ struct ArenaD {
   EigScratchT<double> eig;
 };
 
-// Layout mirrored by arena_doubles() in peps_plan.cuh.
-__device__ inline ArenaD make_arena_d(const DevPlan& P, double* p) {
+// Layout mirrored by arena_doubles() / arena_split_doubles() in
+// peps_plan.cuh.  With P.mat_in_smem == 0, theta and the inverse-iteration
+// factors live at g (the slot) and the rest at p (shared memory).
+__device__ inline ArenaD make_arena_d(const DevPlan& P, double* p, double* g) {
   ArenaD a;
   const int nmax = P.nmax, ld = P.nmax | 1, kmax = P.kmax;
-  a.mat = p; p += al32((long long)nmax * ld);
+  double*& q = P.mat_in_smem ? p : g;
+  a.mat = q; q += al32((long long)nmax * ld);
+  a.eig.lu = q; q += al32(4LL * kmax * nmax);
   a.G = p; p += al32((long long)nmax * ld);
   a.Y = p; p += al32((long long)nmax * kmax);
   a.eig.S = p; p += al32((long long)kmax * kmax);
-  a.eig.lu = p; p += al32(4LL * kmax * nmax);
   a.eig.sw = reinterpret_cast<unsigned char*>(p); p += al32(((long long)kmax * nmax + 7) / 8);
   a.eig.d = p; p += al32(nmax);
   a.eig.e = p; p += al32(nmax);
@@ -91,7 +94,7 @@ __device__ inline void fill_ones_row_d(const DevPlan& P, double* row) {
 // The FP64 buffers of one chain's boundary-MPS chain: rows, carries and Z1
 // carved from the slot's FP64 region (layout mirrored by chain_f64_doubles()
 // in peps_plan.cuh), the arena at `arena` (shared memory or the slot's arena
-// region).
+// region) with its split-out part at `arena_g` (the slot's arena region).
 struct ChainD {
   double* row[2];  // current and next boundary MPS (C tensors at stride TS)
   double* carry[2];
@@ -99,12 +102,12 @@ struct ChainD {
   ArenaD ar;
 };
 
-__device__ inline ChainD make_chain_d(const DevPlan& P, double* p, double* arena) {
+__device__ inline ChainD make_chain_d(const DevPlan& P, double* p, double* arena, double* arena_g) {
   ChainD c;
   for (int i = 0; i < 2; ++i) { c.row[i] = p; p += al32((long long)P.C * P.TS); }
   for (int i = 0; i < 2; ++i) { c.carry[i] = p; p += al32(P.SCR); }
   c.z1 = p;
-  c.ar = make_arena_d(P, arena);
+  c.ar = make_arena_d(P, arena, arena_g);
   return c;
 }
 

@@ -1,0 +1,93 @@
+// df64.cuh -- double-float arithmetic: a value is an unevaluated sum hi + lo
+// of two FP32 numbers (about 48 significant bits, FP32 exponent range).
+//
+// On this GPU a native FP64 multiply-add issues at a small fraction of the
+// FP32 rate, so the O(n^3) parts of the mixed-precision truncation run on
+// FP32 units in this representation instead: a df64 multiply-add is ~18 FP32
+// instructions.  The operations are the classical error-free transformations
+// (Knuth's two-sum, Dekker's product through fmaf); additions use the
+// "sloppy" two-sum variant, whose error is bounded by ~2^-44 of the larger
+// operand -- ample for a Householder reduction whose result is used to 1e-13
+// of the matrix norm.  Every step uses the _rn intrinsics so the compiler
+// never contracts or reorders them.
+#pragma once
+
+#include "portability.cuh"
+#include "scalar.cuh"
+
+namespace vmc {
+
+#ifdef VMC_HOST_EMULATION
+inline float __fadd_rn(float a, float b) { return a + b; }
+inline float __fsub_rn(float a, float b) { return a - b; }
+inline float __fmul_rn(float a, float b) { return a * b; }
+#endif
+
+struct df64 {
+  float hi, lo;
+  df64() = default;
+  __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
+  // from FP64 (constants and the conversion at the edges of a df64 routine)
+  __device__ __forceinline__ df64(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+  __device__ __forceinline__ explicit df64(int i) : hi((float)i), lo(0.f) {}
+  __device__ __forceinline__ double to_double() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ df64 df_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df64(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df64 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return df64(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  df64 s = df_two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return df_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+// division and square root are rare (a few per Householder column): FP64
+__device__ __forceinline__ df64 operator/(df64 a, df64 b) { return df64(a.to_double() / b.to_double()); }
+__device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
+__device__ __forceinline__ df64& operator-=(df64& a, df64 b) { return a = a - b; }
+__device__ __forceinline__ df64& operator*=(df64& a, df64 b) { return a = a * b; }
+// hi carries the sign and the order (|lo| <= ulp(hi) / 2)
+__device__ __forceinline__ bool operator<(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(df64 a, df64 b) { return b < a; }
+__device__ __forceinline__ bool operator==(df64 a, df64 b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator!=(df64 a, df64 b) { return !(a == b); }
+
+__device__ __forceinline__ df64 vfma(df64 a, df64 b, df64 c) { return a * b + c; }
+__device__ __forceinline__ df64 vsqrt(df64 a) { return df64(sqrt(a.to_double())); }
+__device__ __forceinline__ df64 vabs(df64 a) { return a.hi < 0.f ? -a : a; }
+__device__ __forceinline__ bool df_sign(float x) {
+#ifdef VMC_HOST_EMULATION
+  return std::signbit(x);
+#else
+  return signbit(x);
+#endif
+}
+__device__ __forceinline__ df64 vcopysign(df64 a, df64 b) { return df_sign(a.hi) == df_sign(b.hi) ? a : -a; }
+
+__device__ __forceinline__ df64 shfl_xor_t(unsigned mask, df64 v, int o, int width = 32) {
+  return df64(shfl_xor_t(mask, v.hi, o, width), shfl_xor_t(mask, v.lo, o, width));
+}
+__device__ __forceinline__ df64 warp_sum_t(df64 v) {
+#ifndef VMC_HOST_EMULATION
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = v + shfl_xor_t(0xffffffffu, v, o);
+#endif
+  return v;
+}
+
+}  // namespace vmc

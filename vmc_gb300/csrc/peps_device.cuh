@@ -1076,7 +1076,8 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   if (threadIdx.x == 0) g_tile_policy = P.tile_policy;  // read by cta_gemm after the next barrier
 #if VMC_CHAIN_F64
   // the FP64 chain's arena takes the place of the FP32 truncation arena
-  const ChainD ch = make_chain_d(P, S.h64, reinterpret_cast<double*>(P.arena_in_smem ? dyn_smem : S.arena));
+  const ChainD ch = make_chain_d(P, S.h64, reinterpret_cast<double*>(P.arena_in_smem ? dyn_smem : S.arena),
+                                 reinterpret_cast<double*>(S.arena));
 #else
   const Arena ar = make_arena(P, P.arena_in_smem ? dyn_smem : S.arena, S.arena);
 #endif

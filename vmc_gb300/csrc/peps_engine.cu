@@ -152,6 +152,7 @@ static vmc_status upload_plan(vmc_plan* pl) {
     G.arena_in_smem = L.arena_in_smem;
     G.mat_in_smem = L.mat_in_smem;
     G.arena_floats = L.arena_floats;
+    G.arena_g_floats = L.arena_g_floats;
     G.scr1 = L.scr1;
     G.vchunk = L.vchunk;
     G.vbuf = L.vbuf;
@@ -396,14 +397,17 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
     Q.arena_in_smem = 0;
     Q.mat_in_smem = 1;  // "theta lives inside the arena" (arena itself may be global)
     Q.arena_floats = trunc_all;
+    // a mixed plan splits out theta and the inverse-iteration factors (FP64)
+    const long long split_floats = Q.chain64 ? 2 * arena_split_doubles(Q.nmax, Q.kmax) : mat_floats;
     if (trunc_all * 4 <= budget) {
       Q.arena_in_smem = 1;
       Q.mat_in_smem = 1;
-    } else if (!Q.chain64 && (trunc_all - mat_floats) * 4 <= budget && Q.trunc_method == 0) {
+    } else if ((trunc_all - split_floats) * 4 <= budget && Q.trunc_method == 0) {
       Q.arena_in_smem = 1;
       Q.mat_in_smem = 0;
-      Q.arena_floats = trunc_all - mat_floats;
+      Q.arena_floats = trunc_all - split_floats;
     }
+    Q.arena_g_floats = Q.arena_in_smem ? (Q.mat_in_smem ? 0 : split_floats) : Q.arena_floats;
     Q.scr1 = (int)al64(es * std::max(chimax * chimax * D * D, (long long)D * D * D * D));
     {
       // one bond value of a vertical-energy intermediate holds <= chimax * D^3 floats
@@ -439,7 +443,7 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
                     3 * al64((long long)C * TS) +
                     al64((long long)d * C * ES) + al64((long long)(d + 1) * ES) + al64((long long)C * E2S) +
                     2 * al64(E2S) +
-                    (Q.arena_in_smem ? (Q.mat_in_smem ? 0 : mat_floats) : al64(Q.arena_floats)) +
+                    al64(Q.arena_g_floats) +
                     (long long)Q.n_scr * al64(SCR) + al64(2LL * C * Q.VS) +
                     (Q.chain64 ? 2 * chain_f64_doubles(C, TS, SCR) : 0);
   };

@@ -58,6 +58,7 @@ struct DevPlan {
   int threads;            // CTA size of the fused kernel
   int tile_policy;        // register-tile policy of the CTA GEMMs (cta_gemm)
   long long arena_floats;
+  long long arena_g_floats;  // floats of the truncation arena that live in the CTA's slot
   int scr1;               // size of one 1-row GEMM intermediate (floats)
   int vchunk, vbuf;       // vertical-energy chunk (bond values) and buffer size (floats)
   int vert_in_smem;       // vertical-energy buffers live in the shared-memory arena
@@ -130,8 +131,7 @@ __device__ inline Slot make_slot(const DevPlan& P, float* base) {
   s.lenv = p; p += al64((long long)(P.d + 1) * P.ES);
   s.r2 = p; p += al64((long long)P.C * P.E2S);
   for (int i = 0; i < 2; ++i) { s.l2[i] = p; p += al64(P.E2S); }
-  s.arena = p; p += P.arena_in_smem ? (P.mat_in_smem ? 0 : al64((long long)P.es * P.nmax * (P.nmax | 1)))
-                                    : al64(P.arena_floats);
+  s.arena = p; p += al64(P.arena_g_floats);
   for (int i = 0; i < P.n_scr; ++i) { s.scr[i] = p; p += al64(P.SCR); }
   s.venv = p; p += al64(2LL * P.C * P.VS);
   s.h64 = P.chain64 ? reinterpret_cast<double*>(p) : nullptr;
@@ -158,12 +158,18 @@ __host__ __device__ inline long long arena_floats(int nmax, int kmax, int trunc_
 }
 
 // Doubles of the FP64 truncation arena of a mixed-precision plan (layout:
-// make_arena_d in chain_f64.cuh).
+// make_arena_d in chain_f64.cuh), and of the part that can be split out into
+// the CTA's slot when the rest must fit shared memory: theta (read by the Gram
+// and carry GEMMs) and the inverse-iteration factors (one thread each, in
+// sequence).
 __host__ __device__ inline long long arena_doubles(int nmax, int kmax) {
   const int ld = nmax | 1;
   return 2 * al32((long long)nmax * ld) + al32((long long)nmax * kmax) + al32((long long)kmax * kmax) +
          al32(4LL * kmax * nmax) + al32(((long long)kmax * nmax + 7) / 8) + 6 * al32(nmax) + al32(nmax + 1) +
          al32(2LL * nmax) + al32(nmax + 64) + 32;
+}
+__host__ __device__ inline long long arena_split_doubles(int nmax, int kmax) {
+  return al32((long long)nmax * (nmax | 1)) + al32(4LL * kmax * nmax);
 }
 // Doubles of the FP64 chain buffers in a slot (make_chain_d): two boundary
 // rows, two carries and the Z1 intermediate.  The FP64 arena takes the place

@@ -48,6 +48,24 @@ struct Tol<double> {
   static constexpr int inv_iters = 2;
 };
 
+// lane exchange of a value of any of the scalar types (identity in the host build)
+__device__ __forceinline__ float shfl_xor_t(unsigned mask, float v, int o, int width = 32) {
+#ifndef VMC_HOST_EMULATION
+  return __shfl_xor_sync(mask, v, o, width);
+#else
+  (void)mask; (void)o; (void)width;
+  return v;
+#endif
+}
+__device__ __forceinline__ double shfl_xor_t(unsigned mask, double v, int o, int width = 32) {
+#ifndef VMC_HOST_EMULATION
+  return __shfl_xor_sync(mask, v, o, width);
+#else
+  (void)mask; (void)o; (void)width;
+  return v;
+#endif
+}
+
 __device__ __forceinline__ float warp_sum_t(float v) {
 #ifndef VMC_HOST_EMULATION
 #pragma unroll

@@ -17,6 +17,9 @@
 #include "device_common.cuh"
 #include "phase_timers.cuh"
 #include "scalar.cuh"
+#include "df64.cuh"
+
+#include <type_traits>
 
 namespace vmc {
 
@@ -119,7 +122,7 @@ __device__ inline void cta_tridiagonalize(T* A, int n, int lda, T* d, T* e, T* t
       for (; l < m; l += rg) s0 = vfma(row[l], l == 0 ? T(1.) : colj[(size_t)l * lda] * scal, s0);
       T s = (s0 + s1) + (s2 + s3);
 #ifndef VMC_HOST_EMULATION
-      for (int o = rg / 2; o > 0; o >>= 1) s += __shfl_xor_sync(rmask, s, o, rg);
+      for (int o = rg / 2; o > 0; o >>= 1) s += shfl_xor_t(rmask, s, o, rg);
 #endif
       const T pi = tj * s;
       if (rlane == 0) {
@@ -262,6 +265,9 @@ __device__ inline void tri_inverse_iteration(const T* d, const T* e, int n, T la
                                              unsigned char* sw, unsigned seed, const T* orth = nullptr,
                                              int n_orth = 0) {
   const T tiny = Tol<T>::inv_tiny * vmax(tnorm, T(1e-30));
+  // FP64: u0 holds the pivots' reciprocals (one division per row instead of
+  // one per row and iteration; FP64 division costs many FP64 multiply-adds)
+  constexpr bool kRecip = std::is_same<T, double>::value;
   T al = d[0] - lam;
   T be = n > 1 ? e[0] : T(0.);
 #pragma unroll 4
@@ -272,18 +278,32 @@ __device__ inline void tri_inverse_iteration(const T* d, const T* e, int n, T la
     if (vabs(al) >= vabs(c)) {
       T piv = al;
       if (vabs(piv) < tiny) piv = vcopysign(tiny, piv == T(0.) ? T(1.) : piv);
-      const T m = c / piv;
+      T m;
+      if constexpr (kRecip) {
+        const T r = T(1.) / piv;
+        m = c * r;
+        u0[i] = r;
+      } else {
+        m = c / piv;
+        u0[i] = piv;
+      }
       sw[i] = 0;
-      u0[i] = piv;
       u1[i] = be;
       u2[i] = T(0.);
       mul[i] = m;
       al = a1 - m * be;
       be = b1;
     } else {
-      const T m = al / c;
+      T m;
+      if constexpr (kRecip) {
+        const T r = T(1.) / c;
+        m = al * r;
+        u0[i] = r;
+      } else {
+        m = al / c;
+        u0[i] = c;
+      }
       sw[i] = 1;
-      u0[i] = c;
       u1[i] = a1;
       u2[i] = b1;
       mul[i] = m;
@@ -292,7 +312,7 @@ __device__ inline void tri_inverse_iteration(const T* d, const T* e, int n, T la
     }
   }
   if (vabs(al) < tiny) al = vcopysign(tiny, al == T(0.) ? T(1.) : al);
-  u0[n - 1] = al;
+  u0[n - 1] = kRecip ? T(1.) / al : al;
   // the back substitution reads these (times zero) at i = n-1: they must not hold stale data
   u1[n - 1] = T(0.);
   u2[n - 1] = T(0.);
@@ -321,7 +341,8 @@ __device__ inline void tri_inverse_iteration(const T* d, const T* e, int n, T la
     T xn1 = T(0.), xn2 = T(0.), amax = T(0.);
     #pragma unroll 4
     for (int i = n - 1; i >= 0; --i) {
-      const T xi = (x[(size_t)i * xs] - u1[i] * xn1 - u2[i] * xn2) / u0[i];
+      const T num = x[(size_t)i * xs] - u1[i] * xn1 - u2[i] * xn2;
+      const T xi = kRecip ? num * u0[i] : num / u0[i];
       x[(size_t)i * xs] = xi;
       xn2 = xn1;
       xn1 = xi;
@@ -450,9 +471,9 @@ __device__ inline void cta_back_transform(const T* A, int n, int lda, const T* t
       }
 #ifndef VMC_HOST_EMULATION
       for (int o = g / 2; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(gmask, a, o, g);
-        b += __shfl_xor_sync(gmask, b, o, g);
-        sg += __shfl_xor_sync(gmask, sg, o, g);
+        a += shfl_xor_t(gmask, a, o, g);
+        b += shfl_xor_t(gmask, b, o, g);
+        sg += shfl_xor_t(gmask, sg, o, g);
       }
 #endif
       if (lig == 0) {
@@ -481,7 +502,7 @@ __device__ inline void cta_back_transform(const T* A, int n, int lda, const T* t
       for (int i = lig; i < m; i += g)
         s = vfma(i == 0 ? T(1.) : A[(size_t)(j + 1 + i) * lda + j], Y[(size_t)(j + 1 + i) * ldy + t], s);
 #ifndef VMC_HOST_EMULATION
-      for (int o = g / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, g);
+      for (int o = g / 2; o > 0; o >>= 1) s += shfl_xor_t(gmask, s, o, g);
 #endif
       if (lig == 0) cvec[t] = tj * s;
     }
@@ -672,11 +693,43 @@ __device__ inline void tri_topk_vectors(int n, int k, T* Y, int ldy, const EigSc
   VMC_TSTOP(t3, PH_CHOLQR);
 }
 
+// Householder tridiagonalisation of an FP64 matrix carried out in df64 on the
+// FP32 units (df64.cuh): the matrix, the reflectors and T are converted in
+// place (a df64 takes the 8 bytes of a double), reduced, and converted back.
+__device__ inline void cta_tridiagonalize_df(double* G, int n, int ldg, const EigScratchT<double>& w) {
+  df64* A = reinterpret_cast<df64*>(G);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const size_t o = (size_t)(e / n) * ldg + e % n;
+    A[o] = df64(G[o]);
+  }
+  __syncthreads();
+  cta_tridiagonalize(A, n, ldg, reinterpret_cast<df64*>(w.d), reinterpret_cast<df64*>(w.e),
+                     reinterpret_cast<df64*>(w.tau), reinterpret_cast<df64*>(w.v), reinterpret_cast<df64*>(w.p),
+                     reinterpret_cast<df64*>(w.part));
+  // T and tau, then the reflectors (strictly below the diagonal), back to FP64
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    w.d[i] = reinterpret_cast<df64*>(w.d)[i].to_double();
+    w.e[i] = reinterpret_cast<df64*>(w.e)[i].to_double();
+    w.tau[i] = reinterpret_cast<df64*>(w.tau)[i].to_double();
+  }
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int r = e / n, c = e % n;
+    if (r > c) {
+      const size_t o = (size_t)r * ldg + c;
+      G[o] = A[o].to_double();
+    }
+  }
+  __syncthreads();
+}
+
 template <typename T>
 __device__ inline void cta_sym_topk(T* G, int n, int ldg, int k, T* Y, int ldy, const EigScratchT<T>& w,
                                     double* red) {
   VMC_TSTART(t0);
-  cta_tridiagonalize(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);
+  if constexpr (std::is_same<T, double>::value)
+    cta_tridiagonalize_df(G, n, ldg, w);
+  else
+    cta_tridiagonalize(G, n, ldg, w.d, w.e, w.tau, w.v, w.p, w.part);
   VMC_TSTOP(t0, PH_TRIDIAG);
   tri_topk_vectors(n, k, Y, ldy, w, red);
   VMC_TSTART(t4);
