@@ -39,15 +39,20 @@ def _worker_init():
 
 
 def _oracle_chunk(args):
-    """Time the FP64 NumPy restatement on one chunk of chains (runs in a worker process)."""
+    """Time the FP64 NumPy restatement on one chunk of chains (runs in a worker process).  With keep > 0
+    it also returns the first `keep` chains' sampled configurations, log|psi|, sign, E_loc and O_k: the
+    FP64 reference of the bench line's accuracy report."""
     import numpy as np
 
     from oracle import peps as oracle
     from vmc_gb300.synthetic import WORKLOADS, initial_configs, random_tensors, uniform_stream
 
-    wname, n, seed = args
+    wname, n, seed, keep = (tuple(args) + (0,))[:4]
     w = WORKLOADS[wname]
-    T = w.tensors(seed=0)
+    # the engine's inputs: the seeded tensors rounded to its FP32 (complex64) elements
+    rdt = np.complex64 if w.dtype == "complex64" else np.float32
+    T = [[np.asarray(t).astype(rdt).astype(np.complex128 if w.dtype == "complex64" else np.float64) for t in row]
+         for row in w.tensors(seed=0)]
     n_sites = w.shape[0] * w.shape[1]
     cfg = initial_configs(n, n_sites, w.phys_dim, seed=seed).astype(np.int64)
     u = next(uniform_stream(n, n_sites, seed=seed))
@@ -58,17 +63,98 @@ def _oracle_chunk(args):
     cache = init(T, cfg)
     t0 = time.perf_counter()
     c2, ctx = trans(T, cfg, u, cache)
-    est(T, c2, ctx)
+    _, le = est(T, c2, ctx)
+    dt = time.perf_counter() - t0
+    ref = None
+    if keep:
+        k = min(keep, n)
+        ref = {"configs": c2[:k], "logabs": np.log(np.abs(ctx.amp[:k])), "sign": np.sign(ctx.amp[:k]),
+               "E": le.local_estimate[:k], "O": le.local_log_derivatives[:k]}
+    return n, dt, ref
+
+
+GI_SHAPE, GI_DMAX, GI_CHI, GI_G = (9, 9), 2, 32, 0.8
+GI_METRIC = "GI-PEPS samples/s (plaquette sweep + grad log psi + E_loc), pure Z2 gauge 9x9, D=2/sector, chi=32"
+
+
+def _gi_oracle_chunk(args):
+    """Time the FP64 GI oracle (oracle/gi.py) on one chunk of chains of the pure-Z2 9x9 workload: bottom
+    environments, one plaquette sweep and the estimate (runs in a worker process)."""
+    import numpy as np
+
+    from oracle import gi
+    from oracle import peps as oracle
+
+    n, seed = args
+    cfg = gi.GIConfig(GI_SHAPE, 2, GI_DMAX)
+    T = gi.init_tensors(cfg, seed=0)
+    H = gi.z2_pure_gauge_hamiltonian(GI_SHAPE, h=1.0 / (2.0 * GI_G), g=GI_G / 2.0, N=2)
+    strat = oracle.ZipUp(GI_CHI)
+    R, C = GI_SHAPE
+    samples = gi.random_physical_configuration(cfg, n, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    u = rng.random((n, R - 1, C - 1))
+    deltas = np.ones((n, R - 1, C - 1), dtype=np.int64)
+    t0 = time.perf_counter()
+    cache = gi.init_cache(T, cfg, samples, strat)
+    samples, amp, top, _ = gi.transition(T, cfg, samples, deltas, u, cache, strat)
+    gi.estimate(T, cfg, samples, amp, H, strat, top)
     return n, time.perf_counter() - t0
 
 
-def cpu_oracle_rate(wname, n_per_worker, workers, pool):
-    """Samples/s of the oracle over `workers` processes (each one sweep of its chunk)."""
+def gi_oracle_rate(n_per_worker, workers, pool):
+    """Samples/s of the GI oracle over `workers` processes (each one sweep of its chunk)."""
     t0 = time.perf_counter()
-    res = pool.map(_oracle_chunk, [(wname, n_per_worker, 100 + i) for i in range(workers)])
+    res = pool.map(_gi_oracle_chunk, [(n_per_worker, 200 + i) for i in range(workers)])
+    wall = time.perf_counter() - t0
+    return sum(r[0] for r in res) / wall, sum(r[0] for r in res), wall
+
+
+def cpu_oracle_rate(wname, n_per_worker, workers, pool, keep=0):
+    """Samples/s of the oracle over `workers` processes (each one sweep of its chunk); with keep > 0 also
+    the FP64 outputs of the first `keep` chains of chunk 0 (seed 100)."""
+    t0 = time.perf_counter()
+    res = pool.map(_oracle_chunk, [(wname, n_per_worker, 100 + i, keep if i == 0 else 0) for i in range(workers)])
     wall = time.perf_counter() - t0
     n = sum(r[0] for r in res)
-    return n / wall, n, wall
+    return n / wall, n, wall, res[0][2]
+
+
+def accuracy_vs_oracle(eng, w, ref, dev):
+    """Errors of one engine sweep on the oracle chunk's first chains (seed-100 configurations and
+    uniforms, the same FP32 tensors) against the oracle's FP64 results: log psi (max abs), per-sample
+    E_loc (median / max of |dE| / max(1, |E|)), the batch-mean E relative to the energy scale mean|E_loc|
+    and relative to |mean E|, O_k (Frobenius over the batch), over the chains whose sampled
+    configurations agree (a differing chain had an accept decision within float rounding of its
+    threshold)."""
+    import numpy as np
+    import torch
+
+    from vmc_gb300.lowering import pack_tensors
+    from vmc_gb300.synthetic import initial_configs, uniform_stream
+
+    k = len(ref["E"])
+    n_sites = w.shape[0] * w.shape[1]
+    tens = torch.from_numpy(pack_tensors(w.tensors(seed=0))).to(dev)
+    cfg = torch.from_numpy(initial_configs(k, n_sites, w.phys_dim, seed=100)).to(dev)
+    u = torch.from_numpy(next(uniform_stream(k, n_sites, seed=100))).to(dev)
+    cache = eng.init_cache(tens, cfg)
+    res = eng.sweep(tens, cfg, u, cache)
+    torch.cuda.synchronize()
+    same = np.all(res.configs.cpu().numpy() == ref["configs"], axis=1)
+    la, sg = res.logamp.cpu().numpy()[same], res.sign.cpu().numpy()[same]
+    e, e_ref = res.E.cpu().numpy()[same], ref["E"][same]
+    o, o_ref = res.O.cpu().numpy()[same], ref["O"][same]
+    de = np.abs(e - e_ref)
+    return {"chains": int(k), "same_configs": float(same.mean()),
+            "logpsi_abs_max": float(np.max(np.abs(la - ref["logabs"][same]))),
+            "sign_agree": bool(np.all(sg == ref["sign"][same])),
+            "eloc_rel_median": float(np.median(de / np.maximum(1.0, np.abs(e_ref)))),
+            "eloc_rel_max": float(np.max(de / np.maximum(1.0, np.abs(e_ref)))),
+            "e_mean_vs_scale": float(abs(e.mean() - e_ref.mean()) / np.abs(e_ref).mean()),
+            "e_mean_rel": float(abs(e.mean() - e_ref.mean()) / abs(e_ref.mean())),
+            "o_frob_rel": float(np.linalg.norm(o - o_ref) / np.linalg.norm(o_ref)),
+            "min_gap": float(res.gap.min().item())}
 
 
 class ClockSampler:
@@ -128,9 +214,6 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-NCU_DRAM_BYTES_PER_SAMPLE = {"heis8x8_D4_chi16": 13.359e9 / 608}
-
-
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -147,14 +230,38 @@ def run_reference(args, rank, world):
 
     if rank != 0:
         return
-    if args.workload in ("uneven", "gi9x9"):
-        print(json.dumps({"impl": "reference", "unavailable": "the reference arm times single-lattice standard "
-                          "PEPS workloads (the uneven batch reports each lattice's own rate in per_shape)"}),
-              flush=True)
+    if args.workload == "uneven":
+        print(json.dumps({"impl": "reference", "unavailable": "the uneven batch has no single reference "
+                          "workload: it reports each lattice's own rate in per_shape"}), flush=True)
         return
-    w = WORKLOADS[args.workload]
     cores = len(os.sched_getaffinity(0))
     ctx = mp.get_context("spawn")
+    if args.workload == "gi9x9":
+        # one chain per core and step: ~36 s of FP64 NumPy per chain on one core
+        per = max(1, args.gi_ref_chains_per_core)
+        with ctx.Pool(cores, initializer=_worker_init) as pool:
+            for _ in range(args.warmup):
+                gi_oracle_rate(per, cores, pool)
+            t0 = time.perf_counter()
+            n_total = 0
+            for _ in range(args.steps):
+                n_total += gi_oracle_rate(per, cores, pool)[1]
+            wall = time.perf_counter() - t0
+        value = n_total / wall
+        print(json.dumps({
+            "impl": "reference", "metric": GI_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "gi9x9", "vertices": list(GI_SHAPE), "degeneracy_per_charge": [GI_DMAX, GI_DMAX],
+                       "chi": GI_CHI, "N": 2, "g": GI_G, "chains_per_step": per * cores,
+                       "parallelism": "host processes"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{per * cores} chains x 1 plaquette sweep + estimate per step, FP64 NumPy "
+                                       "GI oracle restatement (the reference's JAX CPU path cannot be installed)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
+        return
+    w = WORKLOADS[args.workload]
     per = max(1, args.ref_chains_per_core)
     with ctx.Pool(cores, initializer=_worker_init) as pool:
         for _ in range(args.warmup):
@@ -162,7 +269,7 @@ def run_reference(args, rank, world):
         t0 = time.perf_counter()
         n_total = 0
         for _ in range(args.steps):
-            _, n, _ = cpu_oracle_rate(args.workload, per, cores, pool)
+            _, n, _, _ = cpu_oracle_rate(args.workload, per, cores, pool)
             n_total += n
         wall = time.perf_counter() - t0
     value = n_total / wall
@@ -236,7 +343,8 @@ def shipped_options(w):
     engine's default) when the table has no entry for it."""
     from vmc_gb300 import autotune
 
-    return autotune.shipped_options(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype)
+    return autotune.shipped_options(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype,
+                                    operator=w.operator())
 
 
 def unfused_rate(eng, tens, cfg, args, barrier):
@@ -264,6 +372,52 @@ def unfused_rate(eng, tens, cfg, args, barrier):
     return n * args.steps / (t0.elapsed_time(t1) / 1e3)
 
 
+def time_sweeps(eng, tens, cfg0, uni, args, barrier, clock_index):
+    """Device-resident sweeps: W untimed, then K timed between barriers with CUDA events on the launch
+    stream (one pair per launch), nvidia-smi sampling clocks meanwhile.  Returns (elapsed s, per-launch
+    ms, clock summary)."""
+    import torch
+
+    cfg = cfg0.clone()
+    cache = eng.init_cache(tens, cfg)
+    out = None
+    for i in range(args.warmup):
+        out = eng.sweep(tens, cfg, uni[i], cache, out=out)
+    barrier()
+    eng.raise_on_status()
+    stream = torch.cuda.current_stream(eng.device)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(clock_index) as clocks:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            out = eng.sweep(tens, cfg, uni[args.warmup + i], cache, out=out)
+            ev[i][1].record(stream)
+        t_end.record(stream)
+        barrier()
+    eng.raise_on_status()
+    return t_start.elapsed_time(t_end) / 1e3, [x.elapsed_time(y) for x, y in ev], clocks.summary()
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per sample of the fused kernel, from one ncu
+# capture of one sweep launch of 608 chains (one wave) of the 8x8 D4 chi16 workload per precision; every
+# chain reuses its CTA's slot, so a launch's traffic scales with its chains.  The captures are summarised
+# in profiles/peps_kernel_heis8x8_D4_chi16.md (FP32) and profiles/peps_kernel_mixed_heis8x8_D4_chi16.md.
+NCU_DRAM_BYTES_PER_SAMPLE = {("heis8x8_D4_chi16", "fp32"): 13.359e9 / 608,
+                             ("heis8x8_D4_chi16", "mixed"): None}
+
+
+def precision_of(args, w):
+    """The headline tier: the mixed-precision engine (FP64 boundary-MPS chain) where it exists -- real
+    ZipUp / NoTruncation workloads -- since only it meets the accuracy bars; FP32 elsewhere."""
+    if args.precision != "auto":
+        return args.precision
+    return "mixed" if (w.dtype == "float32" and w.strategy in ("ZipUp", "NoTruncation")) else "fp32"
+
+
 def run_ours(args, rank, world, local_rank):
     import multiprocessing as mp
 
@@ -280,14 +434,17 @@ def run_ours(args, rank, world, local_rank):
 
     from vmc_gb300.engine import PEPSEngine
     from vmc_gb300.lowering import pack_tensors
-    from vmc_gb300.synthetic import WORKLOADS, initial_configs, random_tensors, uniform_stream
+    from vmc_gb300.synthetic import WORKLOADS, initial_configs, uniform_stream
 
     w = WORKLOADS[args.workload]
     n = args.chains or w.n_chains
     dev = torch.device(f"cuda:{local_rank}")
     torch.cuda.set_device(dev)
     n_sites = w.shape[0] * w.shape[1]
-    options = shipped_options(w)
+    prec = precision_of(args, w)
+    # the shipped launch table holds FP32 choices; the mixed tier runs its own defaults
+    fp32_options = shipped_options(w)
+    options = fp32_options if prec == "fp32" else {"precision": "mixed"}
     eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev,
                      dtype=w.dtype, options=options)
     tens = torch.from_numpy(pack_tensors(w.tensors(seed=0))).to(dev)
@@ -301,45 +458,35 @@ def run_ours(args, rank, world, local_rank):
             dist.barrier()
         torch.cuda.synchronize()
 
+    def max_over_ranks(x):
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     # ---------------- device-resident throughput (value) ----------------
-    cfg = cfg0.clone()
-    cache = eng.init_cache(tens, cfg)
-    out = None
-    for i in range(args.warmup):
-        out = eng.sweep(tens, cfg, uni[i], cache, out=out)
-    barrier()
-    eng.raise_on_status()
-    stream = torch.cuda.current_stream(dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier()
-    with ClockSampler(local_rank) as clocks:
-        t_start = torch.cuda.Event(enable_timing=True)
-        t_end = torch.cuda.Event(enable_timing=True)
-        t_start.record(stream)
-        for i in range(args.steps):
-            ev[i][0].record(stream)
-            out = eng.sweep(tens, cfg, uni[args.warmup + i], cache, out=out)
-            ev[i][1].record(stream)
-        t_end.record(stream)
-        barrier()
-    eng.raise_on_status()
-    elapsed = t_start.elapsed_time(t_end) / 1e3
-    launch_ms = [a.elapsed_time(b) for a, b in ev]
-    t_all = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t_all, op=dist.ReduceOp.MAX)
-    elapsed = float(t_all.item())
+    elapsed, launch_ms, clk = time_sweeps(eng, tens, cfg0, uni, args, barrier, local_rank)
+    elapsed = max_over_ranks(elapsed)
     value = world * n * args.steps / elapsed
 
+    # ---------------- the plain FP32 engine on the same chains (the metric's denominator) ----------------
+    plain, eng32 = None, None
+    if prec == "mixed" and not args.no_plain:
+        eng32 = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev,
+                           dtype=w.dtype, options=fp32_options)
+        el32, ms32, clk32 = time_sweeps(eng32, tens, cfg0, uni, args, barrier, local_rank)
+        el32 = max_over_ranks(el32)
+        plain = {"value": world * n * args.steps / el32, "unit": UNIT, "precision": "fp32",
+                 "kernel_ms_per_launch": statistics.mean(ms32), "clocks": clk32,
+                 "launch_options": fp32_options or "engine default"}
+
     # ---------------- the unfused split (amp+O_k launch, then E_loc launch) ----------------
-    unfused = unfused_rate(eng, tens, cfg, args, barrier) if not args.no_unfused else None
+    unfused = unfused_rate(eng, tens, cfg0.clone(), args, barrier) if not args.no_unfused else None
 
     # ---------------- end-to-end through the public API, host buffers ----------------
     e2e_value, h2d, d2h = e2e_public_api(w, n, rank, dev, ustream, args, barrier, options)
     if world > 1:
-        t = torch.tensor([n * args.steps / e2e_value], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_value = world * n * args.steps / float(t.item())
+        e2e_value = world * n * args.steps / max_over_ranks(n * args.steps / e2e_value)
 
     if rank != 0:
         return
@@ -348,26 +495,31 @@ def run_ours(args, rank, world, local_rank):
     mean_launch_s = statistics.mean(launch_ms) / 1e3
     achieved = n * flops / mean_launch_s / 1e12 if flops else None
     peak = peaks.get("bf16_tflops")
-    # DRAM bytes per sample of peps_kernel from one ncu --set full capture of this
-    # workload (608 chains, dram__bytes_read.sum + dram__bytes_write.sum =
-    # 13.36 GB); each chain reuses its CTA slot, so traffic scales with the chains
-    # of a launch
-    traffic = NCU_DRAM_BYTES_PER_SAMPLE.get(w.name)
+    traffic = NCU_DRAM_BYTES_PER_SAMPLE.get((w.name, prec))
+    kernel = "vmc::rm::peps_kernel" if prec == "mixed" else "vmc::rk::peps_kernel"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved and peak else None,
                 "traffic": traffic * n if traffic else None, "traffic_unit": "bytes per launch",
-                "peak_kind": f"{peak_kind} bf16 burst (cuBLAS)", "kernel": "vmc::peps_kernel",
+                "peak_kind": f"{peak_kind} bf16 burst (cuBLAS)", "kernel": kernel,
                 "flop_per_sample": flops, "units_per_launch": n}
-    cpu = None
+    cpu, accuracy = None, None
     if pool is not None:
         per = max(1, args.cpu_chains_per_core)
-        rate, ns, wall = cpu_oracle_rate(w.name, per, cores, pool)
+        keep = min(args.accuracy_chains, per)
+        rate, ns, wall, ref = cpu_oracle_rate(w.name, per, cores, pool, keep=keep)
         pool.close()
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{ns} chains x 1 sweep ({wall:.1f} s), FP64 NumPy oracle restatement over {cores} processes"}
-    clk = clocks.summary()
-    # the kernel runs on the FP32 CUDA cores: its fraction of their nominal FMA peak, at the SM clock
-    # sampled during the run (SMs x 128 FP32 lanes x 2 flops x clock)
+               "sample": f"{ns} chains x 1 sweep ({wall:.1f} s), FP64 NumPy oracle restatement over {cores} "
+                         "processes"}
+        if ref is not None and w.dtype == "float32":
+            accuracy = {"reference": f"FP64 oracle, the first {keep} chains of its sample (same FP32 tensors, "
+                                     "configurations and uniforms), one sweep",
+                        prec: accuracy_vs_oracle(eng, w, ref, dev)}
+            if eng32 is not None:
+                accuracy["fp32"] = accuracy_vs_oracle(eng32, w, ref, dev)
+            accuracy["bars"] = {"e_mean_vs_scale": 1e-5, "o_frob_rel": 1e-4}
+    # the kernel runs on the CUDA cores (the mixed tier's chain also on the FP64 units): the fraction of
+    # the nominal FP32 FMA peak, at the SM clock sampled during the run (SMs x 128 lanes x 2 x clock)
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
     fp32_peak = n_sm * 128 * 2 * mhz * 1e6 / 1e12 if mhz else None
@@ -382,6 +534,7 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
                    "phys_dim": w.phys_dim, "strategy": f"{w.strategy}({w.chi})", "model": w.model,
                    "chains_per_gpu": n, "global_chains": n * world, "parallelism": f"replicas x{world}",
+                   "precision": prec + (" (FP64 boundary-MPS chain, FP32 contractions)" if prec == "mixed" else ""),
                    "launch_options": options or "engine default",
                    "l2": "inputs larger than L2 (bottom-env cache "
                          f"{eng.cache_bytes(n) / 1e9:.2f} GB read+written per step)"},
@@ -393,9 +546,14 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
         "kernel_ms_per_launch": statistics.mean(launch_ms),
     }
+    if plain is not None:
+        plain["mixed_over_plain"] = value / plain["value"]
+        line["plain_fp32"] = plain
+    if accuracy is not None:
+        line["accuracy"] = accuracy
     if unfused is not None:
-        line["unfused"] = {"value": unfused, "unit": UNIT, "launches_per_step": 2,
-                           "what": "FP32 amp+O_k launch then E_loc launch on sampled configurations (no "
+        line["unfused"] = {"value": unfused, "unit": UNIT, "launches_per_step": 2, "precision": prec,
+                           "what": "amp+O_k launch then E_loc launch on sampled configurations (no "
                                    "sampling), device-resident; the fused sweep also samples",
                            "fused_over_unfused": value / unfused}
     print(json.dumps(line), flush=True)
@@ -558,14 +716,22 @@ def run_gi(args, rank, world, local_rank):
     electric basis the GI model samples: g/2 (2 - 2 (-1)^E) per link (the same up to a constant) and
     -1/(2g) (P + P^dag) per plaquette.  value: plaquette sweep + O_k + E_loc samples/s, inputs on the
     device; e2e: the public kernels (build_mc_kernels) with host uniforms in and E/log|psi|/sign out."""
+    import multiprocessing as mp
+
+    # the CPU baseline pool must exist before CUDA is initialised
+    pool = None
+    cores = len(os.sched_getaffinity(0))
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        pool = mp.get_context("spawn").Pool(cores, initializer=_worker_init)
+
     import torch
 
     from vmc_gb300 import ZipUp
     from vmc_gb300.gi import GIPEPS, GIPEPSConfig, build_gi_mc_kernels, z2_pure_gauge_hamiltonian
 
     n = args.chains or 4096
-    g = 0.8
-    shape, dmax, chi = (9, 9), 2, 32
+    g = GI_G
+    shape, dmax, chi = GI_SHAPE, GI_DMAX, GI_CHI
     dev = torch.device(f"cuda:{local_rank}")
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream(dev)
@@ -619,8 +785,14 @@ def run_gi(args, rank, world, local_rank):
     b.record(stream)
     torch.cuda.synchronize()
     t_e2e = a.elapsed_time(b) / 1e3 / args.steps
+    cpu = None
+    if pool is not None:
+        rate, ns, wall = gi_oracle_rate(max(1, args.gi_ref_chains_per_core), cores, pool)
+        pool.close()
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{ns} chains x 1 sweep ({wall:.1f} s), FP64 NumPy GI oracle over {cores} processes"}
     line = {
-        "metric": "GI-PEPS samples/s (plaquette sweep + grad log psi + E_loc), pure Z2 gauge 9x9, D=2/sector, chi=32",
+        "metric": GI_METRIC,
         "value": n / t, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
@@ -630,7 +802,7 @@ def run_gi(args, rank, world, local_rank):
                    "l2": f"inputs larger than L2 (bottom-env cache {eng.cache_bytes(n) / 1e9:.2f} GB)"},
         "roofline": {"bound": "tensor", "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None,
                      "traffic": None, "note": "no algorithmic FLOP count exists for the GI path"},
-        "cpu_baseline": None,
+        "cpu_baseline": cpu,
         "e2e": {"value": n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n * n_plaq * 8, "d2h_bytes_per_step": 3 * n * 8},
         "gpu_launches": 2 * args.steps,
         "clocks": clocks.summary(),
@@ -651,6 +823,13 @@ def main():
     ap.add_argument("--ref-chains-per-core", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-unfused", action="store_true", help="skip the unfused amp+O_k / E_loc comparison leg")
+    ap.add_argument("--gi-ref-chains-per-core", type=int, default=1,
+                    help="GI workload: oracle chains per host core per step (reference arm and cpu_baseline)")
+    ap.add_argument("--precision", choices=["auto", "mixed", "fp32"], default="auto",
+                    help="engine tier of the headline: auto = mixed (FP64 boundary-MPS chain) where it exists")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 leg beside a mixed headline")
+    ap.add_argument("--accuracy-chains", type=int, default=64,
+                    help="chains of the CPU-baseline sample whose FP64 results check both tiers")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

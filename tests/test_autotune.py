@@ -84,8 +84,7 @@ def test_shipped_table_entries_are_valid_candidates(emu_lib):
         assert entry["options"] in CANDIDATES, key
         assert entry["samples_per_s"] == max(c["samples_per_s"] for c in entry["candidates"]), key
         for cand in entry["candidates"]:
-            o = _abi.VmcPlanOptions(cand["options"]["threads"], cand["options"]["smem_kb"],
-                                    cand["options"]["tile_policy"])
+            o = _abi.plan_options(cand["options"])
             plan = ct.c_void_p()
             assert emu_lib.vmc_peps_plan_ex(ct.byref(shape), 2, 4, 2, 0, 1, 2, ct.byref(o), ct.byref(plan)) == \
                 _abi.VMC_OK, (key, cand)
@@ -98,6 +97,22 @@ def test_shipped_options_lookup(monkeypatch):
     assert autotune.shipped_options((8, 8), 4, 16, device="cpu") is None  # no table for the host build
     monkeypatch.setattr(autotune, "_device_name", lambda device: "NVIDIA GB300")
     table = json.loads(autotune.SHIPPED.read_text())
-    want = table["NVIDIA GB300|16x16|D6|chi48|d2|ZipUp|sweeps2|float32"]["options"]
+    key = autotune._key(torch.device("cpu"), (16, 16), 6, 48, 2, "ZipUp", 2, "float32")
+    assert key.startswith("NVIDIA GB300|16x16|D6|chi48|d2|ZipUp|sweeps2|float32|H") and key.endswith("|fp32")
+    want = table[key]["options"]
     assert autotune.shipped_options((16, 16), 6, 48, device="cpu") == want
     assert autotune.shipped_options((5, 7), 3, 9, device="cpu") is None
+
+
+def test_the_cache_key_tells_hamiltonians_apart():
+    """E_loc forms only the amplitudes a term's nonzero elements need, so a Heisenberg winner is not
+    reused for a TFIM plan of the same lattice (and neither for another precision)."""
+    from vmc_gb300 import autotune
+    from vmc_gb300.operators import heisenberg, transverse_field_ising
+
+    dev = torch.device("cpu")
+    kh = autotune._key(dev, (4, 4), 3, 6, 2, "ZipUp", 2, "float32", heisenberg((4, 4)))
+    kt = autotune._key(dev, (4, 4), 3, 6, 2, "ZipUp", 2, "float32", transverse_field_ising((4, 4)))
+    assert kh != kt
+    assert kh == autotune._key(dev, (4, 4), 3, 6, 2, "ZipUp", 2, "float32", None)  # default: Heisenberg
+    assert kh != autotune._key(dev, (4, 4), 3, 6, 2, "ZipUp", 2, "float32", None, precision="mixed")

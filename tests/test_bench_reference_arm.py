@@ -36,3 +36,11 @@ def test_reference_arm_line():
 def test_reference_arm_unavailable_workload():
     d = _run("--workload", "uneven")
     assert d["impl"] == "reference" and "unavailable" in d
+
+
+def test_reference_arm_gi_workload_times_the_gi_oracle():
+    """gi9x9: the FP64 GI oracle over the host cores, one chain per core (about half a minute)."""
+    d = _run("--workload", "gi9x9", "--steps", "1", "--warmup", "0")
+    assert d["impl"] == "reference" and "unavailable" not in d and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"] == d["e2e"]["value"]
+    assert d["config"]["workload"] == "gi9x9"

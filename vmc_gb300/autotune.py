@@ -1,5 +1,6 @@
-"""Launch-configuration autotuner: per (lattice, D, chi, d, dtype, strategy), the CTA size, shared-memory
-budget and GEMM register-tile policy of the fused kernel that give the most samples/s on this GPU.
+"""Launch-configuration autotuner: per (lattice, D, chi, d, dtype, strategy, Hamiltonian structure), the CTA
+size, shared-memory budget and GEMM register-tile policy of the fused FP32 kernel that give the most samples/s
+on this GPU.
 
 ``tune`` builds one plan per candidate (``vmc_peps_plan_ex``), times full sweeps on seeded synthetic
 inputs -- whole waves of chains, after a warm-up sweep -- and records every candidate's rate with the
@@ -12,6 +13,7 @@ package and is guarded by a lock.
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 import threading
@@ -53,9 +55,28 @@ def _device_name(device) -> str:
     return "host-emulation"
 
 
-def _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype) -> str:
+def operator_tag(operator, shape, phys_dim=2, complex_elements=False) -> str:
+    """Fingerprint of a Hamiltonian's nonzero structure on this lattice: which sites and bonds carry
+    terms and which operator elements are nonzero.  The estimate forms only the amplitudes a term's
+    nonzero elements need, so its cost -- and the launch configuration that wins -- depends on it."""
+    from .lowering import lower_operator
+    from .operators import heisenberg
+
+    op = operator if operator is not None else heisenberg(shape)
+    lo = lower_operator(op, shape, phys_dim, complex_elements=complex_elements)
+    h = hashlib.sha1()
+    for a in (lo.onesite, lo.horiz, lo.vert):
+        h.update(np.ascontiguousarray(np.asarray(a) != 0).tobytes())
+    for a in (lo.onesite_mask, lo.horiz_mask, lo.vert_mask):
+        h.update(np.ascontiguousarray(np.asarray(a, dtype=np.int32)).tobytes())
+    h.update(str(int(lo.n_diag)).encode())
+    return h.hexdigest()[:10]
+
+
+def _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator=None, precision="fp32") -> str:
+    tag = operator_tag(operator, shape, phys_dim, dtype == "complex64")
     return (f"{_device_name(device)}|{shape[0]}x{shape[1]}|D{bond_dim}|chi{chi}|d{phys_dim}|{strategy}"
-            f"|sweeps{n_sweeps}|{dtype}")
+            f"|sweeps{n_sweeps}|{dtype}|H{tag}|{precision}")
 
 
 SHIPPED = Path(__file__).resolve().parent / "tuned_gb300.json"
@@ -143,16 +164,16 @@ def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="
     entry = {"options": best["options"], "samples_per_s": best["samples_per_s"], "candidates": results}
     if store:
         with _LOCK:
-            _store(_key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype), entry)
+            _store(_key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op), entry)
     return entry
 
 
 def shipped_options(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32",
-                    device=None):
+                    device=None, operator=None):
     """The winner the shipped table holds for this problem on this GPU, or None (no tuning, no local cache)."""
     device = torch.device(device if device is not None else "cuda")
     hit = _load(SHIPPED).get(_key(device, (int(shape[0]), int(shape[1])), bond_dim, chi, phys_dim, strategy, n_sweeps,
-                                  dtype))
+                                  dtype, operator))
     return dict(hit["options"]) if hit else None
 
 
@@ -161,7 +182,7 @@ def tuned_options(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2
     """The cached winner for this problem on this GPU, tuning it first when it is not cached."""
     shape = (int(shape[0]), int(shape[1]))
     device = torch.device(device if device is not None else ("cuda" if lib is None else "cpu"))
-    key = _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype)
+    key = _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator)
     with _LOCK:
         hit = _load().get(key)
         if hit is None:
@@ -197,7 +218,7 @@ def main(argv=None) -> None:
         entry = tune(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype, w.operator(), dev, store=False,
                      n_chains=n or None)
         entry["chains"] = n or "one wave"
-        table[_key(dev, w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype)] = entry
+        table[_key(dev, w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype, w.operator())] = entry
         print(json.dumps({"workload": name, **entry}), flush=True)
         Path(args.out).write_text(json.dumps(table, indent=1, sort_keys=True))
 

@@ -85,6 +85,10 @@ class PEPSEngine:
         if isinstance(options, str):
             if options != "auto":
                 raise ValueError("options must be None, a dict or 'auto'")
+        if options == "auto" and precision in ("mixed", _abi.VMC_PRECISION_MIXED):
+            # the tuned table holds FP32 launch configurations; the mixed tier runs its defaults
+            options = {}
+        if isinstance(options, str):
             from .autotune import tuned_options
 
             options = tuned_options(self.shape, self.bond_dim, self.chi, self.phys_dim, strategy, n_sweeps,
