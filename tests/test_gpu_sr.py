@@ -1,0 +1,126 @@
+"""The FP64 SR / TDVP layer on the GPU against the FP64 oracle (oracle/sr.py) on the same inputs.
+
+The inputs are the engine's own sweep outputs -- O_k, active slice indices and E_loc of sampled
+chains -- so the solves see the rank structure and scales of a real run:
+
+- 8x8 Heisenberg, D=4, chi=16, 4096 samples: the sliced Jacobian (4096 x 10,816, two slices), SampleSpace
+  DirectSolve with diagonal shift 1e-4, Gram built in 16 column blocks (the reference's sliced
+  DirectSolve, preconditioners.py:117-152 and qgt.py:173-223);
+- 6x6 Heisenberg, D=4, chi=16, 512 samples: the same in ParameterSpace (a 10,368^2 FP64 S);
+- one Euler and one RK4 step of TDVPDriver (integrators.py:45-109): every stage's SR solve is
+  re-solved by the oracle from the stage's recorded inputs, and the step's update is the
+  integrator's combination of those stages.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import sr as osr
+from tests.helpers import hamiltonian, make_case
+from vmc_gb300 import PEPS, ZipUp
+from vmc_gb300.drivers import RK4, Euler, ImaginaryTimeUnit, TDVPDriver
+from vmc_gb300.engine import PEPSEngine
+from vmc_gb300.lowering import pack_tensors, params_per_site
+from vmc_gb300.preconditioners import SRPreconditioner
+from vmc_gb300.qgt import ParameterSpace, SampleSpace
+
+pytestmark = pytest.mark.gpu
+
+N_SAMPLES, N_CHAINS = 1024, 512
+
+
+def _sweep_outputs(device, shape, D, chi, n):
+    H = hamiltonian("heisenberg", shape)
+    T, cfg, u = make_case(shape, D, n, seed=3)
+    eng = PEPSEngine(shape, D, chi, 2, "ZipUp", operator=H, device=device, precision="mixed")
+    tens = torch.from_numpy(pack_tensors(T)).to(device)
+    c = torch.from_numpy(cfg).to(device)
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, torch.from_numpy(u).to(device), cache)
+    torch.cuda.synchronize()
+    eng.raise_on_status()
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(chi), device=device,
+                 tensors=T)
+    return model, res
+
+
+def _oracle_update(o, p, e, shape, D, space, shift, grad_factor=1.0):
+    n = o.shape[0]
+    x, _ = osr.sr_apply(o.cpu().numpy().astype(np.float64), None if p is None else p.cpu().numpy(),
+                        e.cpu().numpy().astype(np.float64), pps=params_per_site(shape, D),
+                        sliced_dims=(2,) * (shape[0] * shape[1]), n_samples=n, space=space,
+                        strategy=osr.DirectSolve(), diag_shift=shift, ordering=osr.SliceOrdering(),
+                        grad_factor=grad_factor, real_params=True)
+    return x
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_config2_sliced_direct_solve_sample_space(cuda_device):
+    shape, D, chi, n = (8, 8), 4, 16, 4096
+    model, res = _sweep_outputs(cuda_device, shape, D, chi, n)
+    assert res.O.shape == (n, 10816)
+    pre = SRPreconditioner(space=SampleSpace(), diag_shift=1e-4)
+    upd, metrics = pre.apply(model, model.tensors, res.configs, res.O, res.p, res.E)
+    x = model.packed(upd).double().cpu().numpy()
+    x_ref = _oracle_update(res.O, res.p, res.E, shape, D, osr.SampleSpace(), 1e-4)
+    assert x.shape == x_ref.shape == (2 * 10816,)
+    # FP64 solves on both sides; the update is returned in the parameters' FP32
+    assert _rel(x, x_ref) < 1e-6, _rel(x, x_ref)
+    assert np.isfinite(float(metrics["residual_error"]))
+
+
+def test_parameter_space_sliced_direct_solve(cuda_device):
+    shape, D, chi, n = (6, 6), 4, 16, 512
+    model, res = _sweep_outputs(cuda_device, shape, D, chi, n)
+    pre = SRPreconditioner(space=ParameterSpace(), diag_shift=1e-4)
+    upd, _ = pre.apply(model, model.tensors, res.configs, res.O, res.p, res.E)
+    x = model.packed(upd).double().cpu().numpy()
+    x_ref = _oracle_update(res.O, res.p, res.E, shape, D, osr.ParameterSpace(), 1e-4)
+    assert _rel(x, x_ref) < 1e-6, _rel(x, x_ref)
+
+
+class _Recording(SRPreconditioner):
+    """SRPreconditioner that keeps every stage's inputs and flat update."""
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.stages = []
+
+    def apply(self, model, params, samples, o, p, local_energies, *, grad_factor=1.0):
+        upd, metrics = super().apply(model, params, samples, o, p, local_energies, grad_factor=grad_factor)
+        self.stages.append((o.clone(), None if p is None else p.clone(), local_energies.clone(), grad_factor,
+                            model.packed(upd).double().cpu().numpy()))
+        return upd, metrics
+
+
+@pytest.mark.parametrize("integrator,space", [(Euler(), SampleSpace()), (RK4(), SampleSpace()),
+                                              (RK4(), ParameterSpace())], ids=["euler", "rk4", "rk4-param"])
+def test_tdvp_step_matches_oracle_stages(cuda_device, integrator, space):
+    shape, D, chi = (4, 4), 3, 6
+    H = hamiltonian("heisenberg", shape)
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(chi), device=cuda_device, rngs=5)
+    theta0 = model.packed().double().cpu().numpy()
+    pre = _Recording(space=space, diag_shift=1e-3)
+    dt = 0.02
+    drv = TDVPDriver(model, H, preconditioner=pre, dt=dt, time_unit=ImaginaryTimeUnit(), integrator=integrator,
+                     n_samples=N_SAMPLES, n_chains=N_CHAINS, sampler_key=9)
+    drv.run(dt)
+    ks = []
+    for o, p, e, gf, x in pre.stages:
+        x_ref = _oracle_update(o, p, e, shape, D, osr.SampleSpace() if isinstance(space, SampleSpace)
+                               else osr.ParameterSpace(), 1e-3, grad_factor=gf)
+        assert _rel(x, x_ref) < 1e-6, _rel(x, x_ref)
+        ks.append(x_ref)
+    if isinstance(integrator, Euler):
+        assert len(ks) == 1
+        want = theta0 + dt * ks[0]
+    else:
+        assert len(ks) == 4
+        want = theta0 + dt * (ks[0] + 2 * ks[1] + 2 * ks[2] + ks[3]) / 6.0
+    got = drv.model.packed().double().cpu().numpy()
+    assert _rel(got - theta0, want - theta0) < 1e-5, _rel(got - theta0, want - theta0)
