@@ -276,6 +276,25 @@ vmc_status vmc_peps_amp_grad(const vmc_plan* plan, void* stream, const float* te
                              size_t workspace_bytes, int32_t* status_dev);
 
 /*
+ * Vector-Jacobian product of the amplitudes: the adjoint of peps_apply
+ * (compat.py:49-61, whose backward scatters g * env_grad into the gradient,
+ * energy.py:276-301).  out_grad[k] = sum_i w_i O_i[k] over the FULL
+ * parameter layout (n_params_full elements; O_i = (dpsi_i / dtheta) / psi_i,
+ * the rows vmc_peps_amp_grad writes).  The kernel builds each sample's
+ * gradient environments as amp_grad does and adds w_i O_i into out_grad in
+ * FP64 (atomics), so no n x n_params matrix exists: memory is the workspace
+ * plus the one gradient.  For the backward of amp_i = sign_i exp(logamp_i)
+ * with output cotangents g_i, pass w_i = g_i amp_i (real plans) or
+ * w_i = conj(g_i) amp_i and conjugate the result (complex plans, where w and
+ * out_grad hold (re, im) pairs).  out_grad is zeroed by the call (stream
+ * ordered); workspace: vmc_workspace_size(plan, n).  Standard (not
+ * gauge-invariant) plans.
+ */
+vmc_status vmc_peps_vjp(const vmc_plan* plan, void* stream, const float* tensors, const int32_t* samples, int n,
+                        const double* weights, double* out_grad, void* workspace, size_t workspace_bytes,
+                        int32_t* status_dev);
+
+/*
  * vmc_peps_amp_grad without a caller workspace.  No counterpart in the
  * reference: it exists for callers that cannot hand the engine scratch memory,
  * e.g. a framework that has reserved the device memory in a pool of its own

@@ -100,6 +100,7 @@ SIGNATURES = {
     "vmc_peps_sweep_recompute": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "vmc_peps_amp_grad": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P]),
     "vmc_peps_amp_grad_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P]),
+    "vmc_peps_vjp": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _SZ, _P]),
     "vmc_peps_local_energy": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _P]),
     "vmc_batch_workspace_size": (_SZ, [ct.POINTER(VmcPepsJob), _I]),
     "vmc_peps_batch": (_I, [ct.POINTER(VmcPepsJob), _I, _P, _P, _SZ, _P]),

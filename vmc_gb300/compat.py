@@ -1,8 +1,10 @@
 """Evaluation surfaces of src/vmc/peps/standard/compat.py on the engine.
 
-* ``peps_apply``: amplitude with a hand-written adjoint (compat.py:31-64),
-  as a ``torch.autograd.Function``: the backward pass reuses the engine's
-  environment sweep (``vmc_peps_amp_grad``) instead of autodiff.
+* ``peps_apply``: amplitude with a hand-written adjoint (compat.py:31-64), the
+  ``vmc_gb300::peps_amplitude`` operator: its backward is the engine's
+  vector-Jacobian product (``vmc_peps_vjp``), which rebuilds the environments
+  and accumulates sum_i g_i dpsi_i/dtheta in the kernel -- nothing per sample
+  is stored between forward and backward.
 * ``_value`` / ``_grad`` / ``_value_and_grad`` (compat.py:67-133).
 * ``local_estimate`` (compat.py:136-194).
 
@@ -13,6 +15,7 @@ from __future__ import annotations
 
 import torch
 
+from . import ops
 from .lowering import params_per_site
 
 __all__ = ["peps_apply", "log_value", "_value", "_grad", "_value_and_grad", "local_estimate",
@@ -40,31 +43,6 @@ def _samples(model, samples):
     return s.to(torch.int32).contiguous()
 
 
-class _PepsAmplitude(torch.autograd.Function):
-    """amp(theta) with d amp / d theta from the stored-environment adjoint (energy.py:276-301)."""
-
-    @staticmethod
-    def forward(ctx, packed, samples, engine):
-        logamp, sign, O = engine.amp_grad(packed.detach().contiguous(), samples, full_gradient=True,
-                                          want_O=packed.requires_grad)
-        amp = engine.amplitude(logamp, sign)
-        if O is not None:
-            ctx.save_for_backward(O, amp)
-        ctx.param_dtype = packed.dtype
-        return amp
-
-    @staticmethod
-    def backward(ctx, g):
-        O, amp = ctx.saved_tensors
-        # d amp_i / d theta = amp_i * O_i  (O = dpsi/dtheta / psi, full layout); psi is holomorphic in
-        # theta, so in torch's convention grad_theta = sum_i g_i * conj(amp_i O_i)
-        if amp.is_complex():
-            grad = (g[:, None] * torch.conj(amp[:, None] * O.to(torch.complex128))).sum(0)
-        else:
-            grad = ((g * amp)[:, None] * O.to(torch.float64)).sum(0)
-        return grad.to(ctx.param_dtype), None, None
-
-
 def peps_apply(tensors, sample, shape, strategy, model=None):
     """compat.py:31-40: amplitude(s) of `sample` (n, n_sites) or (n_sites,)."""
     from .peps import PEPS
@@ -76,7 +54,7 @@ def peps_apply(tensors, sample, shape, strategy, model=None):
             raise TypeError("peps_apply needs the PEPS model (it carries the engine plan)")
     packed = model.packed(tensors if not isinstance(tensors, PEPS) else None)
     s = _samples(model, sample)
-    amp = _PepsAmplitude.apply(packed, s, model.engine())
+    amp = ops.peps_amplitude(ops.register_engine(model.engine()), packed, s)
     return amp if torch.as_tensor(sample).ndim > 1 else amp[0]
 
 

@@ -772,7 +772,8 @@ __device__ __noinline__ void estimate_row(const DevPlan& P, const Slot& S, Share
                                           const float* tensors, const float* top, const int* tbond, const float* bot,
                                           const int* bbond, int row, const int* spins, const double* osc,
                                           float* Orow, int full_gradient, bool want_grad, bool want_energy,
-                                          double* energy) {
+                                          double* energy, const double* vjp_w = nullptr,
+                                          double* vjp_grad = nullptr) {
   const int C = P.C;
   const bool has_h = want_energy && P.row_has_h[row];
   VMC_TSTART(tr);
@@ -807,6 +808,21 @@ __device__ __noinline__ void estimate_row(const DevPlan& P, const Slot& S, Share
         G = elem(Orow, full_gradient ? (size_t)P.d * P.site_osl[s] + (size_t)cur * sz : (size_t)P.site_osl[s]);
       }
       grad_env(Y1, B, Rc, W, G, ba, V, bb, tb, Rb, Lb, U, (float)cs_re, (float)cs_im);
+      if (vjp_grad) {
+        // vector-Jacobian product: grad[full layout of site s, slice cur] += w * O (FP64), with G this
+        // site's O for the chain; the weight stays out of the FP32 G, where a tiny amplitude would underflow
+        double* dst = vjp_grad + (size_t)kEs * ((size_t)P.d * P.site_osl[s] + (size_t)cur * sz);
+        for (int i = threadIdx.x; i < sz; i += blockDim.x) {
+          if (kCplx) {
+            const double gr = G[2 * i], gi = G[2 * i + 1];
+            atomicAdd(dst + 2 * i, vjp_w[0] * gr - vjp_w[1] * gi);
+            atomicAdd(dst + 2 * i + 1, vjp_w[0] * gi + vjp_w[1] * gr);
+          } else {
+            atomicAdd(dst + i, vjp_w[0] * (double)G[i]);
+          }
+        }
+        __syncthreads();  // G (scratch) is rewritten at the next column
+      }
       if (os) {
         // amps_site[p] = sum A[p] . G  (already divided by psi); E += sum_p op[p, s] amps[p]
         for (int p = 0; p < P.d; ++p) {
@@ -1175,7 +1191,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   if (mode == MODE_ENERGY) {
     logamp = logamp_io[chain];
     sgn = sign_io[chain];
-  } else if (threadIdx.x == 0) {
+  } else if (threadIdx.x == 0 && logamp_io) {
     logamp_io[chain] = logamp;
     sign_io[chain] = sgn;
     if (out_margin && mode == MODE_SWEEP) out_margin[chain] = min_margin;
@@ -1183,9 +1199,11 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   if (!isfinite(logamp) && threadIdx.x == 0) atomicOr(status, VMC_DEV_NONFINITE);
 
   // ---------------- bottom-up estimate ----------------
-  const bool want_grad = (mode == MODE_SWEEP || mode == MODE_AMPGRAD);
+  const bool want_grad = (mode == MODE_SWEEP || mode == MODE_AMPGRAD || mode == MODE_VJP);
   const bool want_energy = (mode == MODE_SWEEP || mode == MODE_ENERGY);
   float* Orow = out_O ? elem(out_O, (size_t)chain * n_params) : nullptr;
+  const double* vjp_w = (mode == MODE_VJP) ? J.vjp_w + (size_t)kEs * chain : nullptr;
+  double* vjp_grad = (mode == MODE_VJP) ? J.vjp_grad : nullptr;
   if (Orow && full_gradient) {
     for (int i = threadIdx.x; i < n_params * kEs; i += blockDim.x) Orow[i] = 0.f;
     __syncthreads();
@@ -1226,7 +1244,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
     const double om = exp(S.lt[r] + lb_cur - logamp);
     const double osc[2] = {inv_re * om, inv_im * om};
     estimate_row(P, S, sh, perm, tensors, top, tbonds(P, r), bcur, bbonds(P, r), r, sh.spins[0], osc, Orow,
-                 full_gradient, want_grad, want_energy, energy);
+                 full_gradient, want_grad, want_energy, energy, vjp_w, vjp_grad);
     if (want_energy && r < R - 1 && P.row_has_v[r]) {
       const double vm = exp(S.lt[r] + lb_prev - logamp);
       const double vsc[2] = {inv_re * vm, inv_im * vm};

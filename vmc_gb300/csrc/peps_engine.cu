@@ -626,6 +626,23 @@ vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors
                 workspace_bytes, status_dev);
 }
 
+vmc_status vmc_peps_vjp(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples, int n,
+                        const double* weights, double* out_grad, void* workspace, size_t workspace_bytes,
+                        int32_t* status_dev) {
+  if (!pl || !tensors || !samples || n < 0 || !weights || !out_grad || !workspace || !status_dev)
+    return VMC_ERR_INVALID;
+  if (pl->hp.gi) return VMC_ERR_UNSUPPORTED;
+  const size_t grad_bytes = (size_t)pl->hp.np_sliced * pl->hp.d * pl->hp.es * sizeof(double);
+  if (vmc_memset(out_grad, 0, grad_bytes, static_cast<cudaStream_t>(stream)) != cudaSuccess) return VMC_ERR_CUDA;
+  if (n == 0) return VMC_OK;
+  if (workspace_bytes < vmc_workspace_size(pl, n)) return VMC_ERR_WORKSPACE;
+  ChainJob J = chain_job(pl, MODE_VJP, tensors, nullptr, const_cast<int32_t*>(samples), nullptr, nullptr, n,
+                         nullptr, 1, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+  J.vjp_w = weights;
+  J.vjp_grad = out_grad;
+  return run_job(pl, stream, J, static_cast<float*>(workspace), n_slots(pl, n), status_dev);
+}
+
 // Floats of the per-CTA cache entries of a recomputing sweep on grid CTAs.
 static size_t recompute_cache_floats(const DevPlan& P, int grid) {
   return (size_t)grid * P.cache_floats_per_chain + 2 * (size_t)grid * P.R;

@@ -41,7 +41,7 @@ constexpr long long kMaxArenaSmemBytes = 52 * 1024;
 constexpr long long kMaxArenaSmemBytesF64 = 200 * 1024;
 constexpr long long kDefaultArenaSmemBytesF64 = 52 * 1024;
 enum PermKind { P_ZIPT = 0, P_ZIPB = 1, P_RENV = 2, P_LENV = 3, P_R2 = 4, P_VRB = 5 };
-enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3 };
+enum Mode { MODE_INIT = 0, MODE_SWEEP = 1, MODE_AMPGRAD = 2, MODE_ENERGY = 3, MODE_VJP = 4 };
 
 
 // Device-side plan: scalars plus device pointers into one allocation.
@@ -201,6 +201,9 @@ struct ChainJob {
   double* sign_io;
   float* out_margin;
   float* out_gap;
+  // MODE_VJP: per-chain weights (kEs doubles each) and the FP64 gradient they accumulate into
+  const double* vjp_w;
+  double* vjp_grad;
 };
 
 // The job table of one launch of the fused kernel (a kernel parameter).  Work

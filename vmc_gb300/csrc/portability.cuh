@@ -51,6 +51,11 @@ inline int atomicAdd(int* p, int v) {
   *p += v;
   return o;
 }
+inline double atomicAdd(double* p, double v) {
+  double o = *p;
+  *p += v;
+  return o;
+}
 typedef void* cudaStream_t;
 typedef int cudaError_t;
 #define cudaSuccess 0

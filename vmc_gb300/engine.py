@@ -288,6 +288,22 @@ class PEPSEngine:
             return logamp, sign, O, gap
         return logamp, sign, O
 
+    def vjp(self, tensors, samples, weights):
+        """sum_i w_i O_i over the full parameter layout (``vmc_peps_vjp``), FP64 (complex128 for a complex
+        engine): the adjoint of the amplitudes without an (n, n_params) O matrix."""
+        self._check_tensors(tensors)
+        c = self._configs(samples)
+        n = c.shape[0]
+        w = weights.to(torch.complex128 if self.complex else torch.float64).contiguous()
+        if self.complex:
+            w = torch.view_as_real(w).contiguous()
+        grad = torch.empty(self.n_params_full * (2 if self.complex else 1), dtype=torch.float64, device=self.device)
+        ws = self.workspace(n)
+        st = self.lib.vmc_peps_vjp(self._plan, self._stream(), _vp(tensors), _vp(c), n, _vp(w), _vp(grad), _vp(ws),
+                                   ws.numel(), _vp(self._status))
+        _abi.check(self.lib, st, "vmc_peps_vjp")
+        return torch.view_as_complex(grad.view(-1, 2)) if self.complex else grad
+
     def local_energy(self, tensors, samples, logamp, sign):
         self._check_tensors(tensors)
         c = self._configs(samples)

@@ -54,9 +54,19 @@ def _uniforms(key, n, n_sites, device):
     raise TypeError("key must be a torch.Generator or a float64 tensor of per-site uniforms")
 
 
-def build_mc_kernels(model, operator, *, full_gradient: bool = False):
+# Bottom-environment caches larger than this are not kept between sweeps: each sweep recomputes its
+# chains' bottom rows in the launch instead (one cache entry per resident CTA), the same results for one
+# extra bottom-up pass.  4096 chains of a 16x16 D=6 chi=48 PEPS would hold 58 GB.
+DEFAULT_CACHE_BUDGET_BYTES = 16 << 30
+
+
+def build_mc_kernels(model, operator, *, full_gradient: bool = False, cache_budget_bytes: int | None = None):
     """kernels.py:91-247 for the standard PEPS on the GB300 engine; a GIPEPS model gets the
-    gauge-invariant kernels (src/vmc/peps/gi/kernels.py:17-126, dispatched on the model type there)."""
+    gauge-invariant kernels (src/vmc/peps/gi/kernels.py:17-126, dispatched on the model type there).
+
+    ``cache_budget_bytes`` (default ``DEFAULT_CACHE_BUDGET_BYTES``): when the chains' bottom-environment
+    cache would exceed it, ``init_cache`` keeps none (``Cache.bottom_envs`` is None) and every sweep
+    recomputes the bottom rows inside its launch."""
     from .gi import GIPEPS, build_gi_mc_kernels
 
     if isinstance(model, GIPEPS):
@@ -65,8 +75,12 @@ def build_mc_kernels(model, operator, *, full_gradient: bool = False):
     n_sites = model.shape[0] * model.shape[1]
     d = model.phys_dim
 
+    budget = DEFAULT_CACHE_BUDGET_BYTES if cache_budget_bytes is None else int(cache_budget_bytes)
+
     def init_cache(tensors, config_states) -> Cache:
         cfg = config_states.reshape(-1, n_sites).to(device=engine.device, dtype=torch.int32).contiguous()
+        if engine.cache_bytes(cfg.shape[0]) > budget:
+            return Cache(bottom_envs=None)  # over budget: the sweeps recompute the bottom rows
         return Cache(bottom_envs=engine.init_cache(model.packed(tensors), cfg))
 
     def transition(tensors, config_state, key, cache: Cache, deltas=None):
