@@ -124,20 +124,54 @@ def test_alternative_engine_paths_match_oracle(emu_lib, opts):
     assert_parity(np.linalg.norm(res.O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), True)
 
 
-def test_density_matrix_is_not_the_zipup_product_and_is_rejected(emu_lib):
-    """strategy.py:153-176 carries V_k^H without S_k, so its truncations differ from ZipUp's;
-    the engine reports it as unsupported instead of substituting ZipUp."""
-    import ctypes as ct
-
+def test_density_matrix_is_not_the_zipup_product(emu_lib):
+    """strategy.py:153-176 carries V_k^H without S_k, so its truncations differ from ZipUp's."""
     shape, D, chi = (4, 4), 3, 6
     T, cfg, _ = make_case(shape, D, 8, seed=31)
     zu = oracle.peps_apply(fp32(T), cfg, shape, oracle.ZipUp(chi))
     dm = oracle.peps_apply(fp32(T), cfg, shape, oracle.DensityMatrix(chi))
     assert np.max(np.abs(dm / zu - 1)) > 1e-3
-    plan = ct.c_void_p()
-    st = emu_lib.vmc_peps_plan(ct.byref(_abi.VmcShape(*shape)), D, chi, 2, 0, _abi.VMC_STRATEGY_DENSITY_MATRIX, 2,
-                               ct.byref(plan))
-    assert st == _abi.VMC_ERR_UNSUPPORTED
+
+
+DM_CASES = [((3, 3), 2, 2, "heisenberg", "fp32"), ((4, 4), 3, 3, "heisenberg", "fp32"), ((4, 4), 2, 2, "tfim", "fp32"),
+            ((3, 4), 2, 2, "heisenberg", "fp32"), ((4, 4), 3, 3, "heisenberg", "mixed"), ((3, 4), 2, 2, "tfim", "mixed")]
+
+
+@pytest.mark.parametrize("shape,D,chi,model,precision", DM_CASES)
+def test_density_matrix_matches_oracle(emu_lib, shape, D, chi, model, precision):
+    """DensityMatrix with chi <= D, where every kept eigenvector of rho = theta^H theta has a nonzero
+    eigenvalue.  With more (chi > rank theta at a cut) the kept vectors include arbitrary null vectors of
+    theta, and the reference's result depends on which ones its eigh returns."""
+    H = hamiltonian(model, shape)
+    T, cfg, u = make_case(shape, D, 6, seed=D + chi)
+    eng = _engine(emu_lib, shape, D, chi, "DensityMatrix", H, options={"precision": precision})
+    res, _, _ = _sweep(eng, T, cfg, u)
+    c2, ctx, le = oracle_sweep(fp32(T), shape, D, "DensityMatrix", chi, H, cfg, u)
+    assert np.array_equal(res.configs.numpy(), c2)
+    amp = (res.sign * torch.exp(res.logamp)).numpy()
+    assert np.max(np.abs(amp / ctx.amp - 1)) < (1e-9 if precision == "mixed" else 1e-4)
+    e_ref = le.local_estimate
+    assert np.max(np.abs(res.E.numpy() - e_ref) / np.maximum(1.0, np.abs(e_ref))) < 5e-5
+    o_ref = le.local_log_derivatives
+    assert np.max(np.linalg.norm(res.O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1)) < 5e-5
+    assert eng.status() == 0
+
+
+def test_complex_density_matrix_matches_oracle(emu_lib):
+    shape, D, chi = (4, 4), 3, 3
+    H = hamiltonian("tfim", shape)
+    T = complex_tensors(shape, D, seed=7)
+    rng = np.random.default_rng(7)
+    cfg = rng.integers(0, 2, (5, 16)).astype(np.int32)
+    u = rng.random((5, 16))
+    eng = PEPSEngine(shape, D, chi, 2, "DensityMatrix", operator=H, device="cpu", lib=emu_lib, dtype="complex64")
+    res, _, _ = _sweep(eng, T, cfg, u)
+    c2, ctx, le = oracle_sweep(T, shape, D, "DensityMatrix", chi, H, cfg, u)
+    assert np.array_equal(res.configs.numpy(), c2)
+    amp = np.exp(res.logamp.numpy() + 1j * res.sign.numpy())
+    assert np.max(np.abs(amp / ctx.amp - 1)) < 1e-4
+    o_ref = le.local_log_derivatives
+    assert np.max(np.linalg.norm(res.O.numpy() - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1)) < 5e-5
 
 
 def test_three_state_sites_with_explicit_flip_offsets(emu_lib):

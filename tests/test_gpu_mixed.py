@@ -43,6 +43,7 @@ CASES = [
     ((4, 4), 2, 4, "ZipUp", "tfim"),
     ((4, 4), 3, 6, "ZipUp", "heisenberg"),
     ((6, 6), 4, 16, "ZipUp", "heisenberg"),
+    ((4, 4), 3, 3, "DensityMatrix", "heisenberg"),
 ]
 
 

@@ -30,6 +30,9 @@ CASES = [
     ((3, 3), 2, 4, "Variational", "heisenberg"),
     ((4, 4), 3, 6, "Variational", "tfim"),
     ((3, 4), 2, 3, "Variational", "heisenberg"),
+    # DensityMatrix where every kept eigenvector has a nonzero eigenvalue (chi <= D)
+    ((3, 3), 2, 2, "DensityMatrix", "heisenberg"),
+    ((4, 4), 3, 3, "DensityMatrix", "tfim"),
 ]
 
 

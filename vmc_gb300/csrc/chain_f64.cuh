@@ -172,7 +172,31 @@ __device__ __noinline__ double apply_row_hp(const DevPlan& P, Shared& sh, const 
     cta_gemm_x(make_gemm_x(static_cast<const double*>(Z1), two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat,
                            two(dn, pout * ldm, Rb), two(Rb, ldm, 1), kc * dn, pout * Rb, Lb * pin));
     VMC_TSTOP(tth, PH_THETA);
-    if (mrows <= ncols && kout >= mrows) {
+    if (P.strategy == VMC_STRATEGY_DENSITY_MATRIX) {
+      // DensityMatrix (strategy.py:153-176): new tensor theta V, carry V^T, V = the top-kout eigenvectors
+      // of rho = theta^T theta (V = I when every column is kept)
+      if (kout >= ncols) {
+        for (int e = threadIdx.x; e < ncols * kout; e += blockDim.x) ar.Y[e] = (e / kout == e % kout) ? 1.0 : 0.0;
+        __syncthreads();
+      } else {
+        const int ldg = ncols | 1;
+        const double* cm = mat;
+        cta_gemm_x(make_gemm_x(cm, lin(1), ldm, cm, lin(1), ldm, ar.G, lin(ldg), lin(1), ncols, ncols, mrows));
+        cta_sym_topk<double>(ar.G, ncols, ldg, kout, ar.Y, kout, ar.eig, sh.red);
+        if (threadIdx.x == 0) {
+          const double lk = ar.eig.lam[kout - 1], lk1 = ar.eig.lam[kout];
+          const float gap = lk > 0.0 ? (float)fmax((lk - lk1) / lk, 0.0) : 0.f;
+          if (gap < *min_gap) *min_gap = gap;
+        }
+      }
+      cta_gemm_x(make_gemm_x(static_cast<const double*>(mat), lin(ldm), 1, static_cast<const double*>(ar.Y), lin(1),
+                             kout, out, lin(kout), lin(1), mrows, kout, ncols));
+      for (int e = threadIdx.x; e < kout * ncols; e += blockDim.x) {
+        const int kk = e / ncols, col = e % ncols;
+        carry_next[(size_t)kk * ncols + (col % Rb) * dn + col / Rb] = ar.Y[(size_t)col * kout + kk];
+      }
+      __syncthreads();
+    } else if (mrows <= ncols && kout >= mrows) {
       // every row direction is kept: U = I, carry = theta
       for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) out[e] = (e / mrows == e % mrows) ? 1.0 : 0.0;
       for (int e = threadIdx.x; e < mrows * ncols; e += blockDim.x) {

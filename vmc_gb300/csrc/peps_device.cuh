@@ -397,7 +397,39 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
     float* mat = ar.mat;
     gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat, two(dn, pout * ldm, Rb),
                        two(Rb, ldm, 1), kc * dn, pout * Rb, Lb * pin));
-    if (mrows <= ncols && kout >= mrows) {
+    if (P.strategy == VMC_STRATEGY_DENSITY_MATRIX) {
+      // ---- DensityMatrix (strategy.py:153-176): rho = theta^H theta and its top-kout eigenvectors V;
+      // the new tensor is theta V (columns not normalised) and the carry V^H.  With every column kept,
+      // V = I: rho's eigenbasis is then any unitary, which the carry undoes in the next theta, and the
+      // later column Grams (theta'^H theta') do not see it ----
+      if (kout >= ncols) {
+        for (int e = threadIdx.x; e < ncols * kout; e += blockDim.x) set_elem(ar.Y, e, (e / kout == e % kout) ? 1.f : 0.f);
+        __syncthreads();
+      } else {
+        const int ldg = ncols | 1;
+        gemm_ca(make_gemm(mat, lin(1), ldm, mat, lin(1), ldm, ar.G, lin(ldg), lin(1), ncols, ncols, mrows));
+        if (kCplx)
+          cta_herm_topk(ar.G, ncols, ldg, kout, ar.Y, kout, ar.eig, sh.red);
+        else
+          cta_sym_topk(ar.G, ncols, ldg, kout, ar.Y, kout, ar.eig, sh.red);
+        if (threadIdx.x == 0) {
+          // a kept eigenvalue at the rounding level of a null space: no gap (kept vectors arbitrary)
+          const float lk = ar.eig.lam[kout - 1], lk1 = ar.eig.lam[kout];
+          const float gap = lk > 0.f ? fmaxf((lk - lk1) / lk, 0.f) : 0.f;
+          if (gap < *min_gap) *min_gap = gap;
+        }
+      }
+      gemm(make_gemm(mat, lin(ldm), 1, ar.Y, lin(1), kout, out, lin(kout), lin(1), mrows, kout, ncols));
+      // carry'[k'][w][r'] = conj(V[(r', w)][k'])
+      for (int e = threadIdx.x; e < kout * ncols; e += blockDim.x) {
+        const int kk = e / ncols, col = e % ncols;
+        const float* y = elem(ar.Y, (size_t)col * kout + kk);
+        float* c = elem(carry_next, (size_t)kk * ncols + (col % Rb) * dn + col / Rb);
+        c[0] = y[0];
+        if (kCplx) c[1] = -y[1];
+      }
+      __syncthreads();
+    } else if (mrows <= ncols && kout >= mrows) {
       // every row direction is kept: U = I, carry = theta
       for (int e = threadIdx.x; e < mrows * mrows; e += blockDim.x) set_elem(out, e, (e / mrows == e % mrows) ? 1.f : 0.f);
       for (int e = threadIdx.x; e < mrows * ncols; e += blockDim.x) {

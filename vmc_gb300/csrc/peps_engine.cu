@@ -71,7 +71,9 @@ static std::vector<int> apply_bonds(const std::vector<int>& bin, const std::vect
   out[0] = left;
   for (int i = 0; i < C - 1; ++i) {
     const int m = left * pout, n = bin[i + 1] * wb[i + 1];
-    const int k = std::min(chi, std::min(m, n));
+    // ZipUp / Variational keep min(chi, rank bound); DensityMatrix keeps min(chi, columns) eigenvectors of
+    // the column Gram (strategy.py:167)
+    const int k = strategy == VMC_STRATEGY_DENSITY_MATRIX ? std::min(chi, n) : std::min(chi, std::min(m, n));
     out[i + 1] = k;
     left = k;
   }
@@ -270,10 +272,10 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
   if (phys_dim > (gi_N ? kMaxD : kMaxPhys)) return VMC_ERR_UNSUPPORTED;
   if (dtype != VMC_DTYPE_F32 && dtype != VMC_DTYPE_C64) return VMC_ERR_UNSUPPORTED;
   if (strategy < 0 || strategy > VMC_STRATEGY_VARIATIONAL || n_sweeps < 0) return VMC_ERR_INVALID;
-  // DensityMatrix (strategy.py:153-176) carries V_k^H without the singular
-  // values, so its next cut truncates an unweighted theta: not the ZipUp
-  // product, and ill-defined for rank-deficient theta.  Not implemented.
-  if (strategy == VMC_STRATEGY_DENSITY_MATRIX) return VMC_ERR_UNSUPPORTED;
+  // DensityMatrix (strategy.py:153-176) carries V_k^H: with the Gram eigensolver only (it is one), and
+  // not on gauge-invariant plans
+  if (strategy == VMC_STRATEGY_DENSITY_MATRIX && (gi_N > 0 || (opts && opts->trunc_method != 0)))
+    return VMC_ERR_UNSUPPORTED;
   vmc_plan* pl = new (std::nothrow) vmc_plan();
   if (!pl) return VMC_ERR_INVALID;
   DevPlan& P = pl->hp;
