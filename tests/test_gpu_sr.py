@@ -124,3 +124,42 @@ def test_tdvp_step_matches_oracle_stages(cuda_device, integrator, space):
         want = theta0 + dt * (ks[0] + 2 * ks[1] + 2 * ks[2] + ks[3]) / 6.0
     got = drv.model.packed().double().cpu().numpy()
     assert _rel(got - theta0, want - theta0) < 1e-5, _rel(got - theta0, want - theta0)
+
+
+@pytest.mark.parametrize("space,qr", [(SampleSpace(), False), (ParameterSpace(), False), (ParameterSpace(), True)],
+                         ids=["sample-direct", "parameter-direct", "parameter-qr"])
+def test_gauge_removed_solve_matches_the_dense_formulation(cuda_device, space, qr):
+    """Gauge removal on the GPU (6x6 D4 chi16, 512 samples, full gradient): the update against the
+    reference's formulation (solve with O Q, return Q y) evaluated with an explicit Q in FP64."""
+    from vmc_gb300.gauge import GaugeConfig, compute_gauge_projection
+    from vmc_gb300.preconditioners import QRSolve
+
+    shape, D, chi, n = (6, 6), 4, 16, 512
+    H = hamiltonian("heisenberg", shape)
+    T, cfg, u = make_case(shape, D, n, seed=3)
+    eng = PEPSEngine(shape, D, chi, 2, "ZipUp", operator=H, device=cuda_device, precision="mixed")
+    tens = torch.from_numpy(pack_tensors(T)).to(cuda_device)
+    c = torch.from_numpy(cfg).to(cuda_device)
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, torch.from_numpy(u).to(cuda_device), cache, full_gradient=True)
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(chi), device=cuda_device, tensors=T)
+    pre = SRPreconditioner(space=space, diag_shift=1e-3, gauge_config=GaugeConfig(),
+                           strategy=QRSolve() if qr else SRPreconditioner().strategy)
+    upd, metrics = pre.apply(model, model.tensors, res.configs, res.O, None, res.E)
+    x = model.packed(upd).double()
+    Q = compute_gauge_projection(GaugeConfig(), model, model.tensors).dense()
+    oc = res.O.double() @ Q
+    oc = oc - oc.mean(0)
+    e = res.E.double()
+    dv = (e - e.mean()) / n
+    if qr:
+        red = torch.linalg.lstsq(oc.cpu(), dv.cpu(), driver="gelsd", rcond=1e-12).solution.to(cuda_device)
+    elif isinstance(space, SampleSpace):
+        red = oc.T @ torch.linalg.solve(oc @ oc.T / n + 1e-3 * torch.eye(n, dtype=torch.float64, device=cuda_device),
+                                        dv)
+    else:
+        red = torch.linalg.solve(oc.T @ oc / n + 1e-3 * torch.eye(Q.shape[1], dtype=torch.float64,
+                                                                  device=cuda_device), oc.T @ dv)
+    want = 2.0 * (Q @ red)
+    assert torch.linalg.norm(x - want) / torch.linalg.norm(want) < 1e-5
+    assert metrics["gauge_rank"] == 2 * 6 * 5 * 16 + 1

@@ -87,6 +87,48 @@ def _direct_solve(space, jac, dv, diag_shift, solver):
     return x, {"residual_error": res}
 
 
+def _full_layout(o, p, model):
+    """The sliced O (n, n_params_sliced) scattered into the full layout (n, d * n_params_sliced): a
+    sample's columns of site s go to the block of its own slice p (ravel order of (d, u, v, l, r))."""
+    pps = params_per_site(model.shape, model.bond_dim)
+    d = model.phys_dim
+    base, sz = [], []
+    off = 0
+    for n_s in pps:
+        base.append(torch.arange(n_s, device=o.device) + d * off)
+        sz.append(torch.full((n_s,), n_s, device=o.device))
+        off += n_s
+    base = torch.cat(base)
+    sz = torch.cat(sz)
+    idx = base[None, :] + p.to(torch.int64) * sz[None, :]
+    full = torch.zeros((o.shape[0], d * off), dtype=o.dtype, device=o.device)
+    return full.scatter_(1, idx, o)
+
+
+def _gauge_direct_solve(space, O, dv, diag_shift, solver, proj):
+    """The SR solve in the complement of the gauge directions (preconditioners.py:288-309 with
+    O_eff = O Q and updates Q y), through U (proj.U, a basis of the gauge span): Q Q^H = 1 - U U^H."""
+    O = O.to(torch.complex128 if O.is_complex() else torch.float64)
+    n = O.shape[0]
+    Oc = O - O.mean(dim=0)
+    U = proj.U.to(O.dtype)
+    eye = lambda k: torch.eye(k, dtype=O.dtype, device=O.device)  # noqa: E731
+    if isinstance(space, SampleSpace):
+        W = Oc @ U
+        T = (Oc @ Oc.conj().T - W @ W.conj().T) / n
+        y = solver(T + diag_shift * eye(n), dv)
+        x = proj.project(Oc.conj().T @ y)
+        res = torch.linalg.norm(T @ y - dv) ** 2 / torch.linalg.norm(dv) ** 2
+        return x, {"residual_error": res, "gauge_rank": proj.rank}
+    S = (Oc.conj().T @ Oc) / n
+    SU = S @ U
+    PSP = S - U @ SU.conj().T - SU @ U.conj().T + U @ (U.conj().T @ SU) @ U.conj().T
+    F = proj.project(Oc.conj().T @ dv)
+    x = solver(PSP + diag_shift * eye(S.shape[0]), F)
+    res = torch.linalg.norm(PSP @ x - F) ** 2 / torch.linalg.norm(F) ** 2
+    return x, {"residual_error": res, "gauge_rank": proj.rank}
+
+
 def _qr_solve(jac: Jacobian, dv, rcond, min_norm, lib=None):
     """preconditioners.py:166-214: column-pivoted QR of the centred full Jacobian (diag shift
     unused), all in FP64 (complex128) on the Jacobian's device: the factorisation is the
@@ -164,10 +206,6 @@ class SRPreconditioner:
 
     def apply(self, model, params, samples, o, p, local_energies, *, grad_factor=1.0):
         """Returns (updates as a list of per-site tensors shaped like model.tensors, metrics)."""
-        if self.gauge_config is not None:
-            from .gauge import compute_gauge_projection
-
-            compute_gauge_projection(self.gauge_config, model, params)
         e = local_energies.reshape(-1)
         e = e.to(torch.complex128 if e.is_complex() else torch.float64)
         n_samples = samples.shape[0]
@@ -181,6 +219,30 @@ class SRPreconditioner:
         # slices per site: phys_dim, or a GI model's phys_dim * nc per site (src/vmc/peps/gi/model.py:1066-1080)
         sd = model.sliced_dims() if hasattr(model, "sliced_dims") else (model.phys_dim,) * (
             model.shape[0] * model.shape[1])
+        if self.gauge_config is not None:
+            # gauge removal (preconditioners.py:288-309): the solve in the complement of the gauge span,
+            # the update returned in the full parameter layout
+            from .gauge import compute_gauge_projection
+
+            if hasattr(model, "sliced_dims"):
+                raise NotImplementedError("gauge removal: standard PEPS")
+            proj = compute_gauge_projection(self.gauge_config, model, params)
+            O_full = o if p is None else _full_layout(o, p, model)
+            if isinstance(self.strategy, DirectSolve):
+                x, metrics = _gauge_direct_solve(self.space, O_full, dv, self.diag_shift, self.strategy.solver,
+                                                 proj)
+            else:
+                if isinstance(self.space, SampleSpace):
+                    raise NotImplementedError("QRSolve not supported for SampleSpace")
+                # the minimum-norm solution of (O P) x = dv lies in range(P) and equals Q (O Q)^+ dv
+                o_p = proj.project_rows(O_full.to(proj.U.dtype))
+                x, metrics = _qr_solve(Jacobian(o_p), dv, self.strategy.rcond, self.strategy.min_norm)
+                metrics = dict(metrics, gauge_rank=proj.rank)
+            param_dtype = getattr(model, "dtype", torch.float32)
+            if not complex_factor and not param_dtype.is_complex:
+                x = 2.0 * x.real
+            self._metrics = metrics
+            return model.unpack(x.to(param_dtype)), metrics
         jac = Jacobian(o) if p is None else SlicedJacobian(o, p, sd, self.ordering)
         if isinstance(self.strategy, DirectSolve):
             x, metrics = _direct_solve(self.space, jac, dv, self.diag_shift, self.strategy.solver)
