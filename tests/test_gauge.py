@@ -52,6 +52,8 @@ def test_projection_is_orthogonal_and_spans_the_generators():
     assert torch.allclose(U.T @ U, torch.eye(U.shape[1], dtype=U.dtype), atol=1e-12)
     G = gauge_generators(model)
     assert torch.linalg.norm(proj.project(G)) < 1e-10 * torch.linalg.norm(G)
+    # the scalar bond gauges are dependent around each of the 6 plaquettes of the 3 x 4 lattice
+    assert info["n_generators"] == 17 * D * D + 1 and info["rank"] == 17 * D * D - 6 + 1
     Q = proj.dense()
     assert Q.shape == (proj.n_params, proj.n_params - info["rank"])
     x = torch.randn(proj.n_params, dtype=torch.float64)

@@ -162,4 +162,6 @@ def test_gauge_removed_solve_matches_the_dense_formulation(cuda_device, space, q
                                                                   device=cuda_device), oc.T @ dv)
     want = 2.0 * (Q @ red)
     assert torch.linalg.norm(x - want) / torch.linalg.norm(want) < 1e-5
-    assert metrics["gauge_rank"] == 2 * 6 * 5 * 16 + 1
+    # 60 bonds x D^2 generators and the global scale, less one dependency per plaquette: the scalar
+    # (T = 1) gauges span the lattice graph's cut space, of dimension n_sites - 1 = 35, not 60
+    assert metrics["gauge_rank"] == 60 * 16 - 25 + 1
