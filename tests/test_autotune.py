@@ -37,7 +37,7 @@ def test_every_candidate_matches_the_oracle(emu_lib, options):
 def test_invalid_options_are_refused(emu_lib):
     shape = _abi.VmcShape(3, 3)
     plan = ct.c_void_p()
-    for bad in [(48, -1, 0), (300, -1, 0), (128, -2, 0), (128, -1, 4), (128, -1, -1)]:
+    for bad in [(48, -1, 0), (300, -1, 0), (128, -2, 0), (128, -1, 5), (128, -1, -1)]:
         o = _abi.VmcPlanOptions(*bad)
         assert emu_lib.vmc_peps_plan_ex(ct.byref(shape), 2, 4, 2, 0, 1, 2, ct.byref(o), ct.byref(plan)) == \
             _abi.VMC_ERR_INVALID

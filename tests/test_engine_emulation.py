@@ -107,8 +107,10 @@ def test_amp_grad_and_local_energy_match_oracle(emu_lib):
 
 
 @pytest.mark.parametrize("opts", [{"vchunk": 1, "vert_smem": 1}, {"trunc_method": "jacobi"}, {"smem_kb": 0},
-                                  {"smem_kb": 24}, {"tile_policy": 1}, {"tile_policy": 2}],
-                         ids=["chunk1", "jacobi", "all-global", "mat-global", "small-tiles", "large-tiles"])
+                                  {"smem_kb": 24}, {"tile_policy": 1}, {"tile_policy": 2},
+                                  {"threads": 128, "tile_policy": 4}],
+                         ids=["chunk1", "jacobi", "all-global", "mat-global", "small-tiles", "large-tiles",
+                              "tcgen05-plan"])
 def test_alternative_engine_paths_match_oracle(emu_lib, opts):
     """Chunked vertical energy, the Jacobi truncation and the global-memory fallbacks agree with the oracle."""
     shape, D, chi = (4, 4), 3, 6

@@ -47,16 +47,17 @@ def test_tune_then_auto(cuda_device, tmp_path, monkeypatch):
     assert eng.options == entry["options"]
 
 
+@pytest.mark.parametrize("policy", [3, 4], ids=["mma-sync", "tcgen05"])
 @pytest.mark.parametrize("threads", [128, 256])
-def test_tensor_core_policy_at_large_bonds(cuda_device, threads):
-    """tile_policy 3 (3xTF32 tensor-core GEMMs) where its GEMMs engage: 4x4, D=6, chi=36 against the FP64
-    oracle, with the bars of an active truncation (the FFMA tiles give a median of 3e-6 and a maximum of
-    8e-5 on these samples)."""
+def test_tensor_core_policy_at_large_bonds(cuda_device, threads, policy):
+    """tile_policies 3 (3xTF32 mma.sync GEMMs) and 4 (3xTF32 tcgen05 GEMMs, accumulators in tensor memory)
+    where their GEMMs engage: 4x4, D=6, chi=36 against the FP64 oracle, with the bars of an active
+    truncation (the FFMA tiles give a median of 3e-6 and a maximum of 8e-5 on these samples)."""
     shape, D, chi = (4, 4), 6, 36
     H = hamiltonian("heisenberg", shape)
     T, cfg, _ = make_case(shape, D, 6, seed=21)
     eng = PEPSEngine(shape, D, chi, 2, "ZipUp", operator=H, device=cuda_device,
-                     options={"threads": threads, "smem_kb": -1, "tile_policy": 3})
+                     options={"threads": threads, "smem_kb": -1, "tile_policy": policy})
     tens = torch.from_numpy(pack_tensors(T)).to(cuda_device)
     c = torch.from_numpy(cfg).to(cuda_device)
     la, sg, O = eng.amp_grad(tens, c)

@@ -111,8 +111,34 @@ def test_mixed_precision_plans_outside_its_scope_are_refused(emu_lib, dtype, str
     assert st == _abi.VMC_ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("dtype,opts,gi", [
+    (_abi.VMC_DTYPE_C64, {}, False),
+    (_abi.VMC_DTYPE_F32, {"threads": 64}, False),
+    (_abi.VMC_DTYPE_F32, {"precision": "mixed"}, False),
+    (_abi.VMC_DTYPE_F32, {}, True),
+], ids=["complex", "two-warps", "mixed", "gi"])
+def test_tcgen05_tiles_outside_their_scope_are_refused(emu_lib, dtype, opts, gi):
+    """tile_policy 4 runs real FP32 standard plans in CTAs of at least four warps (one per TMEM lane
+    quadrant of the 128-row accumulator)."""
+    o = _abi.plan_options(dict({"tile_policy": 4}, **opts))
+    plan = ct.c_void_p()
+    if gi:
+        st = emu_lib.vmc_gi_plan(ct.byref(_abi.VmcShape(3, 3)), 2, 2, 4, dtype, _abi.VMC_STRATEGY_ZIP_UP, 2,
+                                 ct.byref(o), ct.byref(plan))
+    else:
+        st = emu_lib.vmc_peps_plan_ex(ct.byref(_abi.VmcShape(4, 4)), 3, 6, 2, dtype, _abi.VMC_STRATEGY_ZIP_UP, 2,
+                                      ct.byref(o), ct.byref(plan))
+    assert st == _abi.VMC_ERR_UNSUPPORTED
+    st = emu_lib.vmc_peps_plan_ex(ct.byref(_abi.VmcShape(4, 4)), 3, 6, 2, _abi.VMC_DTYPE_F32,
+                                  _abi.VMC_STRATEGY_ZIP_UP, 2, ct.byref(_abi.plan_options({"tile_policy": 4})),
+                                  ct.byref(plan))
+    assert st == _abi.VMC_OK
+    emu_lib.vmc_plan_destroy(plan)
+
+
 def test_invalid_plan_options_are_rejected(emu_lib):
-    for bad in ({"precision": 2}, {"trunc_method": 2}, {"vchunk": -1}, {"vert_smem": -1}):
+    for bad in ({"precision": 2}, {"trunc_method": 2}, {"vchunk": -1}, {"vert_smem": -1}, {"tile_policy": 5},
+                {"precision": 2, "tile_policy": 4}):
         plan = ct.c_void_p()
         st = emu_lib.vmc_peps_plan_ex(ct.byref(_abi.VmcShape(4, 4)), 3, 6, 2, _abi.VMC_DTYPE_F32,
                                       _abi.VMC_STRATEGY_ZIP_UP, 2, ct.byref(_abi.plan_options(bad)), ct.byref(plan))

@@ -38,6 +38,8 @@ CANDIDATES = [
     {"threads": 64, "smem_kb": 20, "tile_policy": 0},
     {"threads": 128, "smem_kb": -1, "tile_policy": 3},
     {"threads": 256, "smem_kb": -1, "tile_policy": 3},
+    {"threads": 128, "smem_kb": -1, "tile_policy": 4},
+    {"threads": 256, "smem_kb": -1, "tile_policy": 4},
 ]
 
 _LOCK = threading.Lock()

@@ -270,6 +270,184 @@ __device__ inline void gemm_mma(const Gemm& g) {
 }
 #endif
 
+#ifndef VMC_GEMM_TCGEN05
+#define VMC_GEMM_TCGEN05 0
+#endif
+// CTA GEMMs large enough for a 128-row tensor-core tile run on tcgen05 (tile policy 4)
+constexpr bool kGemmTcgen05 = VMC_GEMM_TCGEN05 != 0;
+// shared-memory staging of one K chunk of a tcgen05 GEMM: A (128 x 32) and B (128 x 32), TF32 hi and lo
+constexpr int kTcRows = 128, kTcK = 32;
+constexpr long long kTcStageBytes = 4LL * kTcRows * kTcK * 4;  // 64 KB
+constexpr int kTcTmemCols = 128;
+
+#if VMC_GEMM_TCGEN05 && !defined(VMC_HOST_EMULATION)
+// ---------------------------------------------------------------------------
+// tcgen05 path (sm_100 family): C = alpha * A B on the 5th-generation tensor cores with the accumulator
+// in tensor memory.  Per 128-row x (<= 128)-column tile of C and 32-deep K chunk, the CTA stages A and B
+// from their index maps into shared memory in the no-swizzle K-major canonical layout (8-row x 16-byte
+// core matrices; LBO = byte stride between core matrices along K, SBO = 128 between 8-row groups), split
+// into TF32 hi and lo parts; one thread issues hi*hi + hi*lo + lo*hi (12 kind::tf32 MMAs of K = 8),
+// commits them to an mbarrier and the CTA waits (bounded: a timeout sets VMC_DEV_TIMEOUT in the status
+// word and the GEMM carries on with whatever the accumulator holds).  The products keep ~2^-22 relative
+// accuracy, FP32 level.  Warps read the accumulator back with tcgen05.ld (warp w: TMEM lanes
+// 32 (w % 4) .. +31 = tile rows; warp groups split the columns) and write C through its index maps.
+// ---------------------------------------------------------------------------
+VMC_SHARED uint32_t g_tc_tmem;          // TMEM base address (column 0, lane 0) of this CTA
+VMC_SHARED __align__(8) uint64_t g_tc_mbar;
+VMC_SHARED uint32_t g_tc_phase;         // parity of the mbarrier phase the next commit completes
+VMC_SHARED int32_t* g_tc_status;        // the launch's status word
+
+__device__ __forceinline__ uint32_t smem_addr_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Kernel start, all threads: TMEM columns for the accumulator (warp 0), the mbarrier (thread 0).
+__device__ inline void tc_setup(int32_t* status) {
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr_u32(&g_tc_tmem)),
+                 "r"((uint32_t)kTcTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr_u32(&g_tc_mbar)));
+    g_tc_phase = 0;
+    g_tc_status = status;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+}
+
+// Kernel end, all threads: return the TMEM columns (every MMA was waited for).
+__device__ inline void tc_teardown() {
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if ((threadIdx.x >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(g_tc_tmem), "r"((uint32_t)kTcTmemCols));
+}
+
+// Stage rows [r0, r0 + 128) x k [k0, k0 + 32) of an operand (row offsets `rm`, k stride `sk`) as TF32 hi
+// and lo in the canonical layout; rows >= nrows and k >= K are zero.
+__device__ __forceinline__ void tc_stage(const float* X, const IMap& rm, int sk, int nrows, int K, int r0, int k0,
+                                         unsigned char* hi, unsigned char* lo) {
+  constexpr uint32_t lbo = (kTcRows / 8) * 128;
+  for (int e = threadIdx.x; e < kTcRows * kTcK; e += blockDim.x) {
+    const int r = e / kTcK, k = e % kTcK;
+    const int gr = r0 + r, gk = k0 + k;
+    float x = 0.f;
+    if (gr < nrows && gk < K) x = X[imap(rm, gr) + (size_t)gk * sk];
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(x - __uint_as_float(h)));
+    const uint32_t off = (k >> 2) * lbo + (r >> 3) * 128 + (r & 7) * 16 + (k & 3) * 4;
+    *reinterpret_cast<uint32_t*>(hi + off) = h;
+    *reinterpret_cast<uint32_t*>(lo + off) = l;
+  }
+}
+
+// Bounded wait for the mbarrier phase the last commit completes; flips the CTA's phase.
+__device__ __forceinline__ void tc_wait() {
+  const uint32_t bar = smem_addr_u32(&g_tc_mbar), parity = g_tc_phase;
+  uint32_t done = 0;
+  for (long long it = 0; it < (1LL << 26) && !done; ++it) {
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity));
+  }
+  if (!done && threadIdx.x == 0) atomicOr(g_tc_status, 2);  // VMC_DEV_TIMEOUT
+  __syncthreads();
+  if (threadIdx.x == 0) g_tc_phase = parity ^ 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;");
+}
+
+__device__ inline void gemm_tc5(const Gemm& g) {
+  extern __shared__ __align__(16) float dyn_smem[];
+  unsigned char* stage = reinterpret_cast<unsigned char*>(dyn_smem);
+  unsigned char* a_hi = stage;
+  unsigned char* a_lo = stage + kTcRows * kTcK * 4;
+  unsigned char* b_hi = stage + 2 * kTcRows * kTcK * 4;
+  unsigned char* b_lo = stage + 3 * kTcRows * kTcK * 4;
+  constexpr uint32_t lbo = (kTcRows / 8) * 128;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int quad = warp & 3, group = warp >> 2, ngroups = nwarps >= 8 ? 2 : 1;
+  const uint32_t tmem = g_tc_tmem;
+  for (int m0 = 0; m0 < g.M; m0 += kTcRows) {
+    for (int n0 = 0; n0 < g.N; n0 += kTcTmemCols) {
+      const int nt = min(kTcTmemCols, g.N - n0);
+      const int ntp = (nt + 15) & ~15;  // MMA N: a multiple of 16 (zero rows of B beyond N)
+      const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(ntp >> 3) << 17) |
+                             ((uint32_t)(kTcRows >> 4) << 24);
+      for (int k0 = 0; k0 < g.K; k0 += kTcK) {
+        tc_stage(g.A, g.am, g.sak, g.M, g.K, m0, k0, a_hi, a_lo);
+        // B as rows n (N x K, K-major): element (n, k) at B[bn(n) + k sbk]
+        tc_stage(g.B, g.bn, g.sbk, g.N, g.K, n0, k0, b_hi, b_lo);
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const int ksteps = min(kTcK, g.K - k0 + 7) / 8;
+          for (int s = 0; s < ksteps; ++s) {
+            const uint32_t ao = s * 2 * lbo;
+            const uint64_t dah = tc_smem_desc(smem_addr_u32(a_hi) + ao, lbo, 128);
+            const uint64_t dal = tc_smem_desc(smem_addr_u32(a_lo) + ao, lbo, 128);
+            const uint64_t dbh = tc_smem_desc(smem_addr_u32(b_hi) + ao, lbo, 128);
+            const uint64_t dbl = tc_smem_desc(smem_addr_u32(b_lo) + ao, lbo, 128);
+            const uint32_t first = (k0 == 0 && s == 0) ? 0u : 1u;
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                "l"(dal), "l"(dbh), "r"(idesc), "r"(first));
+            asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dah), "l"(dbl),
+                         "r"(idesc));
+            asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dah), "l"(dbh),
+                         "r"(idesc));
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr_u32(&g_tc_mbar)));
+        }
+        tc_wait();  // the staging buffers are rewritten by the next chunk
+      }
+      // accumulator -> C: warp quad q holds rows 32 q .. +31 of the tile; column groups split by warp group
+      if (warp < 4 * ngroups) {
+        const int row = m0 + quad * 32 + lane;
+        const int cols_per = ((ntp / ngroups) + 7) & ~7;
+        const int c_begin = group * cols_per, c_end = min(ntp, c_begin + cols_per);
+        const int co = row < g.M ? imap(g.cm, row) : 0;
+        for (int c0 = c_begin; c0 < c_end; c0 += 8) {
+          uint32_t v[8];
+          const uint32_t addr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                         "=r"(v[7])
+                       : "r"(addr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+          if (row < g.M) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int n = n0 + c0 + j;
+              if (c0 + j < nt) {
+                float* dst = g.C + co + imap(g.cn, n);
+                const float val = g.alpha * __uint_as_float(v[j]);
+                *dst = g.accumulate ? (*dst + val) : val;
+              }
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncthreads();  // the next tile's MMAs overwrite the accumulator
+      asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+  }
+}
+#endif
+
 // CTA-wide GEMM; ends with a barrier so C is visible to the whole CTA.
 // Register-tile policy of the CTA's GEMMs, set per chain from its plan (an
 // autotuned choice per (D, chi)): 0 the default thresholds below; 1 smaller
@@ -300,6 +478,13 @@ VMC_GEMM_LINKAGE void cta_gemm(const Gemm& g) {
     __syncthreads();
     return;
   }
+#if VMC_GEMM_TCGEN05 && !defined(VMC_HOST_EMULATION)
+  if (g.M >= 64 && g.N >= 16 && g.K >= 16 && (long long)g.M * g.N * g.K >= (1LL << 17)) {
+    gemm_tc5(g);
+    __syncthreads();
+    return;
+  }
+#endif
 #ifndef VMC_HOST_EMULATION
   if (kGemmTensorCores && g.M >= 16 && g.N >= 8 && g.K >= 8 && work >= nt * 32) {
     gemm_mma(g);

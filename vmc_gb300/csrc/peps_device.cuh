@@ -1335,6 +1335,9 @@ __global__ void __launch_bounds__(kThreads, VMC_MIN_CTAS) peps_kernel(const __gr
   VMC_SHARED int item;
   float* slot = slots + (size_t)blockIdx.x * jobs.slot_floats;
   const int total = jobs.first[jobs.n_jobs];
+#if VMC_GEMM_TCGEN05 && !defined(VMC_HOST_EMULATION)
+  tc_setup(status);
+#endif
   for (int i = blockIdx.x;; i += gridDim.x) {
     if (next) {
       if (threadIdx.x == 0) item = atomicAdd(next, 1);
@@ -1347,6 +1350,9 @@ __global__ void __launch_bounds__(kThreads, VMC_MIN_CTAS) peps_kernel(const __gr
     while (j + 1 < jobs.n_jobs && i >= jobs.first[j + 1]) ++j;
     run_chain(jobs.job[j], i - jobs.first[j], slot, status);
   }
+#if VMC_GEMM_TCGEN05 && !defined(VMC_HOST_EMULATION)
+  tc_teardown();
+#endif
 }
 #else  // the gauge-invariant translation unit
 

@@ -155,6 +155,7 @@ static vmc_status upload_plan(vmc_plan* pl) {
     G.mat_in_smem = L.mat_in_smem;
     G.arena_floats = L.arena_floats;
     G.arena_g_floats = L.arena_g_floats;
+    G.dyn_smem_bytes = L.dyn_smem_bytes;
     G.scr1 = L.scr1;
     G.vchunk = L.vchunk;
     G.vbuf = L.vbuf;
@@ -256,15 +257,20 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
   if (!shape || !out_plan) return VMC_ERR_INVALID;
   if (opts && (opts->threads != 0 && (opts->threads < 64 || opts->threads > kThreads || opts->threads % 32 != 0)))
     return VMC_ERR_INVALID;
-  if (opts && (opts->tile_policy < 0 || opts->tile_policy > 3 || opts->smem_kb < -1)) return VMC_ERR_INVALID;
+  if (opts && (opts->tile_policy < 0 || opts->tile_policy > 4 || opts->smem_kb < -1)) return VMC_ERR_INVALID;
   if (opts && (opts->precision < VMC_PRECISION_FP32 || opts->precision > VMC_PRECISION_MIXED ||
                opts->trunc_method < 0 || opts->trunc_method > 1 || opts->vchunk < 0 || opts->vert_smem < 0))
     return VMC_ERR_INVALID;
+  // tile policy 4 (tcgen05 GEMMs): real FP32 standard plans, CTAs of at least 4 warps (one per TMEM lane quadrant)
+  if (opts && opts->tile_policy == 4 &&
+      (dtype != VMC_DTYPE_F32 || gi_N > 0 || opts->precision != VMC_PRECISION_FP32 ||
+       (opts->threads != 0 && opts->threads < 128)))
+    return VMC_ERR_UNSUPPORTED;
   const int precision = opts ? opts->precision : VMC_PRECISION_FP32;
   // the FP64 chain exists for real ZipUp / NoTruncation plans with the Gram eigensolver and FFMA tiles
   if (precision == VMC_PRECISION_MIXED &&
       (dtype != VMC_DTYPE_F32 || gi_N > 0 || strategy == VMC_STRATEGY_VARIATIONAL || opts->trunc_method != 0 ||
-       opts->tile_policy == 3))
+       opts->tile_policy >= 3))
     return VMC_ERR_UNSUPPORTED;
   *out_plan = nullptr;
   const int R = shape->n_rows, C = shape->n_cols;
@@ -386,6 +392,8 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
   const long long smem_cap = P.chain64 ? kMaxArenaSmemBytesF64 : kMaxArenaSmemBytes;
   long long budget = P.chain64 ? kDefaultArenaSmemBytesF64 : kMaxArenaSmemBytes;
   if (opts && opts->smem_kb >= 0) budget = std::min<long long>(opts->smem_kb * 1024LL, smem_cap);
+  // tile policy 4: the dynamic shared memory is the tcgen05 staging area; every other buffer in the slot
+  if (P.tile_policy == 4) budget = 0;
   const int opt_vchunk = opts ? opts->vchunk : 0;
   const int opt_vert_smem = opts ? opts->vert_smem : 0;
   // Buffer placement for a shared-memory budget (bytes per CTA): truncation
@@ -450,11 +458,13 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
                     (Q.chain64 ? 2 * chain_f64_doubles(C, TS, SCR) : 0);
   };
   lay_out(P, budget);
+  P.dyn_smem_bytes = P.tile_policy == 4 ? kTcStageBytes : (P.arena_in_smem ? P.arena_floats * 4 : 0);
   // The same plan with everything in the slot (no dynamic shared memory): an
   // uneven batch dominated by plans too large for shared memory runs them all
   // this way, so those keep the whole L1 (shared memory and L1 share one array).
   pl->hpg = P;
   lay_out(pl->hpg, 0);
+  pl->hpg.dyn_smem_bytes = P.tile_policy == 4 ? kTcStageBytes : 0;
   P.cache_floats_per_chain = al64((long long)R * C * TS);
   if (chimax * D > kMaxVec) {
     delete pl;
@@ -467,7 +477,7 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
     return st;
   }
   {
-    const size_t smem = P.arena_in_smem ? (size_t)P.arena_floats * 4 : 0;
+    const size_t smem = (size_t)P.dyn_smem_bytes;
     int per_sm = 4, occ = 0;
     if (kernels_of(P).prepare(P.threads, smem, &occ) == cudaSuccess && occ > 0) per_sm = occ;
     pl->slots_max = vmc_num_sms() * per_sm;
@@ -588,7 +598,7 @@ static vmc_status run_job(const vmc_plan* pl, void* stream, ChainJob J, float* w
   bj.first[1] = J.n_chains;
   bj.n_jobs = 1;
   bj.slot_floats = pl->hp.slot_floats;
-  const size_t smem = pl->hp.arena_in_smem ? (size_t)pl->hp.arena_floats * 4 : 0;
+  const size_t smem = (size_t)pl->hp.dyn_smem_bytes;
   return K.run(bj, grid, pl->hp.threads, smem, stream, wsf + pl->hp.perm_floats, nullptr, status) == cudaSuccess
              ? VMC_OK
              : VMC_ERR_CUDA;
@@ -810,7 +820,7 @@ static vmc_status batch_layout(const vmc_peps_job* jobs, int n_jobs, int layout,
     if (j.n_chains == 0) continue;
     total += j.n_chains;
     L->slot_floats = std::max(L->slot_floats, P.slot_floats);
-    L->smem = std::max(L->smem, P.arena_in_smem ? (size_t)P.arena_floats * 4 : (size_t)0);
+    L->smem = std::max(L->smem, (size_t)P.dyn_smem_bytes);
     L->order[L->n++] = i;
   }
   if (total > 0x7fffffffLL) return VMC_ERR_UNSUPPORTED;

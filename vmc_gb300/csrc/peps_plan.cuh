@@ -59,6 +59,7 @@ struct DevPlan {
   int tile_policy;        // register-tile policy of the CTA GEMMs (cta_gemm)
   long long arena_floats;
   long long arena_g_floats;  // floats of the truncation arena that live in the CTA's slot
+  long long dyn_smem_bytes;  // dynamic shared memory per CTA (the arena's, or tcgen05 staging for tile policy 4)
   int scr1;               // size of one 1-row GEMM intermediate (floats)
   int vchunk, vbuf;       // vertical-energy chunk (bond values) and buffer size (floats)
   int vert_in_smem;       // vertical-energy buffers live in the shared-memory arena
@@ -230,6 +231,7 @@ struct KernelSet {
 };
 namespace rk { const KernelSet& kernels(); }  // real FP32 elements
 namespace rt { const KernelSet& kernels(); }  // real FP32 elements, tensor-core GEMMs (tile_policy 3)
+namespace rq { const KernelSet& kernels(); }  // real FP32 elements, tcgen05 GEMMs (tile_policy 4)
 namespace rm { const KernelSet& kernels(); }  // real, mixed precision: FP64 boundary-MPS chain
 namespace ck { const KernelSet& kernels(); }  // complex64 elements
 namespace gr { const KernelSet& kernels(); }  // gauge-invariant plans, real FP32
@@ -238,6 +240,7 @@ inline const KernelSet& kernels_of(const DevPlan& P) {
   if (P.gi) return P.es == 2 ? gc::kernels() : gr::kernels();
   if (P.es == 2) return ck::kernels();
   if (P.chain64) return rm::kernels();
+  if (P.tile_policy == 4) return rq::kernels();
   return P.tile_policy == 3 ? rt::kernels() : rk::kernels();
 }
 
