@@ -165,3 +165,30 @@ def test_gauge_removed_solve_matches_the_dense_formulation(cuda_device, space, q
     # 60 bonds x D^2 generators and the global scale, less one dependency per plaquette: the scalar
     # (T = 1) gauges span the lattice graph's cut space, of dimension n_sites - 1 = 35, not 60
     assert metrics["gauge_rank"] == 60 * 16 - 25 + 1
+
+
+@pytest.mark.parametrize("space", [SampleSpace(), ParameterSpace()], ids=["sample", "parameter"])
+def test_graph_tdvp_step_matches_oracle(cuda_device, space):
+    """A replayed GraphTDVPDriver Euler step: the parameter change over the replay is dt times the
+    oracle's SR update (oracle/sr.py) of the sweep outputs the replay left in the driver's buffers."""
+    from vmc_gb300.tdvp_graph import GraphTDVPDriver
+
+    shape, D, chi = (4, 4), 3, 6
+    H = hamiltonian("heisenberg", shape)
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(chi), device=cuda_device, rngs=5)
+    dt = 0.02
+    drv = GraphTDVPDriver(model, H, preconditioner=SRPreconditioner(space=space, diag_shift=1e-3), dt=dt,
+                          time_unit=ImaginaryTimeUnit(), integrator=Euler(), n_samples=N_SAMPLES,
+                          n_chains=N_CHAINS, sampler_key=9)
+    drv.run(2 * dt)  # the eager step, then the capture
+    assert drv._graph is not None
+    theta0 = drv.parameters.double().cpu().numpy()
+    drv.run(dt)      # one replay
+    theta1 = drv.parameters.double().cpu().numpy()
+    n = N_SAMPLES
+    o = drv._O.reshape(-1, drv._O.shape[-1])[:n]
+    p = drv._p.reshape(-1, drv._p.shape[-1])[:n]
+    e = drv._E.reshape(-1)[:n]
+    x_ref = _oracle_update(o, p, e, shape, D, osr.SampleSpace() if isinstance(space, SampleSpace)
+                           else osr.ParameterSpace(), 1e-3, grad_factor=drv.time_unit.grad_factor)
+    assert _rel(theta1 - theta0, dt * x_ref) < 1e-5, _rel(theta1 - theta0, dt * x_ref)

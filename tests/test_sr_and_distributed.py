@@ -184,3 +184,69 @@ def test_two_gloo_ranks_reduce_like_one_process():
     ref = osr.to_dense(osr.SlicedJacobian(o, p, sd, osr.SliceOrdering()), osr.ParameterSpace())
     assert np.allclose(S, ref, rtol=1e-10, atol=1e-12)
     assert np.array_equal(go, o) and np.array_equal(gp, p)
+
+
+def _tdvp_driver(lib, group=None, integrator=None):
+    from vmc_gb300 import PEPS, ZipUp
+    from vmc_gb300.drivers import Euler, ImaginaryTimeUnit, TDVPDriver
+    from vmc_gb300.operators import transverse_field_ising
+    from vmc_gb300.preconditioners import SRPreconditioner
+    from tests.helpers import uniform_init_tensors
+
+    shape, D = (2, 3), 2
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(4), tensors=uniform_init_tensors(shape, D, seed=3),
+                 device="cpu", lib=lib)
+    # 5 chains over 2 ranks (3 + 2), 16 samples of 4 sweeps per chain (20 drawn, 16 kept)
+    return TDVPDriver(model, transverse_field_ising(shape), dt=0.01, time_unit=ImaginaryTimeUnit(),
+                      integrator=integrator or Euler(),
+                      preconditioner=SRPreconditioner(space=gq.SampleSpace(), diag_shift=1e-2), n_samples=16,
+                      n_chains=5, sampler_key=5, process_group=group)
+
+
+def _tdvp_worker(rank, world, port, lib_path, out):
+    from vmc_gb300 import _abi
+    from vmc_gb300.drivers import RK4
+
+    torch.set_num_threads(1)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        drv = _tdvp_driver(_abi.bind(lib_path), dist.group.WORLD, RK4())
+        drv.run(0.02)
+        out.put((rank, drv.model.packed().numpy().copy(), float(drv.energy["mean"]),
+                 drv._sampler_configuration.numpy().copy()))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_tdvp_driver_equals_one_process(emu_lib):
+    """TDVPDriver over 2 gloo ranks (uneven shards of 3 + 2 chains, two RK4 steps): both ranks end with the
+    parameters and energy of the one-process run, bit for bit, and each holds its shard's configurations."""
+    from tests.conftest import build_emulation_library
+    from vmc_gb300.drivers import RK4
+
+    n_threads = torch.get_num_threads()
+    torch.set_num_threads(1)
+    try:
+        ref = _tdvp_driver(emu_lib, None, RK4())
+        ref.run(0.02)
+    finally:
+        torch.set_num_threads(n_threads)
+    theta = ref.model.packed().numpy()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + ((os.getpid() + 7) % 2000)
+    procs = [ctx.Process(target=_tdvp_worker, args=(r, 2, port, str(build_emulation_library()), q))
+             for r in range(2)]
+    for pr in procs:
+        pr.start()
+    res = sorted([q.get(timeout=300) for _ in range(2)], key=lambda r: r[0])
+    for pr in procs:
+        pr.join(timeout=60)
+        assert pr.exitcode == 0
+    for rank, th, e, cfg in res:
+        assert np.array_equal(th, theta), rank
+        assert e == float(ref.energy["mean"])
+    cfg_all = np.concatenate([r[3] for r in res])
+    assert np.array_equal(cfg_all, ref._sampler_configuration.numpy())

@@ -349,11 +349,13 @@ __device__ __forceinline__ void tc_stage(const float* X, const IMap& rm, int sk,
   }
 }
 
-// Bounded wait for the mbarrier phase the last commit completes; flips the CTA's phase.
+// Bounded wait for the mbarrier phase the last commit completes; flips the CTA's phase.  Once any CTA of
+// the launch has timed out, no further wait spins: the launch runs to its end and the host reads
+// VMC_DEV_TIMEOUT from the status word.
 __device__ __forceinline__ void tc_wait() {
   const uint32_t bar = smem_addr_u32(&g_tc_mbar), parity = g_tc_phase;
-  uint32_t done = 0;
-  for (long long it = 0; it < (1LL << 26) && !done; ++it) {
+  uint32_t done = (*reinterpret_cast<volatile int32_t*>(g_tc_status) & 2) ? 1u : 0u;
+  for (int it = 0; it < (1 << 22) && !done; ++it) {
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)

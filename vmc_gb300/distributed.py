@@ -2,9 +2,14 @@
 
 Chains are independent (the reference vmaps them, src/vmc/core/sampling.py:38),
 so each rank samples its own shard with no collective on the data path.  The
-only exchange is in the SR solve: per derivative call one all-reduce of
-[sum E, sum O, O^H O] (ParameterSpace) or an all-gather of the O rows
-(SampleSpace), after which every rank solves the same FP64 system.
+only exchange is in the SR solve.  ``TDVPDriver(process_group=...)`` gathers the
+shards' sample histories along the chain axis (``gather_chain_axis``), so every
+rank holds the single-process arrays in the single-process order and solves the
+same FP64 system: one all-gather of N x P_sliced values per derivative call,
+against P_full^2 for an all-reduce of S (at 8x8, D=4: 4096 x 10,816 FP32
+against 21,632^2 FP64).  ``parameter_space_qgt`` (one all-reduce of
+[sum O, O^H O]) and ``gather_jacobian`` remain for callers that hold only the
+sliced Jacobian of their shard.
 """
 from __future__ import annotations
 
@@ -13,7 +18,8 @@ import torch.distributed as dist
 
 from .qgt import SlicedJacobian, iter_sliced_blocks
 
-__all__ = ["shard_chains", "global_energy", "parameter_space_qgt", "gather_jacobian"]
+__all__ = ["shard_chains", "global_energy", "parameter_space_qgt", "gather_jacobian", "gather_chain_axis",
+           "group_rank_size"]
 
 
 def shard_chains(n_chains: int, world_size: int, rank: int):
@@ -26,6 +32,31 @@ def shard_chains(n_chains: int, world_size: int, rank: int):
 
 def _ready(group):
     return dist.is_available() and dist.is_initialized() and dist.get_world_size(group) > 1
+
+
+def group_rank_size(group):
+    """(rank, world size) of this process in `group` ((0, 1) without an initialised process group)."""
+    if not (dist.is_available() and dist.is_initialized()):
+        return 0, 1
+    return dist.get_rank(group), dist.get_world_size(group)
+
+
+def gather_chain_axis(x: torch.Tensor, n_chains: int, group=None) -> torch.Tensor:
+    """All-gather of per-rank histories x (steps, count_r, ...) over contiguous chain shards
+    (``shard_chains``) into (steps, n_chains, ...), chains in global order."""
+    if not _ready(group):
+        return x
+    ws = dist.get_world_size(group)
+    counts = [shard_chains(n_chains, ws, r)[1] for r in range(ws)]
+    cplx = x.is_complex()
+    xr = torch.view_as_real(x) if cplx else x
+    m = max(counts)
+    pad = xr.new_zeros((xr.shape[0], m) + tuple(xr.shape[2:]))
+    pad[:, :xr.shape[1]] = xr
+    bufs = [torch.empty_like(pad) for _ in range(ws)]
+    dist.all_gather(bufs, pad, group=group)
+    out = torch.cat([b[:, :c] for b, c in zip(bufs, counts)], dim=1)
+    return torch.view_as_complex(out.contiguous()) if cplx else out
 
 
 def global_energy(e_local: torch.Tensor, group=None):

@@ -5,6 +5,13 @@ State is the list-of-lists of site tensors; the derivative is the SR update
 computed from one engine sampling run (init_cache + n_steps fused sweeps).
 Real-time evolution (grad factor -i) needs complex parameters: it runs on a
 complex PEPS and raises NotImplementedError for a real one.
+
+With ``process_group`` (one process per GPU, e.g. ``torch.distributed.group.WORLD``)
+the chains are sharded contiguously across the group's ranks (``shard_chains``):
+each rank sweeps its shard, drawing the same uniform stream as one process would
+and keeping its rows; the step's histories are all-gathered along the chain axis,
+and every rank runs the same SR solve on the single-process arrays, so the
+parameters stay identical on all ranks and equal to a one-process run's.
 """
 from __future__ import annotations
 
@@ -13,6 +20,7 @@ import math
 
 import torch
 
+from . import distributed as _dist
 from .kernels import build_mc_kernels
 from .preconditioners import SRPreconditioner
 from .sampling import _sample_counts, _trim_samples, make_mc_sampler
@@ -108,9 +116,13 @@ class TDVPDriver:
 
     def __init__(self, model, operator, *, preconditioner: SRPreconditioner, dt: float, t0: float = 0.0,
                  time_unit: TimeUnit = RealTimeUnit(), integrator: Integrator | None = None, sampler_key=0,
-                 n_samples: int = 1, n_chains: int = 1, full_gradient: bool = False):
+                 n_samples: int = 1, n_chains: int = 1, full_gradient: bool = False, process_group=None):
         if isinstance(time_unit.grad_factor, complex) and not getattr(model, "is_complex", False):
             raise NotImplementedError("real-time TDVP needs complex parameters: use a complex PEPS")
+        self._group = process_group
+        self._rank, self._world = _dist.group_rank_size(process_group) if process_group is not None else (0, 1)
+        if self._world > 1 and hasattr(model, "gi_config_states"):
+            raise NotImplementedError("chain sharding runs standard PEPS; a gauge-invariant PEPS runs on one rank")
         self._model = model
         self.operator = operator
         self.preconditioner = preconditioner
@@ -131,18 +143,66 @@ class TDVPDriver:
         else:
             self._sampler_configuration = torch.randint(0, model.phys_dim, (self.n_chains,) + model.shape,
                                                         generator=self._gen, device=dev, dtype=torch.int32)
+        # this rank's chains [start, start + count); the whole range on one process
+        self._shard = _dist.shard_chains(self.n_chains, self._world, self._rank)
+        if self._world > 1:
+            start, count = self._shard
+            self._sampler_configuration = self._sampler_configuration[start:start + count].clone()
         init_cache, transition, estimate = build_mc_kernels(model, operator, full_gradient=self.full_gradient)
         self._init_cache = init_cache
+        self._transition, self._estimate = transition, estimate
         self._mc_sampler = make_mc_sampler(transition, estimate)
         self.residual_error = None
         self.diag_shift_error = None
         self.solve_time = None
         self._loss_stats = None
 
+    def _sharded_sampling(self, tensors, configs, gen, chain_length):
+        """This rank's sweeps over its chain shard with the uniforms (and flip offsets) one process
+        would draw for those chains; the histories gathered over the group along the chain axis."""
+        start, count = self._shard
+        n_sites = configs.shape[-1]
+        dev = self._model.device
+        d = self._model.phys_dim
+        cache = self._init_cache(tensors, configs)
+        hist_cfg, ests = [], []
+        for _ in range(chain_length):
+            # the draws of kernels.transition with a generator key, for all chains; this rank's rows kept
+            u = torch.rand((self.n_chains, n_sites), generator=gen, dtype=torch.float64, device=dev)
+            deltas = None
+            if d > 2:
+                deltas = torch.randint(1, d, (self.n_chains, n_sites), generator=gen, device=dev,
+                                       dtype=torch.int32)[start:start + count].contiguous()
+            configs, _, ctx = self._transition(tensors, configs, u[start:start + count].contiguous(), cache,
+                                               deltas=deltas)
+            cache, est = self._estimate(tensors, configs, ctx)
+            hist_cfg.append(configs.clone())
+            ests.append(est)
+
+        def gathered(field):
+            if getattr(ests[0], field) is None:
+                return None
+            return _dist.gather_chain_axis(torch.stack([getattr(e, field) for e in ests]), self.n_chains,
+                                           self._group)
+
+        hist = _dist.gather_chain_axis(torch.stack(hist_cfg), self.n_chains, self._group)
+        return configs, hist, gathered("local_log_derivatives"), gathered("local_estimate"), \
+            gathered("active_slice_indices")
+
     def _time_derivative(self, tensors, t, carry):
         """tdvp.py:113-163."""
         gen, configs = carry
         _, num_chains, chain_length, total = _sample_counts(self.n_samples, self.n_chains)
+        if self._world > 1:
+            configs, hist, o_h, e_h, p_h = self._sharded_sampling(tensors, configs, gen, chain_length)
+            samples = _trim_samples(hist, total, self.n_samples)
+            o = _trim_samples(o_h, total, self.n_samples)
+            e = _trim_samples(e_h, total, self.n_samples)
+            p = None if self.full_gradient else _trim_samples(p_h, total, self.n_samples)
+            self._model.tensors = tensors
+            updates, metrics = self.preconditioner.apply(self._model, tensors, samples, o, p, e,
+                                                         grad_factor=self.time_unit.grad_factor)
+            return updates, (gen, configs), (e, metrics)
         cache = self._init_cache(tensors, configs)
         (configs, _, _), (hist, est) = self._mc_sampler(tensors, configs.reshape(num_chains, -1), gen, cache,
                                                           n_steps=chain_length)
@@ -163,7 +223,7 @@ class TDVPDriver:
         eps = 1e-12 * max(1.0, abs(duration), abs(self.dt))
         assert abs(duration - n_steps * self.dt) <= eps, f"T={duration} must be an integer multiple of dt={self.dt}"
         assert n_steps > 0
-        carry = (self._gen, self._sampler_configuration.reshape(self.n_chains, -1))
+        carry = (self._gen, self._sampler_configuration.reshape(self._shard[1], -1))
         e = None
         metrics = {}
         for _ in range(n_steps):
