@@ -442,6 +442,24 @@ size_t vmc_qr_pivoted_workspace_size(int n);
 vmc_status vmc_qr_pivoted(void* stream, int complex_elements, double* a, int64_t lda, int m, int n, int nrhs,
                           double* tau, int32_t* jpvt, void* workspace, size_t workspace_bytes);
 
+/*
+ * The sample-space Gram matrix of a real sliced Jacobian in FP64, the matrix
+ * the SampleSpace SR solve factorises before its centring terms
+ * (src/vmc/qgt/qgt.py:173-223 sums it over the expanded slice blocks,
+ * sum_k (O o [p == k]) (O o [p == k])^T; src/vmc/qgt/jacobian.py:56-93):
+ *     out[i n + j] = sum_c [p[i ld + c] == p[j ld + c]] o[i ld + c] o[j ld + c]
+ *   o: n x ncols FP32 log-derivatives (the engine's out_O, sliced layout);
+ *   p: n x ncols active slice indices (the engine's out_p); both row-major
+ *      with row stride ld >= ncols elements;
+ *   out: n x n FP64, row-major; every entry is written (the matrix is
+ *      symmetric).
+ * The products are exact (FP32 inputs) and are summed in double-float on the
+ * FP32 units, flushed into FP64 every 256 columns.  One kernel on `stream`;
+ * allocates nothing.
+ */
+vmc_status vmc_sliced_gram(void* stream, const float* o, const int8_t* p, int n, int ncols, int64_t ld,
+                           double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,9 +1,11 @@
-"""FP64 factorisations of the SR solve on the GPU.
+"""FP64 factorisations and Gram matrices of the SR solve on the GPU.
 
 ``qr_pivoted`` is the column-pivoted QR of src/vmc/preconditioners/preconditioners.py:178-180
 (``jax.lax.linalg.qr(o_centered, full_matrices=False, pivoting=True)``, LAPACK/MAGMA xGEQP3),
-run by the engine library's ``vmc_qr_pivoted`` kernels in FP64 or complex128.  Nothing here
-computes on the CPU: without the CUDA library and a GPU it raises ``EngineUnavailable``.
+run by the engine library's ``vmc_qr_pivoted`` kernels in FP64 or complex128.  ``sliced_gram``
+is the sample-space Gram matrix of a real sliced Jacobian (``vmc_sliced_gram``), the FP64 matrix
+of the SampleSpace solve (src/vmc/qgt/qgt.py:173-223).  Nothing here computes on the CPU: without
+the CUDA library and a GPU it raises ``EngineUnavailable``.
 """
 from __future__ import annotations
 
@@ -14,7 +16,7 @@ import torch
 from . import _abi
 from ._lib import EngineUnavailable
 
-__all__ = ["qr_pivoted"]
+__all__ = ["qr_pivoted", "sliced_gram"]
 
 
 def _resolve_lib(lib, device):
@@ -25,6 +27,23 @@ def _resolve_lib(lib, device):
     from ._lib import lib as _load
 
     return _load()
+
+
+def sliced_gram(o: torch.Tensor, p: torch.Tensor, lib=None) -> torch.Tensor:
+    """T[i, j] = sum_c [p[i, c] == p[j, c]] o[i, c] o[j, c] in FP64 for FP32 o and int8 p of shape
+    (n, ncols): the sum over slices k of (o masked to slice k) (o masked to slice k)^T."""
+    if o.dim() != 2 or p.shape != o.shape or o.dtype != torch.float32 or p.dtype != torch.int8:
+        raise ValueError("sliced_gram takes FP32 o and int8 p of the same (n, ncols) shape")
+    lib = _resolve_lib(lib, o.device)
+    o = o.contiguous()
+    p = p.contiguous()
+    n, ncols = o.shape
+    out = torch.empty((n, n), dtype=torch.float64, device=o.device)
+    stream = ct.c_void_p(torch.cuda.current_stream(o.device).cuda_stream) if o.device.type == "cuda" else None
+    st = lib.vmc_sliced_gram(stream, ct.c_void_p(o.data_ptr()), ct.c_void_p(p.data_ptr()), n, ncols,
+                             max(ncols, 1), ct.c_void_p(out.data_ptr()))
+    _abi.check(lib, st, "vmc_sliced_gram")
+    return out
 
 
 def qr_pivoted(a: torch.Tensor, rhs: torch.Tensor | None = None, lib=None):

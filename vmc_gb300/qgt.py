@@ -7,7 +7,9 @@ Jacobian stores, per sample, only the active slice of each site; slice k of
 the expanded Jacobian is where(p == k, o, 0) (jacobian.py:56-93).
 
 The dense builds accumulate over column blocks (``n_blocks`` slices of the
-parameter axis) so the FP64 working set stays bounded.
+parameter axis) so the FP64 working set stays bounded.  The SampleSpace Gram of
+a real sliced Jacobian on the GPU is the engine's ``vmc_sliced_gram`` kernel
+(the masked product of the sliced rows, without the expanded blocks' zero half).
 """
 from __future__ import annotations
 
@@ -104,19 +106,43 @@ def jacobian_mean(jac) -> torch.Tensor:
     return torch.cat([b.mean(dim=0) for b in iter_sliced_blocks(jac)])
 
 
+def sliced_centring(jac: SlicedJacobian):
+    """(w, |mean|^2) of a real sliced Jacobian without the expanded blocks: the mean of expanded
+    column (k, c) is sum_i o_ic [p_ic == k] / n, and row i of the expanded O meets it only in its own
+    slice, so w_i = (O_exp mean)_i = sum_c o_ic mean[p_ic, c]."""
+    o64 = _f64(jac.o)
+    n = o64.shape[0]
+    pl = jac.p.long()
+    mean = torch.zeros((jac.phys_dim, o64.shape[1]), dtype=torch.float64, device=o64.device)
+    mean.scatter_add_(0, pl, o64)
+    mean /= n
+    return (o64 * mean.gather(0, pl)).sum(dim=1), (mean * mean).sum()
+
+
+def _kernel_gram(jac) -> bool:
+    return (isinstance(jac, SlicedJacobian) and jac.o.device.type == "cuda" and jac.o.dtype == torch.float32
+            and jac.p.dtype == torch.int8)
+
+
 def _sample_space_dense(jac, n_blocks):
     src = jac.O if isinstance(jac, Jacobian) else jac.o
     n, dev = src.shape[0], src.device
     dt = torch.complex128 if src.is_complex() else torch.float64
-    G = torch.zeros((n, n), dtype=dt, device=dev)
-    w = torch.zeros(n, dtype=dt, device=dev)
-    msq = torch.zeros((), dtype=torch.float64, device=dev)
-    blocks = [_f64(jac.O)] if isinstance(jac, Jacobian) else iter_sliced_blocks(jac, n_blocks)
-    for ob in blocks:
-        G += ob @ ob.conj().T
-        mb = ob.mean(dim=0)
-        w += ob @ mb.conj()
-        msq += torch.vdot(mb, mb).real
+    if _kernel_gram(jac):
+        from .linalg import sliced_gram
+
+        G = sliced_gram(jac.o, jac.p)
+        w, msq = sliced_centring(jac)
+    else:
+        G = torch.zeros((n, n), dtype=dt, device=dev)
+        w = torch.zeros(n, dtype=dt, device=dev)
+        msq = torch.zeros((), dtype=torch.float64, device=dev)
+        blocks = [_f64(jac.O)] if isinstance(jac, Jacobian) else iter_sliced_blocks(jac, n_blocks)
+        for ob in blocks:
+            G += ob @ ob.conj().T
+            mb = ob.mean(dim=0)
+            w += ob @ mb.conj()
+            msq += torch.vdot(mb, mb).real
     G /= n
     ones = torch.ones(n, dtype=dt, device=dev)
     G -= (w[:, None] * ones[None, :]) / n
