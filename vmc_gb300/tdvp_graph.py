@@ -236,3 +236,9 @@ class GraphTDVPDriver:
         self._counter.fill_(int(state["counter"]))
         self._loss_stats = None if state["loss_stats"] is None else EnergyStats(state["loss_stats"])
         self._model.tensors = self._model.unpack(self._theta.clone())
+
+    def save(self, path) -> None:
+        torch.save(self.state_dict(), path)
+
+    def load(self, path) -> None:
+        self.load_state_dict(torch.load(path, map_location="cpu", weights_only=True))
