@@ -338,13 +338,13 @@ def e2e_public_api(w, n, rank, dev, ustream, args, barrier, options=None):
     return n * args.steps / elapsed, h2d, d2h
 
 
-def shipped_options(w):
-    """The launch configuration the shipped GB300 autotune table holds for this workload, or None (the
-    engine's default) when the table has no entry for it."""
+def shipped_options(w, precision="fp32"):
+    """The launch configuration the shipped GB300 autotune table holds for this workload and precision,
+    or None (the engine's default) when the table has no entry for it."""
     from vmc_gb300 import autotune
 
     return autotune.shipped_options(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype,
-                                    operator=w.operator())
+                                    operator=w.operator(), precision=precision)
 
 
 def unfused_rate(eng, tens, cfg, args, barrier):
@@ -442,9 +442,9 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(dev)
     n_sites = w.shape[0] * w.shape[1]
     prec = precision_of(args, w)
-    # the shipped launch table holds FP32 choices; the mixed tier runs its own defaults
+    # the shipped launch table holds each tier's own choice (the engine's defaults where it has none)
     fp32_options = shipped_options(w)
-    options = fp32_options if prec == "fp32" else {"precision": "mixed"}
+    options = fp32_options if prec == "fp32" else dict(shipped_options(w, "mixed") or {}, precision="mixed")
     eng = PEPSEngine(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, operator=w.operator(), device=dev,
                      dtype=w.dtype, options=options)
     tens = torch.from_numpy(pack_tensors(w.tensors(seed=0))).to(dev)

@@ -60,6 +60,23 @@ def test_tune_and_cache(emu_lib, tmp_path, monkeypatch):
     assert eng.options == CANDIDATES[5]
 
 
+def test_mixed_tier_is_tuned_under_its_own_key(emu_lib, tmp_path, monkeypatch):
+    from vmc_gb300.autotune import MIXED_CANDIDATES
+
+    monkeypatch.setenv("VMC_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    entry = tune((3, 3), 2, 4, lib=emu_lib, candidates=MIXED_CANDIDATES[:2], precision="mixed")
+    data = json.loads((tmp_path / "tune.json").read_text())
+    (key,) = data
+    assert key.endswith("|mixed") and data[key]["options"] == entry["options"]
+    data[key]["options"] = MIXED_CANDIDATES[3]
+    (tmp_path / "tune.json").write_text(json.dumps(data))
+    eng = PEPSEngine((3, 3), 2, 4, device="cpu", lib=emu_lib, options="auto", precision="mixed")
+    assert eng.options == dict(MIXED_CANDIDATES[3], precision="mixed")
+    # the FP32 entry of the same problem is a different key: tuning it leaves the mixed one alone
+    tune((3, 3), 2, 4, lib=emu_lib, candidates=CANDIDATES[:1])
+    assert len(json.loads((tmp_path / "tune.json").read_text())) == 2
+
+
 def test_shipped_table_is_the_fallback(emu_lib, tmp_path, monkeypatch):
     import vmc_gb300.autotune as at
 
@@ -77,14 +94,17 @@ def test_shipped_table_entries_are_valid_candidates(emu_lib):
     valid plan configuration (vmc_peps_plan_ex accepts it)."""
     from vmc_gb300.autotune import SHIPPED
 
+    from vmc_gb300.autotune import MIXED_CANDIDATES
+
     table = json.loads(SHIPPED.read_text())
     assert table
     shape = _abi.VmcShape(3, 3)
     for key, entry in table.items():
-        assert entry["options"] in CANDIDATES, key
+        mixed = key.endswith("|mixed")
+        assert entry["options"] in (MIXED_CANDIDATES if mixed else CANDIDATES), key
         assert entry["samples_per_s"] == max(c["samples_per_s"] for c in entry["candidates"]), key
         for cand in entry["candidates"]:
-            o = _abi.plan_options(cand["options"])
+            o = _abi.plan_options(dict(cand["options"], precision="mixed" if mixed else "fp32"))
             plan = ct.c_void_p()
             assert emu_lib.vmc_peps_plan_ex(ct.byref(shape), 2, 4, 2, 0, 1, 2, ct.byref(o), ct.byref(plan)) == \
                 _abi.VMC_OK, (key, cand)

@@ -22,7 +22,7 @@ from pathlib import Path
 import numpy as np
 import torch
 
-__all__ = ["CANDIDATES", "cache_path", "shipped_options", "tune", "tuned_options"]
+__all__ = ["CANDIDATES", "MIXED_CANDIDATES", "cache_path", "shipped_options", "tune", "tuned_options"]
 
 # (threads, smem_kb, tile_policy); smem_kb -1 = the 52 KB default, 0 = all buffers in the slot
 CANDIDATES = [
@@ -40,6 +40,21 @@ CANDIDATES = [
     {"threads": 256, "smem_kb": -1, "tile_policy": 3},
     {"threads": 128, "smem_kb": -1, "tile_policy": 4},
     {"threads": 256, "smem_kb": -1, "tile_policy": 4},
+]
+
+# the mixed-precision tier (FFMA tiles and the Gram eigensolver only); its FP64 arena is twice the FP32
+# one, smem_kb -1 = its 52 KB default (the eigensolver's working set at 8x8 D4), up to 200 KB
+MIXED_CANDIDATES = [
+    {"threads": 128, "smem_kb": -1, "tile_policy": 0},
+    {"threads": 128, "smem_kb": 0, "tile_policy": 0},
+    {"threads": 128, "smem_kb": 110, "tile_policy": 0},
+    {"threads": 128, "smem_kb": 200, "tile_policy": 0},
+    {"threads": 128, "smem_kb": -1, "tile_policy": 1},
+    {"threads": 128, "smem_kb": -1, "tile_policy": 2},
+    {"threads": 256, "smem_kb": -1, "tile_policy": 0},
+    {"threads": 256, "smem_kb": 110, "tile_policy": 0},
+    {"threads": 64, "smem_kb": -1, "tile_policy": 0},
+    {"threads": 64, "smem_kb": 0, "tile_policy": 0},
 ]
 
 _LOCK = threading.Lock()
@@ -103,13 +118,13 @@ def _store(key: str, entry: dict) -> None:
 
 
 def _time_candidate(options, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator, device, lib,
-                    waves, reps, seed=0, n_chains=None):
+                    waves, reps, seed=0, n_chains=None, precision="fp32"):
     from .engine import PEPSEngine
     from .lowering import pack_tensors
     from .synthetic import initial_configs, random_tensors
 
     eng = PEPSEngine(shape, bond_dim, chi, phys_dim, strategy, n_sweeps, operator=operator, device=device,
-                     lib=lib, dtype=dtype, options=options)
+                     lib=lib, dtype=dtype, options=options, precision=precision)
     n = int(n_chains) if n_chains else max(1, waves * eng.resident_chains)
     n_sites = shape[0] * shape[1]
     T = random_tensors(shape, bond_dim, phys_dim=phys_dim, seed=seed,
@@ -145,8 +160,10 @@ def _time_candidate(options, shape, bond_dim, chi, phys_dim, strategy, n_sweeps,
 
 
 def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32", operator=None,
-         device=None, lib=None, candidates=None, waves=1, reps=1, store=True, n_chains=None) -> dict:
+         device=None, lib=None, candidates=None, waves=1, reps=1, store=True, n_chains=None,
+         precision="fp32") -> dict:
     """Time every candidate on this problem; returns {"options", "samples_per_s", "candidates"}.
+    ``precision``: "fp32" or "mixed" (the candidates default to ``MIXED_CANDIDATES`` for the latter).
     ``n_chains``: chains per timed sweep (the run's own count); None times ``waves`` full waves of each
     candidate's resident chains.  One wave favours configurations whose extra resident chains only pay
     off within a wave, so a table meant for a given run size is best tuned at that size."""
@@ -158,40 +175,41 @@ def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="
         raise ValueError("tuning a d != 2 plan needs its operator")
     op = operator if operator is not None else heisenberg(shape)
     results = []
-    for cand in candidates or CANDIDATES:
+    for cand in candidates or (MIXED_CANDIDATES if precision == "mixed" else CANDIDATES):
         rate = _time_candidate(cand, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op, device, lib,
-                               waves, reps, n_chains=n_chains)
+                               waves, reps, n_chains=n_chains, precision=precision)
         results.append({"options": dict(cand), "samples_per_s": rate})
     best = max(results, key=lambda r: r["samples_per_s"])
     entry = {"options": best["options"], "samples_per_s": best["samples_per_s"], "candidates": results}
     if store:
         with _LOCK:
-            _store(_key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op), entry)
+            _store(_key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op, precision), entry)
     return entry
 
 
 def shipped_options(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32",
-                    device=None, operator=None):
+                    device=None, operator=None, precision="fp32"):
     """The winner the shipped table holds for this problem on this GPU, or None (no tuning, no local cache)."""
     device = torch.device(device if device is not None else "cuda")
     hit = _load(SHIPPED).get(_key(device, (int(shape[0]), int(shape[1])), bond_dim, chi, phys_dim, strategy, n_sweeps,
-                                  dtype, operator))
+                                  dtype, operator, precision))
     return dict(hit["options"]) if hit else None
 
 
 def tuned_options(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="float32", operator=None,
-                  device=None, lib=None) -> dict:
+                  device=None, lib=None, precision="fp32") -> dict:
     """The cached winner for this problem on this GPU, tuning it first when it is not cached."""
     shape = (int(shape[0]), int(shape[1]))
     device = torch.device(device if device is not None else ("cuda" if lib is None else "cpu"))
-    key = _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator)
+    key = _key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator, precision)
     with _LOCK:
         hit = _load().get(key)
         if hit is None:
             hit = _load(SHIPPED).get(key)
     if hit is not None:
         return dict(hit["options"])
-    return dict(tune(shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator, device, lib)["options"])
+    return dict(tune(shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, operator, device, lib,
+                     precision=precision)["options"])
 
 
 def main(argv=None) -> None:
@@ -205,6 +223,7 @@ def main(argv=None) -> None:
                                                        "heis8x8_D5_chi25", "tfim10x10_D4_chi16_c64",
                                                        "heis12x12_D6_chi36", "heis16x16_D6_chi48"])
     ap.add_argument("--out", default=str(SHIPPED))
+    ap.add_argument("--precision", choices=["fp32", "mixed"], default="fp32")
     ap.add_argument("--chains", type=int, default=-1,
                     help="chains per timed sweep: -1 the workload's own count when one sweep of it stays under "
                          "about 20 s, else one wave; 0 one wave; N > 0 exactly N")
@@ -218,9 +237,10 @@ def main(argv=None) -> None:
             # about 2.4 TFLOP/s of algorithmic work is what one GB300 sustains on these plans
             n = w.n_chains if (w.flops_per_sample() or 0) * w.n_chains < 20 * 2.4e12 else 0
         entry = tune(w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype, w.operator(), dev, store=False,
-                     n_chains=n or None)
+                     n_chains=n or None, precision=args.precision)
         entry["chains"] = n or "one wave"
-        table[_key(dev, w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype, w.operator())] = entry
+        table[_key(dev, w.shape, w.bond_dim, w.chi, w.phys_dim, w.strategy, 2, w.dtype, w.operator(),
+                   args.precision)] = entry
         print(json.dumps({"workload": name, **entry}), flush=True)
         Path(args.out).write_text(json.dumps(table, indent=1, sort_keys=True))
 

@@ -85,15 +85,13 @@ class PEPSEngine:
         if isinstance(options, str):
             if options != "auto":
                 raise ValueError("options must be None, a dict or 'auto'")
-        if options == "auto" and precision in ("mixed", _abi.VMC_PRECISION_MIXED):
-            # the tuned table holds FP32 launch configurations; the mixed tier runs its defaults
-            options = {}
         if isinstance(options, str):
             from .autotune import tuned_options
 
+            prec = "mixed" if precision in ("mixed", _abi.VMC_PRECISION_MIXED) else "fp32"
             options = tuned_options(self.shape, self.bond_dim, self.chi, self.phys_dim, strategy, n_sweeps,
                                     "complex64" if self.complex else "float32", operator=operator,
-                                    device=self.device, lib=lib)
+                                    device=self.device, lib=lib, precision=prec)
         if precision is not None:
             options = dict(options or {})
             options["precision"] = precision
