@@ -23,7 +23,7 @@ inline float __fsub_rn(float a, float b) { return a - b; }
 inline float __fmul_rn(float a, float b) { return a * b; }
 #endif
 
-struct df64 {
+struct __align__(8) df64 {
   float hi, lo;
   df64() = default;
   __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
@@ -31,6 +31,8 @@ struct df64 {
   __device__ __forceinline__ df64(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
   __device__ __forceinline__ explicit df64(int i) : hi((float)i), lo(0.f) {}
   __device__ __forceinline__ double to_double() const { return (double)hi + (double)lo; }
+  // nearest FP32 value (|lo| <= ulp(hi) / 2)
+  __device__ __forceinline__ float to_float() const { return __fadd_rn(hi, lo); }
 };
 
 __device__ __forceinline__ df64 df_fast_two_sum(float a, float b) {

@@ -722,6 +722,38 @@ __device__ inline void cta_tridiagonalize_df(double* G, int n, int ldg, const Ei
   __syncthreads();
 }
 
+// Top-k eigenvectors of a symmetric n x n matrix held in df64: the Householder tridiagonalisation and
+// the back-transform run in df64 on the FP32 units; the eigenvalues (FP32 brackets refined by Newton's
+// method) and inverse iteration run in FP64 on T, whose d and e are converted in place.  The reflectors
+// stay in A and tau in df64; Y (n x k, row stride ldy) is computed as FP64 by the tridiagonal solver and
+// converted to df64 in place (a df64 takes the 8 bytes of a double).
+__device__ inline void cta_sym_topk_df(df64* A, int n, int lda, int k, df64* Y, int ldy,
+                                       const EigScratchT<double>& w, double* red) {
+  VMC_TSTART(t0);
+  df64* d = reinterpret_cast<df64*>(w.d);
+  df64* e = reinterpret_cast<df64*>(w.e);
+  df64* tau = reinterpret_cast<df64*>(w.tau);
+  cta_tridiagonalize(A, n, lda, d, e, tau, reinterpret_cast<df64*>(w.v), reinterpret_cast<df64*>(w.p),
+                     reinterpret_cast<df64*>(w.part));
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    w.d[i] = d[i].to_double();
+    w.e[i] = e[i].to_double();
+  }
+  __syncthreads();
+  VMC_TSTOP(t0, PH_TRIDIAG);
+  double* Yd = reinterpret_cast<double*>(Y);
+  tri_topk_vectors(n, k, Yd, ldy, w, red);
+  for (int el = threadIdx.x; el < n * k; el += blockDim.x) {
+    const size_t o = (size_t)(el / k) * ldy + el % k;
+    Y[o] = df64(Yd[o]);
+  }
+  __syncthreads();
+  VMC_TSTART(t4);
+  cta_back_transform(static_cast<const df64*>(A), n, lda, static_cast<const df64*>(tau), Y, k, ldy,
+                     reinterpret_cast<df64*>(w.cvec));
+  VMC_TSTOP(t4, PH_BACK);
+}
+
 template <typename T>
 __device__ inline void cta_sym_topk(T* G, int n, int ldg, int k, T* Y, int ldy, const EigScratchT<T>& w,
                                     double* red) {
