@@ -71,26 +71,6 @@ __device__ __forceinline__ void df_ld(const float* p, float& h, float& l) {
   l = 0.f;
 }
 
-// (sh, sl) += (ah + al)(bh + bl); AL / BL: whether A / B carry a low part
-template <bool AL, bool BL>
-__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
-  const float p = __fmul_rn(ah, bh);
-  float e = fmaf(ah, bh, -p);
-  if (BL) e = fmaf(ah, bl, e);
-  if (AL) e = fmaf(al, bh, e);
-  const float s = __fadd_rn(sh, p);
-  const float bb = __fsub_rn(s, sh);
-  const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-  sl = __fadd_rn(sl, __fadd_rn(t, e));
-  sh = s;
-}
-
-__device__ __forceinline__ void df_renorm(float& sh, float& sl) {
-  const float s = __fadd_rn(sh, sl);
-  sl = __fsub_rn(sl, __fsub_rn(s, sh));
-  sh = s;
-}
-
 template <typename TA, typename TB, int TM, int TN>
 __device__ __forceinline__ void gemm_tiles_d(const GemmD<TA, TB>& g) {
   constexpr bool AL = std::is_same<TA, df64>::value, BL = std::is_same<TB, df64>::value;

@@ -70,6 +70,45 @@ __device__ __forceinline__ bool operator==(df64 a, df64 b) { return a.hi == b.hi
 __device__ __forceinline__ bool operator!=(df64 a, df64 b) { return !(a == b); }
 
 __device__ __forceinline__ df64 vfma(df64 a, df64 b, df64 c) { return a * b + c; }
+
+// Accumulation without renormalising at every step (GEMM-style inner loops):
+// (sh, sl) += (ah + al)(bh + bl) as the error-free product fl(ah bh) + its fmaf
+// residual + the cross terms (lo * lo dropped, ~2^-47 relative), added by
+// Knuth's two-sum; sl grows by at most ~2^-24 |sh| per step until df_renorm.
+// AL / BL: whether a / b carry a low part.
+template <bool AL, bool BL>
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  float e = fmaf(ah, bh, -p);
+  if (BL) e = fmaf(ah, bl, e);
+  if (AL) e = fmaf(al, bh, e);
+  const float s = __fadd_rn(sh, p);
+  const float bb = __fsub_rn(s, sh);
+  const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  sl = __fadd_rn(sl, __fadd_rn(t, e));
+  sh = s;
+}
+
+__device__ __forceinline__ void df_renorm(float& sh, float& sl) {
+  const float s = __fadd_rn(sh, sl);
+  sl = __fsub_rn(sl, __fsub_rn(s, sh));
+  sh = s;
+}
+
+// s += a b without the final renormalisation (call df_norm before using s)
+__device__ __forceinline__ void acc_mac(df64& s, df64 a, df64 b) { df_mac<true, true>(s.hi, s.lo, a.hi, a.lo, b.hi, b.lo); }
+__device__ __forceinline__ df64 df_norm(df64 s) {
+  df_renorm(s.hi, s.lo);
+  return s;
+}
+// a - x1 y1 - x2 y2 with one renormalisation
+__device__ __forceinline__ df64 df_sub2(df64 a, df64 x1, df64 y1, df64 x2, df64 y2) {
+  float sh = a.hi, sl = a.lo;
+  df_mac<true, true>(sh, sl, -x1.hi, -x1.lo, y1.hi, y1.lo);
+  df_mac<true, true>(sh, sl, -x2.hi, -x2.lo, y2.hi, y2.lo);
+  df_renorm(sh, sl);
+  return df64(sh, sl);
+}
 __device__ __forceinline__ df64 vsqrt(df64 a) { return df64(sqrt(a.to_double())); }
 __device__ __forceinline__ df64 vabs(df64 a) { return a.hi < 0.f ? -a : a; }
 __device__ __forceinline__ bool df_sign(float x) {

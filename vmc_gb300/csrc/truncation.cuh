@@ -47,6 +47,7 @@ __device__ __forceinline__ void warp_sync() {
 template <typename T>
 __device__ inline void cta_tridiagonalize(T* A, int n, int lda, T* d, T* e, T* tau, T* v,
                                           T* p, T* part) {
+  constexpr bool kDF = std::is_same<T, df64>::value;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = (nt + 31) >> 5;
   if (n == 1) {
@@ -84,7 +85,8 @@ __device__ inline void cta_tridiagonalize(T* A, int n, int lda, T* d, T* e, T* t
       scal = T(1.) / (alpha - beta);
     }
     // column j stays unscaled until barrier (2): the matrix-vector product
-    // below rebuilds v from it, so v needs no barrier of its own
+    // below rebuilds v from it, so v needs no barrier of its own (df64: a
+    // product per element costs more than the barrier, so v is read back)
     const T* colj = A + (size_t)(j + 1) * lda + j;
     for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? T(1.) : colj[(size_t)i * lda] * scal;
     if (tid == 0) {
@@ -102,8 +104,32 @@ __device__ inline void cta_tridiagonalize(T* A, int n, int lda, T* d, T* e, T* t
       __syncthreads();
       continue;
     }
+    if constexpr (kDF) __syncthreads();  // v visible
     // p = tau * A_sub v, rg threads per row; partial p.v per warp
     T pv = T(0.);
+    if constexpr (kDF) {
+      for (int i = rrow; i < m; i += nrow_thr) {
+        const T* row = As + (size_t)i * lda;
+        T s0 = T(0.), s1 = T(0.), s2 = T(0.), s3 = T(0.);
+        int l = rlane;
+        for (; l + 3 * rg < m; l += 4 * rg) {
+          acc_mac(s0, row[l], v[l]);
+          acc_mac(s1, row[l + rg], v[l + rg]);
+          acc_mac(s2, row[l + 2 * rg], v[l + 2 * rg]);
+          acc_mac(s3, row[l + 3 * rg], v[l + 3 * rg]);
+        }
+        for (; l < m; l += rg) acc_mac(s0, row[l], v[l]);
+        T s = (df_norm(s0) + df_norm(s1)) + (df_norm(s2) + df_norm(s3));
+#ifndef VMC_HOST_EMULATION
+        for (int o = rg / 2; o > 0; o >>= 1) s += shfl_xor_t(rmask, s, o, rg);
+#endif
+        const T pi = tj * s;
+        if (rlane == 0) {
+          p[i] = pi;
+          pv = vfma(pi, v[i], pv);
+        }
+      }
+    } else {
     for (int i = rrow; i < m; i += nrow_thr) {
       const T* row = As + (size_t)i * lda;
       T s0 = T(0.), s1 = T(0.), s2 = T(0.), s3 = T(0.);
@@ -129,6 +155,7 @@ __device__ inline void cta_tridiagonalize(T* A, int n, int lda, T* d, T* e, T* t
         p[i] = pi;
         pv = vfma(pi, i == 0 ? T(1.) : colj[(size_t)i * lda] * scal, pv);
       }
+    }
     }
     pv = warp_sum_t(pv);
     if (lane == 0) part[32 + warp] = pv;
@@ -160,7 +187,11 @@ __device__ inline void cta_tridiagonalize(T* A, int n, int lda, T* d, T* e, T* t
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           if (q < nl) {
-            const T nv = a[q] - vi * wl[q] - wi * vl[q];
+            T nv;
+            if constexpr (kDF)
+              nv = df_sub2(a[q], vi, wl[q], wi, vl[q]);
+            else
+              nv = a[q] - vi * wl[q] - wi * vl[q];
             arow[l0 + q * gx] = nv;
             if (l0 + q * gx == 0 && i >= 2) s = vfma(nv, nv, s);
           }
@@ -465,9 +496,20 @@ __device__ inline void cta_back_transform(const T* A, int n, int lda, const T* t
         const T y = Y[(size_t)row * ldy + t];
         const T vb = (i == 0) ? T(1.) : A[(size_t)row * lda + (j - 1)];
         const T va = (i == 0) ? T(0.) : ((i == 1) ? T(1.) : A[(size_t)row * lda + j]);
-        a = vfma(va, y, a);
-        b = vfma(vb, y, b);
-        sg = vfma(va, vb, sg);
+        if constexpr (std::is_same<T, df64>::value) {
+          acc_mac(a, va, y);
+          acc_mac(b, vb, y);
+          acc_mac(sg, va, vb);
+        } else {
+          a = vfma(va, y, a);
+          b = vfma(vb, y, b);
+          sg = vfma(va, vb, sg);
+        }
+      }
+      if constexpr (std::is_same<T, df64>::value) {
+        a = df_norm(a);
+        b = df_norm(b);
+        sg = df_norm(sg);
       }
 #ifndef VMC_HOST_EMULATION
       for (int o = g / 2; o > 0; o >>= 1) {
@@ -488,7 +530,11 @@ __device__ inline void cta_back_transform(const T* A, int n, int lda, const T* t
       const T vb = (i == 0) ? T(1.) : A[(size_t)row * lda + (j - 1)];
       const T va = (i == 0) ? T(0.) : ((i == 1) ? T(1.) : A[(size_t)row * lda + j]);
       T* yrow = Y + (size_t)row * ldy;
-      for (int t = ux; t < k; t += gx) yrow[t] -= va * cvec[t] + vb * cv2[t];
+      if constexpr (std::is_same<T, df64>::value) {
+        for (int t = ux; t < k; t += gx) yrow[t] = df_sub2(yrow[t], va, cvec[t], vb, cv2[t]);
+      } else {
+        for (int t = ux; t < k; t += gx) yrow[t] -= va * cvec[t] + vb * cv2[t];
+      }
     }
     __syncthreads();
   }
