@@ -428,13 +428,19 @@ __device__ inline bool cta_cholqr(T* Y, int n, int k, int ldy, T* S, int* flag) 
   }
   __syncthreads();
   if (*flag) return false;
+  // FP64: R's diagonal replaced by its reciprocals (k divisions instead of n k)
+  constexpr bool kRecip = std::is_same<T, double>::value;
+  if constexpr (kRecip) {
+    for (int t = tid; t < k; t += blockDim.x) S[t * k + t] = T(1.) / S[t * k + t];
+    __syncthreads();
+  }
   // Y <- Y R^-1, one row per thread
   for (int i = tid; i < n; i += blockDim.x) {
     T* y = Y + (size_t)i * ldy;
     for (int t = 0; t < k; ++t) {
       T v = y[t];
       for (int s = 0; s < t; ++s) v -= y[s] * S[s * k + t];
-      y[t] = v / S[t * k + t];
+      y[t] = kRecip ? v * S[t * k + t] : v / S[t * k + t];
     }
   }
   __syncthreads();
