@@ -411,7 +411,7 @@ NCU_DRAM_BYTES_PER_SAMPLE = {("heis8x8_D4_chi16", "fp32"): (3.451871e9 + 7.28318
 
 
 def precision_of(args, w):
-    """The headline tier: the mixed-precision engine (FP64 boundary-MPS chain) where it exists -- real
+    """The headline tier: the mixed-precision engine (boundary-MPS chain in double-float) where it exists -- real
     ZipUp / NoTruncation workloads -- since only it meets the accuracy bars; FP32 elsewhere."""
     if args.precision != "auto":
         return args.precision
@@ -518,7 +518,7 @@ def run_ours(args, rank, world, local_rank):
             if eng32 is not None:
                 accuracy["fp32"] = accuracy_vs_oracle(eng32, w, ref, dev)
             accuracy["bars"] = {"e_mean_vs_scale": 1e-5, "o_frob_rel": 1e-4}
-    # the kernel runs on the CUDA cores (the mixed tier's chain also on the FP64 units): the fraction of
+    # the kernel runs on the CUDA cores (the mixed tier's eigenvalues also on the FP64 units): the fraction of
     # the nominal FP32 FMA peak, at the SM clock sampled during the run (SMs x 128 lanes x 2 x clock)
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
@@ -534,7 +534,7 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": w.name, "shape": list(w.shape), "bond_dim": w.bond_dim, "chi": w.chi,
                    "phys_dim": w.phys_dim, "strategy": f"{w.strategy}({w.chi})", "model": w.model,
                    "chains_per_gpu": n, "global_chains": n * world, "parallelism": f"replicas x{world}",
-                   "precision": prec + (" (FP64 boundary-MPS chain, FP32 contractions)" if prec == "mixed" else ""),
+                   "precision": prec + (" (boundary-MPS chain in double-float with FP64 eigenvalues, FP32 elsewhere)" if prec == "mixed" else ""),
                    "launch_options": options or "engine default",
                    "l2": "inputs larger than L2 (bottom-env cache "
                          f"{eng.cache_bytes(n) / 1e9:.2f} GB read+written per step)"},
@@ -826,7 +826,7 @@ def main():
     ap.add_argument("--gi-ref-chains-per-core", type=int, default=1,
                     help="GI workload: oracle chains per host core per step (reference arm and cpu_baseline)")
     ap.add_argument("--precision", choices=["auto", "mixed", "fp32"], default="auto",
-                    help="engine tier of the headline: auto = mixed (FP64 boundary-MPS chain) where it exists")
+                    help="engine tier of the headline: auto = mixed (double-float boundary-MPS chain) where it exists")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 leg beside a mixed headline")
     ap.add_argument("--accuracy-chains", type=int, default=64,
                     help="chains of the CPU-baseline sample whose FP64 results check both tiers")

@@ -94,13 +94,15 @@ enum {
   /* every contraction, truncation and stored tensor in FP32 */
   VMC_PRECISION_FP32 = 0,
   /* the boundary-MPS chain -- zip-up theta, its truncation and the stored
-   * boundary tensors that feed the next row's zip -- in FP64; environments,
-   * Metropolis ratios, gradients and energies in FP32.  Real ZipUp and
-   * NoTruncation plans.  Truncated amplitudes are ill-conditioned (the kept
-   * subspace moves by the relative perturbation of theta divided by the
-   * relative singular-value gap at the cut), so FP32 storage on the chain
-   * alone puts the batch-mean energy ~1e-4 off the FP64 result at 8x8, D=4,
-   * chi=16; this tier brings it to ~1e-7. */
+   * boundary tensors that feed the next row's zip -- in double-float (pairs
+   * of FP32 values, ~48 significant bits, on the FP32 units; the
+   * eigenvalues' refinement and inverse iteration in FP64); environments,
+   * Metropolis ratios, gradients and energies in FP32.  Real ZipUp,
+   * DensityMatrix and NoTruncation plans.  Truncated amplitudes are
+   * ill-conditioned (the kept subspace moves by the relative error of the
+   * decomposition divided by the relative singular-value gap at the cut), so
+   * an FP32 truncation puts the batch-mean energy ~6e-5 of the energy scale
+   * off the FP64 result at 8x8, D=4, chi=16; this tier brings it to ~1e-7. */
   VMC_PRECISION_MIXED = 1
 };
 

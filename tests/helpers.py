@@ -100,7 +100,7 @@ def assert_parity(rel_errors, truncating, median_tol=TRUNC_MEDIAN_TOL, max_tol=T
 # error by the cancellation.  "O" is the Frobenius norm over the batch.
 E_BAR = 1e-5
 O_BAR = 1e-4
-# FP64 chain: the amplitude is the FP64 contraction of FP64 boundary tensors
+# mixed tier: the amplitude is the FP64 contraction of double-float boundary tensors
 MIXED_AMP_TOL = 1e-9
 
 

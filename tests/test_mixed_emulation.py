@@ -1,4 +1,4 @@
-"""The mixed-precision tier (FP64 boundary-MPS chain, FP32 elsewhere) in the host-emulation build
+"""The mixed-precision tier (boundary-MPS chain in double-float, FP32 elsewhere) in the host-emulation build
 against the FP64 oracle: amplitudes at the FP64 level, energies and log-derivatives at the FP32
 level, and at 8x8, D=4, chi=16 the accuracy bars (batch-mean E within 1e-5 of the energy scale,
 O_k within 1e-4 Frobenius over the batch) that the FP32 tier misses."""
@@ -75,7 +75,7 @@ def test_mixed_amp_grad_and_local_energy_match_oracle(emu_lib):
 
 
 def test_config2_mixed_meets_the_accuracy_bar_where_fp32_does_not(emu_lib):
-    """8x8 Heisenberg, D=4, chi=16, ZipUp(16), 6 chains: the FP64 chain takes the amplitudes to the
+    """8x8 Heisenberg, D=4, chi=16, ZipUp(16), 6 chains: the double-float chain takes the amplitudes to the
     FP64 level and the batch-mean E and O_k inside the bars; the FP32 tier's truncations move them by
     eps_fp32 / (relative gap) and miss both."""
     shape, D, chi = (8, 8), 4, 16

@@ -1123,7 +1123,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, int chain, float* s
   Slot S = make_slot(P, slot_base);
   if (threadIdx.x == 0) g_tile_policy = P.tile_policy;  // read by cta_gemm after the next barrier
 #if VMC_CHAIN_F64
-  // the FP64 chain's arena takes the place of the FP32 truncation arena
+  // the high-precision chain's arena (8-byte df64 elements) takes the place of the FP32 truncation arena
   const ChainD ch = make_chain_d(P, S.h64, reinterpret_cast<double*>(P.arena_in_smem ? dyn_smem : S.arena),
                                  reinterpret_cast<double*>(S.arena));
 #else

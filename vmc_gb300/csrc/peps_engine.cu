@@ -267,7 +267,8 @@ static vmc_status create_plan(const vmc_shape* shape, int bond_dim, int chi, int
        (opts->threads != 0 && opts->threads < 128)))
     return VMC_ERR_UNSUPPORTED;
   const int precision = opts ? opts->precision : VMC_PRECISION_FP32;
-  // the FP64 chain exists for real ZipUp / NoTruncation plans with the Gram eigensolver and FFMA tiles
+  // the high-precision chain exists for real ZipUp / NoTruncation / DensityMatrix plans with the Gram
+  // eigensolver and FFMA tiles
   if (precision == VMC_PRECISION_MIXED &&
       (dtype != VMC_DTYPE_F32 || gi_N > 0 || strategy == VMC_STRATEGY_VARIATIONAL || opts->trunc_method != 0 ||
        opts->tile_policy >= 3))

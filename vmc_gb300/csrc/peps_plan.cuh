@@ -52,7 +52,7 @@ struct DevPlan {
   int TS, ES, E2S, SCR, MM;  // buffer sizes (floats)
   int nmax, kmax;         // largest truncation matrix side / kept bond
   int trunc_method;       // 0: Gram + tridiagonal eigensolver, 1: one-sided Jacobi
-  int chain64;            // mixed precision: the boundary-MPS chain in FP64 (chain_f64.cuh), the rest FP32
+  int chain64;            // mixed precision: the boundary-MPS chain in double-float (chain_f64.cuh), the rest FP32
   int arena_in_smem;      // truncation arena in dynamic shared memory
   int mat_in_smem;        // theta matrix inside the arena (else in a separate global slot region)
   int threads;            // CTA size of the fused kernel
@@ -112,7 +112,7 @@ struct Slot {
   float* l2[2];  // E2S
   float* arena;  // truncation arena when it does not fit shared memory
   float* venv;   // Variational: left envs C*VS, then right envs C*VS
-  double* h64;   // mixed precision: the FP64 boundary-MPS chain (chain_f64_doubles doubles), else null
+  double* h64;   // mixed precision: the df64 boundary-MPS chain (chain_f64_doubles 8-byte elements), else null
   float* scr[11 + 2 * kMaxPhys + 5];  // n_scr = 11 + 2 kMaxPhys buffers (GI plans use the first 12)
 };
 
@@ -172,7 +172,7 @@ __host__ __device__ inline long long arena_doubles(int nmax, int kmax) {
 __host__ __device__ inline long long arena_split_doubles(int nmax, int kmax) {
   return al32((long long)nmax * (nmax | 1)) + al32(4LL * kmax * nmax);
 }
-// Doubles of the FP64 chain buffers in a slot (make_chain_d): two boundary
+// 8-byte elements of the df64 chain buffers in a slot (make_chain_d): two boundary
 // rows, two carries and the Z1 intermediate.  The FP64 arena takes the place
 // of the FP32 one (shared memory or the slot's arena region).
 __host__ __device__ inline long long chain_f64_doubles(int C, long long TS, long long SCR) {
@@ -232,7 +232,7 @@ struct KernelSet {
 namespace rk { const KernelSet& kernels(); }  // real FP32 elements
 namespace rt { const KernelSet& kernels(); }  // real FP32 elements, tensor-core GEMMs (tile_policy 3)
 namespace rq { const KernelSet& kernels(); }  // real FP32 elements, tcgen05 GEMMs (tile_policy 4)
-namespace rm { const KernelSet& kernels(); }  // real, mixed precision: FP64 boundary-MPS chain
+namespace rm { const KernelSet& kernels(); }  // real, mixed precision: df64 boundary-MPS chain
 namespace ck { const KernelSet& kernels(); }  // complex64 elements
 namespace gr { const KernelSet& kernels(); }  // gauge-invariant plans, real FP32
 namespace gc { const KernelSet& kernels(); }  // gauge-invariant plans, complex64

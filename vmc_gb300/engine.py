@@ -58,7 +58,7 @@ class PEPSEngine:
         smem_kb / tile_policy / precision / trunc_method / vchunk / vert_smem (vmc_plan_options), or
         "auto" for the autotuned choice of this (lattice, D, chi, dtype, strategy, precision) from
         vmc_gb300.autotune.  ``precision``: "fp32" (default) or "mixed" -- the boundary-MPS chain in
-        FP64, everything else FP32 (overrides the options' precision)."""
+        double-float (FP64 eigenvalues), everything else FP32 (overrides the options' precision)."""
         self.shape = (int(shape[0]), int(shape[1]))
         self.complex = str(dtype).replace("torch.", "") in ("complex64", "complex128")
         # dtypes of this engine's parameters / O_k and of E_loc
