@@ -462,6 +462,21 @@ vmc_status vmc_qr_pivoted(void* stream, int complex_elements, double* a, int64_t
 vmc_status vmc_sliced_gram(void* stream, const float* o, const int8_t* p, int n, int ncols, int64_t ld,
                            double* out);
 
+/*
+ * The parameter-space Gram matrix of the same sliced Jacobian, O_exp^T O_exp,
+ * in FP64: the matrix of the ParameterSpace SR solve before its centring term
+ * (src/vmc/qgt/qgt.py:173-223 on the expanded blocks in slice order,
+ * jacobian.py:21-33):
+ *     out[(k ncols + c) W + (k' ncols + c')] =
+ *         sum_i [p[i ld + c] == k][p[i ld + c'] == k'] o[i ld + c] o[i ld + c']
+ * with W = d ncols; o, p as for vmc_sliced_gram; out: W x W FP64 row-major,
+ * every entry written.  d = 2 slices (VMC_ERR_UNSUPPORTED otherwise).  Exact
+ * products summed in double-float, flushed into FP64 every 256 samples.  One
+ * kernel on `stream`; allocates nothing.
+ */
+vmc_status vmc_sliced_gram_params(void* stream, const float* o, const int8_t* p, int n, int ncols, int64_t ld,
+                                  int d, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,3 +39,34 @@ def test_sample_space_dense_uses_the_kernel_and_agrees(cuda_device):
     oc = dense - dense.mean(0)
     ref = oc @ oc.T / 300
     assert float(torch.linalg.norm(T - ref) / torch.linalg.norm(ref)) < 1e-12
+
+
+@pytest.mark.parametrize("n,ncols", [(700, 300), (64, 31), (1, 5), (33, 64)])
+def test_sliced_gram_params_matches_fp64_expanded_product(cuda_device, n, ncols):
+    from vmc_gb300.linalg import sliced_gram_params
+
+    g = torch.Generator(device=cuda_device)
+    g.manual_seed(n + 7 * ncols)
+    o = torch.randn((n, ncols), generator=g, device=cuda_device, dtype=torch.float32)
+    p = torch.randint(0, 2, (n, ncols), generator=g, device=cuda_device, dtype=torch.int8)
+    S = sliced_gram_params(o, p)
+    jac = gq.SlicedJacobian(o, p, (2,) * ncols)
+    E = torch.cat(list(gq.iter_sliced_blocks(jac)), dim=1)
+    ref = E.T @ E
+    assert torch.equal(S, S.T)
+    scale = torch.sqrt(torch.outer(torch.diagonal(ref), torch.diagonal(ref))).clamp_min(1e-300)
+    assert float(((S - ref).abs() / scale).max()) < 1e-12
+    assert float(torch.linalg.norm(S - ref) / torch.linalg.norm(ref)) < 1e-13
+
+
+def test_parameter_space_dense_uses_the_kernel_and_agrees(cuda_device):
+    g = torch.Generator(device=cuda_device)
+    g.manual_seed(5)
+    o = torch.randn((300, 200), generator=g, device=cuda_device, dtype=torch.float32)
+    p = torch.randint(0, 2, (300, 200), generator=g, device=cuda_device, dtype=torch.int8)
+    jac = gq.SlicedJacobian(o, p, (2,) * 200)
+    S = gq.QGT(jac, gq.ParameterSpace()).to_dense()
+    E = torch.cat(list(gq.iter_sliced_blocks(jac)), dim=1)
+    m = E.mean(0)
+    ref = E.T @ E / 300 - m[:, None] * m[None, :]
+    assert float(torch.linalg.norm(S - ref) / torch.linalg.norm(ref)) < 1e-12

@@ -69,3 +69,39 @@ def test_sliced_centring_equals_the_block_terms(d):
         msq_ref += mb @ mb
     assert torch.allclose(w, w_ref, rtol=1e-12, atol=1e-14)
     assert torch.allclose(msq, msq_ref, rtol=1e-12)
+
+
+def _expanded_params(o, p, d):
+    o = o.astype(np.float64)
+    E = np.concatenate([np.where(p == k, o, 0.0) for k in range(d)], axis=1)
+    return E.T @ E
+
+
+@pytest.mark.parametrize("n,ncols,ld", [(37, 45, None), (5, 33, 40), (1, 1, None)])
+def test_sliced_gram_params_equals_the_expanded_product(emu_lib, n, ncols, ld):
+    rng = np.random.default_rng(n * ncols)
+    o = rng.standard_normal((n, ncols)).astype(np.float32)
+    p = rng.integers(0, 2, (n, ncols)).astype(np.int8)
+    ld = ncols if ld is None else ld
+    ob = np.zeros((n, ld), np.float32)
+    pb = np.zeros((n, ld), np.int8)
+    ob[:, :ncols] = o
+    pb[:, :ncols] = p
+    out = np.full((2 * ncols, 2 * ncols), np.nan)
+    st = emu_lib.vmc_sliced_gram_params(None, ob.ctypes.data_as(ct.c_void_p), pb.ctypes.data_as(ct.c_void_p), n,
+                                        ncols, ld, 2, out.ctypes.data_as(ct.c_void_p))
+    assert st == _abi.VMC_OK
+    assert np.allclose(out, _expanded_params(o, p, 2), rtol=1e-12, atol=1e-12)
+
+
+def test_sliced_gram_params_rejects_bad_arguments(emu_lib):
+    o = np.zeros((4, 8), np.float32)
+    p = np.zeros((4, 8), np.int8)
+    out = np.zeros((16, 16))
+    args = (o.ctypes.data_as(ct.c_void_p), p.ctypes.data_as(ct.c_void_p))
+    assert emu_lib.vmc_sliced_gram_params(None, *args, 4, 8, 8, 3, out.ctypes.data_as(ct.c_void_p)) == \
+        _abi.VMC_ERR_UNSUPPORTED
+    assert emu_lib.vmc_sliced_gram_params(None, *args, 4, 8, 7, 2, out.ctypes.data_as(ct.c_void_p)) == \
+        _abi.VMC_ERR_INVALID
+    assert emu_lib.vmc_sliced_gram_params(None, None, None, 4, 8, 8, 2, None) == _abi.VMC_ERR_INVALID
+    assert emu_lib.vmc_sliced_gram_params(None, None, None, 0, 0, 1, 2, None) == _abi.VMC_OK

@@ -110,6 +110,7 @@ SIGNATURES = {
     "vmc_qr_pivoted_workspace_size": (_SZ, [_I]),
     "vmc_qr_pivoted": (_I, [_P, _I, _P, ct.c_int64, _I, _I, _I, _P, _P, _P, _SZ]),
     "vmc_sliced_gram": (_I, [_P, _P, _P, _I, _I, ct.c_int64, _P]),
+    "vmc_sliced_gram_params": (_I, [_P, _P, _P, _I, _I, ct.c_int64, _I, _P]),
 }
 
 

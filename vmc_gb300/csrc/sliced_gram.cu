@@ -1,6 +1,8 @@
-// sliced_gram.cu -- the sample-space Gram matrix of a sliced Jacobian, the FP64
-// matrix the SampleSpace SR solve factorises (qgt.py:173-223 builds it from the
-// expanded blocks, sum_k (O o [p == k]) (O o [p == k])^H; jacobian.py:56-93).
+// sliced_gram.cu -- the Gram matrices of a sliced Jacobian in FP64: the
+// sample-space T the SampleSpace SR solve factorises (qgt.py:173-223 builds it
+// from the expanded blocks, sum_k (O o [p == k]) (O o [p == k])^H;
+// jacobian.py:56-93), and the parameter-space O_exp^T O_exp of the
+// ParameterSpace solve (second kernel below).
 //
 // For real FP32 log-derivatives o (n samples x ncols sliced columns) and the
 // active slice p of every (sample, column):
@@ -130,6 +132,113 @@ __global__ void __launch_bounds__(kThreads) sliced_gram_kernel(const float* __re
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// ParameterSpace: S[(k, c), (k', c')] = sum_i [p_ic == k][p_ic' == k'] o_ic o_ic', the Gram matrix of
+// the expanded Jacobian's columns in slice order (column k * ncols + c), for d == 2 slices.  Each
+// sample's product o_ic o_ic' belongs to exactly one of the d^2 = 4 slice pairs, so a thread keeps four
+// df64 accumulators per column pair and adds the exact product to the one its slice pair selects
+// (selects, one two-sum).  32 x 32 column-pair tiles on and below the diagonal, 256 threads with 2 x 2
+// pairs each, 32-sample slabs staged in shared memory; FP64 flushes every 256 samples.
+// ---------------------------------------------------------------------------
+constexpr int kPTile = 32;
+
+__global__ void __launch_bounds__(kThreads) sliced_gram_params_kernel(const float* __restrict__ o,
+                                                                       const int8_t* __restrict__ p, int n,
+                                                                       int ncols, long long ld,
+                                                                       double* __restrict__ out) {
+  __shared__ __align__(16) float sa[kSlab][kPTile];
+  __shared__ __align__(16) float sb[kSlab][kPTile];
+  __shared__ __align__(16) int8_t qa[kSlab][kPTile];
+  __shared__ __align__(16) int8_t qb[kSlab][kPTile];
+  int I, J;
+  tile_of(blockIdx.x, I, J);
+  const int c0 = I * kPTile, d0 = J * kPTile;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  float hi[4][2][2], lo[4][2][2];
+  double acc[4][2][2];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) hi[q][r][c] = lo[q][r][c] = 0.f, acc[q][r][c] = 0.0;
+  const int n_slabs = (n + kSlab - 1) / kSlab;
+  for (int sl = 0; sl < n_slabs; ++sl) {
+    const int i0 = sl * kSlab;
+    // stage: 32 samples x 32 columns of each block, consecutive threads on consecutive columns
+    for (int e = tid; e < kSlab * kPTile; e += kThreads) {
+      const int ii = e / kPTile, cc = e % kPTile, gi = i0 + ii;
+      const int ga = c0 + cc, gb = d0 + cc;
+      const bool ka = gi < n && ga < ncols, kb = gi < n && gb < ncols;
+      sa[ii][cc] = ka ? o[(size_t)gi * ld + ga] : 0.f;
+      qa[ii][cc] = ka ? p[(size_t)gi * ld + ga] : (int8_t)0;
+      sb[ii][cc] = kb ? o[(size_t)gi * ld + gb] : 0.f;
+      qb[ii][cc] = kb ? p[(size_t)gi * ld + gb] : (int8_t)0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ii = 0; ii < kSlab; ++ii) {
+      const float2 a2 = *reinterpret_cast<const float2*>(&sa[ii][ty * 2]);
+      const float2 b2 = *reinterpret_cast<const float2*>(&sb[ii][tx * 2]);
+      const float a[2] = {a2.x, a2.y}, b[2] = {b2.x, b2.y};
+      const int pa[2] = {qa[ii][ty * 2] & 1, qa[ii][ty * 2 + 1] & 1};
+      const int pb[2] = {qb[ii][tx * 2] & 1, qb[ii][tx * 2 + 1] & 1};
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const float prod = __fmul_rn(a[r], b[c]);
+          const float err = fmaf(a[r], b[c], -prod);
+          const int q = 2 * pa[r] + pb[c];
+          const float th = q == 0 ? hi[0][r][c] : q == 1 ? hi[1][r][c] : q == 2 ? hi[2][r][c] : hi[3][r][c];
+          const float tl = q == 0 ? lo[0][r][c] : q == 1 ? lo[1][r][c] : q == 2 ? lo[2][r][c] : lo[3][r][c];
+          float sum, t;
+          two_sum(th, prod, sum, t);
+          const float nl = __fadd_rn(tl, __fadd_rn(t, err));
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            hi[k][r][c] = q == k ? sum : hi[k][r][c];
+            lo[k][r][c] = q == k ? nl : lo[k][r][c];
+          }
+        }
+    }
+    __syncthreads();
+    const bool flush = (sl + 1) % kFlushSlabs == 0 || sl + 1 == n_slabs;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          if (flush) {
+            acc[q][r][c] += (double)hi[q][r][c] + (double)lo[q][r][c];
+            hi[q][r][c] = lo[q][r][c] = 0.f;
+          } else {
+            const float sum = __fadd_rn(hi[q][r][c], lo[q][r][c]);
+            lo[q][r][c] = __fsub_rn(lo[q][r][c], __fsub_rn(sum, hi[q][r][c]));
+            hi[q][r][c] = sum;
+          }
+        }
+  }
+  const size_t W = 2 * (size_t)ncols;
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int cc = c0 + ty * 2 + r;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int dd = d0 + tx * 2 + c;
+      if (cc < ncols && dd < ncols) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const size_t row = (size_t)(q >> 1) * ncols + cc, col = (size_t)(q & 1) * ncols + dd;
+          out[row * W + col] = acc[q][r][c];
+          if (I != J) out[col * W + row] = acc[q][r][c];
+        }
+      }
+    }
+  }
+}
 #endif
 
 }  // namespace gram
@@ -158,6 +267,37 @@ vmc_status vmc_sliced_gram(void* stream, const float* o, const int8_t* p, int n,
   const long long blocks = tiles * (tiles + 1) / 2;
   if (blocks > 0x7fffffffLL) return VMC_ERR_UNSUPPORTED;
   VMC_LAUNCH(sliced_gram_kernel, (unsigned)blocks, kThreads, 0, stream, o, p, n, ncols, (long long)ld, out);
+  return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
+#endif
+}
+
+vmc_status vmc_sliced_gram_params(void* stream, const float* o, const int8_t* p, int n, int ncols, int64_t ld,
+                                  int d, double* out) {
+  if (n < 0 || ncols < 0 || ld < (ncols > 1 ? ncols : 1) || ((long long)n * ncols > 0 && (!o || !p)) ||
+      (ncols > 0 && !out))
+    return VMC_ERR_INVALID;
+  if (d != 2) return VMC_ERR_UNSUPPORTED;
+  if (ncols == 0) return VMC_OK;
+  using namespace vmc::gram;
+#ifdef VMC_HOST_EMULATION
+  (void)stream;
+  const size_t W = (size_t)d * ncols;
+  for (size_t e = 0; e < W * W; ++e) out[e] = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < ncols; ++c) {
+      const double a = o[(size_t)i * ld + c];
+      const size_t row = (size_t)p[(size_t)i * ld + c] * ncols + c;
+      for (int c2 = 0; c2 < ncols; ++c2)
+        out[row * W + (size_t)p[(size_t)i * ld + c2] * ncols + c2] += a * o[(size_t)i * ld + c2];
+    }
+  return VMC_OK;
+#else
+  const long long tiles = (ncols + kPTile - 1) / kPTile;
+  const long long blocks = tiles * (tiles + 1) / 2;
+  if (blocks > 0x7fffffffLL) return VMC_ERR_UNSUPPORTED;
+  if (n == 0) return vmc_memset(out, 0, (size_t)4 * ncols * ncols * sizeof(double), (cudaStream_t)stream) ==
+                             cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
+  VMC_LAUNCH(sliced_gram_params_kernel, (unsigned)blocks, kThreads, 0, stream, o, p, n, ncols, (long long)ld, out);
   return vmc_last_error() == cudaSuccess ? VMC_OK : VMC_ERR_CUDA;
 #endif
 }

@@ -16,7 +16,7 @@ import torch
 from . import _abi
 from ._lib import EngineUnavailable
 
-__all__ = ["qr_pivoted", "sliced_gram"]
+__all__ = ["qr_pivoted", "sliced_gram", "sliced_gram_params"]
 
 
 def _resolve_lib(lib, device):
@@ -43,6 +43,23 @@ def sliced_gram(o: torch.Tensor, p: torch.Tensor, lib=None) -> torch.Tensor:
     st = lib.vmc_sliced_gram(stream, ct.c_void_p(o.data_ptr()), ct.c_void_p(p.data_ptr()), n, ncols,
                              max(ncols, 1), ct.c_void_p(out.data_ptr()))
     _abi.check(lib, st, "vmc_sliced_gram")
+    return out
+
+
+def sliced_gram_params(o: torch.Tensor, p: torch.Tensor, d: int = 2, lib=None) -> torch.Tensor:
+    """S = O_exp^T O_exp in FP64 for FP32 o and int8 p of shape (n, ncols), O_exp the expanded Jacobian in
+    slice order (column k * ncols + c is o[:, c] masked to slice k); d = 2 slices."""
+    if o.dim() != 2 or p.shape != o.shape or o.dtype != torch.float32 or p.dtype != torch.int8:
+        raise ValueError("sliced_gram_params takes FP32 o and int8 p of the same (n, ncols) shape")
+    lib = _resolve_lib(lib, o.device)
+    o = o.contiguous()
+    p = p.contiguous()
+    n, ncols = o.shape
+    out = torch.empty((d * ncols, d * ncols), dtype=torch.float64, device=o.device)
+    stream = ct.c_void_p(torch.cuda.current_stream(o.device).cuda_stream) if o.device.type == "cuda" else None
+    st = lib.vmc_sliced_gram_params(stream, ct.c_void_p(o.data_ptr()), ct.c_void_p(p.data_ptr()), n, ncols,
+                                    max(ncols, 1), int(d), ct.c_void_p(out.data_ptr()))
+    _abi.check(lib, st, "vmc_sliced_gram_params")
     return out
 
 

@@ -3,9 +3,12 @@ against the expanded-block build with cuBLAS FP64 GEMMs (``qgt.iter_sliced_block
 per slice), on synthetic FP32 log-derivatives with the 8x8 Heisenberg D=4 sliced layout by default.
 
     python -m vmc_gb300.profile_gram --n 4096 --ncols 10816 --reps 5
+    python -m vmc_gb300.profile_gram --space parameter --reps 3
 
-The kernel computes n(n+1)/2 x ncols masked products (the lower triangle); the expanded build computes
-n^2 x ncols x d multiply-adds, half of them on zeros.
+SampleSpace: the kernel computes n(n+1)/2 x ncols masked products (the lower triangle); the expanded
+build computes n^2 x ncols x d multiply-adds, half of them on zeros.  ParameterSpace (d = 2): the kernel
+computes about n x ncols^2 / 2 products into the (d ncols)^2 matrix; the expanded build computes
+n x (d ncols)^2 multiply-adds.
 """
 from __future__ import annotations
 
@@ -25,6 +28,7 @@ def main(argv=None) -> None:
     ap.add_argument("--d", type=int, default=2)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--kernel-only", action="store_true", help="skip the cuBLAS build (for profiler captures)")
+    ap.add_argument("--space", choices=["sample", "parameter"], default="sample")
     args = ap.parse_args(argv)
     dev = torch.device("cuda:0")
     g = torch.Generator(device=dev)
@@ -44,6 +48,27 @@ def main(argv=None) -> None:
         torch.cuda.synchronize()
         return out, e0.elapsed_time(e1) / args.reps
 
+    if args.space == "parameter":
+        from .linalg import sliced_gram_params
+
+        S, ms_k = timed(lambda: sliced_gram_params(o, p, args.d))
+        res = {"space": "parameter", "n": args.n, "ncols": args.ncols, "d": args.d, "kernel_ms": round(ms_k, 3),
+               "kernel_products_per_s": args.n * args.ncols * (args.ncols + 32) / 2 / (ms_k * 1e-3)}
+        if not args.kernel_only:
+            del S
+
+            def expanded():
+                E = torch.cat(list(gq.iter_sliced_blocks(jac)), dim=1)
+                return E.T @ E
+
+            G, ms_b = timed(expanded)
+            S = sliced_gram_params(o, p, args.d)
+            res.update({"cublas_expanded_ms": round(ms_b, 3),
+                        "cublas_fp64_tflops": 2.0 * args.n * (args.d * args.ncols) ** 2 / (ms_b * 1e-3) / 1e12,
+                        "speedup": ms_b / ms_k,
+                        "rel_frobenius_diff": float(torch.linalg.norm(S - G) / torch.linalg.norm(G))})
+        print(json.dumps(res))
+        return
     T, ms_k = timed(lambda: sliced_gram(o, p))
     res = {"n": args.n, "ncols": args.ncols, "d": args.d, "kernel_ms": round(ms_k, 3),
            "kernel_products_per_s": args.n * (args.n + 1) / 2 * args.ncols / (ms_k * 1e-3)}

@@ -163,6 +163,19 @@ class QGT:
         """qgt.py:173-223."""
         if isinstance(self.space, SampleSpace):
             return _sample_space_dense(self.jac, self.n_blocks)
+        if (_kernel_gram(self.jac) and isinstance(self.jac.ordering, SliceOrdering) and self.jac.phys_dim == 2):
+            # O_exp^T O_exp from the sliced rows (vmc_sliced_gram_params), less the centring term
+            from .linalg import sliced_gram_params
+
+            n = self.jac.o.shape[0]
+            S = sliced_gram_params(self.jac.o, self.jac.p, 2)
+            S /= n
+            o64 = _f64(self.jac.o)
+            mean = torch.zeros((2, o64.shape[1]), dtype=torch.float64, device=o64.device)
+            mean.scatter_add_(0, self.jac.p.long(), o64)
+            m = (mean / n).reshape(-1)
+            S -= m[:, None] * m[None, :]
+            return S
         O = _dense_O(self.jac)
         m = O.mean(dim=0)
         return (O.conj().T @ O) / O.shape[0] - m.conj()[:, None] * m[None, :]
