@@ -138,3 +138,19 @@ def test_config2_mixed_meets_the_accuracy_bar_on_256_chains(cuda_device):
     assert acc["e_mean_scaled"] < E_BAR, acc
     assert acc["o_frob"] < O_BAR, acc
     assert acc32["o_frob"] > 10 * acc["o_frob"], (acc, acc32)
+
+
+def test_mixed_tier_at_8x8_D5_chi25(cuda_device):
+    """8x8 Heisenberg, D=5, ZipUp(25) (125 x 125 truncations), 16 chains: the double-float chain keeps
+    the amplitudes at ~1e-11 and O_k at ~1e-6; E_loc carries the FP32 energy contractions' rounding,
+    which grows with D (host emulation of the same chains: per sample up to 9e-5)."""
+    shape, D, chi = (8, 8), 5, 25
+    H = hamiltonian("heisenberg", shape)
+    T, cfg, u = make_case(shape, D, 16, seed=7)
+    _, res = _sweep(cuda_device, shape, D, chi, "ZipUp", H, T, cfg, u, MIXED)
+    c2, ctx, le = oracle_sweep(fp32(T), shape, D, "ZipUp", chi, H, cfg, u)
+    acc = accuracy(res, c2, ctx, le)
+    assert acc["same_configs"] >= 0.9, acc
+    assert acc["amp_rel_max"] < MIXED_AMP_TOL * 100, acc
+    assert acc["o_frob"] < 1e-5, acc
+    assert acc["eloc_rel_max"] < 1e-3 and acc["e_mean_scaled"] < 1e-4, acc
