@@ -14,6 +14,7 @@ from oracle import peps as oracle
 from tests.helpers import assert_parity, fp32, hamiltonian, make_case, oracle_sweep
 from vmc_gb300 import _abi
 from vmc_gb300.autotune import CANDIDATES, tune, tuned_options
+from vmc_gb300.operators import transverse_field_ising
 from vmc_gb300.engine import PEPSEngine
 from vmc_gb300.lowering import pack_tensors
 
@@ -136,3 +137,13 @@ def test_the_cache_key_tells_hamiltonians_apart():
     assert kh != kt
     assert kh == autotune._key(dev, (4, 4), 3, 6, 2, "ZipUp", 2, "float32", None)  # default: Heisenberg
     assert kh != autotune._key(dev, (4, 4), 3, 6, 2, "ZipUp", 2, "float32", None, precision="mixed")
+
+
+def test_unsupported_candidates_are_skipped(emu_lib, tmp_path, monkeypatch):
+    """The tcgen05 tile policy exists for real FP32 plans only: tuning a complex plan skips it and says so."""
+    monkeypatch.setenv("VMC_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    cands = [{"threads": 128, "smem_kb": -1, "tile_policy": 0}, {"threads": 128, "smem_kb": -1, "tile_policy": 4}]
+    entry = tune((3, 3), 2, 4, dtype="complex64", operator=transverse_field_ising((3, 3)), lib=emu_lib,
+                 candidates=cands, store=False)
+    assert entry["options"] == cands[0] and entry["unsupported"] == [cands[1]]
+    assert len(entry["candidates"]) == 1

@@ -22,6 +22,8 @@ from pathlib import Path
 import numpy as np
 import torch
 
+from . import _abi
+
 __all__ = ["CANDIDATES", "MIXED_CANDIDATES", "cache_path", "shipped_options", "tune", "tuned_options"]
 
 # (threads, smem_kb, tile_policy); smem_kb -1 = the 52 KB default, 0 = all buffers in the slot
@@ -174,13 +176,25 @@ def tune(shape, bond_dim, chi, phys_dim=2, strategy="ZipUp", n_sweeps=2, dtype="
     if operator is None and phys_dim != 2:
         raise ValueError("tuning a d != 2 plan needs its operator")
     op = operator if operator is not None else heisenberg(shape)
-    results = []
+    results, skipped = [], []
     for cand in candidates or (MIXED_CANDIDATES if precision == "mixed" else CANDIDATES):
-        rate = _time_candidate(cand, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op, device, lib,
-                               waves, reps, n_chains=n_chains, precision=precision)
+        try:
+            rate = _time_candidate(cand, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op, device,
+                                   lib, waves, reps, n_chains=n_chains, precision=precision)
+        except _abi.VmcError as e:
+            # a configuration the plan does not support for this problem (the tcgen05 tiles on complex
+            # elements, say) is not a candidate here
+            if e.status != _abi.VMC_ERR_UNSUPPORTED:
+                raise
+            skipped.append(dict(cand))
+            continue
         results.append({"options": dict(cand), "samples_per_s": rate})
+    if not results:
+        raise ValueError("no launch configuration supports this problem")
     best = max(results, key=lambda r: r["samples_per_s"])
     entry = {"options": best["options"], "samples_per_s": best["samples_per_s"], "candidates": results}
+    if skipped:
+        entry["unsupported"] = skipped
     if store:
         with _LOCK:
             _store(_key(device, shape, bond_dim, chi, phys_dim, strategy, n_sweeps, dtype, op, precision), entry)
