@@ -3,11 +3,20 @@
 // environments, Metropolis, estimate (O_k, E_loc) and the fused persistent
 // kernel.
 //
-// Included twice by peps_engine.cu, once per element type, inside a namespace
-// that defines kCplx (complex elements) and kEs (floats per element: 1 for
-// real FP32, 2 for complex64 stored as interleaved (re, im) floats).  Every
-// buffer size in the DevPlan counts floats; every tensor dimension counts
+// Included by each kernel translation unit (peps_kernels_*.cu) inside a
+// namespace that defines kCplx (complex elements) and kEs (floats per element:
+// 1 for real FP32, 2 for complex64 stored as interleaved (re, im) floats).
+// Every buffer size in the DevPlan counts floats; every tensor dimension counts
 // elements.
+
+// Code a gauge-invariant plan never runs (GI plans refuse DensityMatrix and the VJP mode) is left out of
+// the GI kernel's translation unit, whose register allocation it would otherwise burden.
+#ifdef VMC_GI_TU
+constexpr bool kDensityMatrixCode = false, kVjpCode = false;
+#else
+constexpr bool kDensityMatrixCode = true, kVjpCode = true;
+#endif
+
 // GEMMs on this file's element type.  The conjugating variants are the
 // conj(.) of the reference's complex contractions (no-ops for real elements).
 __device__ inline void gemm(Gemm g) {
@@ -397,7 +406,7 @@ __device__ __noinline__ double apply_row(const DevPlan& P, const Slot& S, Shared
     float* mat = ar.mat;
     gemm(make_gemm(Z1, two(dn, Lb * pin * dn, 1), dn, Ap, lin(1), pout * Rb, mat, two(dn, pout * ldm, Rb),
                        two(Rb, ldm, 1), kc * dn, pout * Rb, Lb * pin));
-    if (P.strategy == VMC_STRATEGY_DENSITY_MATRIX) {
+    if (kDensityMatrixCode && P.strategy == VMC_STRATEGY_DENSITY_MATRIX) {
       // ---- DensityMatrix (strategy.py:153-176): rho = theta^H theta and its top-kout eigenvectors V;
       // the new tensor is theta V (columns not normalised) and the carry V^H.  With every column kept,
       // V = I: rho's eigenbasis is then any unitary, which the carry undoes in the next theta, and the
@@ -840,7 +849,7 @@ __device__ __noinline__ void estimate_row(const DevPlan& P, const Slot& S, Share
         G = elem(Orow, full_gradient ? (size_t)P.d * P.site_osl[s] + (size_t)cur * sz : (size_t)P.site_osl[s]);
       }
       grad_env(Y1, B, Rc, W, G, ba, V, bb, tb, Rb, Lb, U, (float)cs_re, (float)cs_im);
-      if (vjp_grad) {
+      if (kVjpCode && vjp_grad) {
         // vector-Jacobian product: grad[full layout of site s, slice cur] += w * O (FP64), with G this
         // site's O for the chain; the weight stays out of the FP32 G, where a tiny amplitude would underflow
         double* dst = vjp_grad + (size_t)kEs * ((size_t)P.d * P.site_osl[s] + (size_t)cur * sz);
