@@ -126,7 +126,8 @@ def accuracy_vs_oracle(eng, w, ref, dev):
     E_loc (median / max of |dE| / max(1, |E|)), the batch-mean E relative to the energy scale mean|E_loc|
     and relative to |mean E|, O_k (Frobenius over the batch), over the chains whose sampled
     configurations agree (a differing chain had an accept decision within float rounding of its
-    threshold), and the fraction of chains with an accept decision within 1e-4 of its threshold."""
+    threshold), the fraction of chains with an accept decision within 1e-4 of its threshold, and the
+    fraction with a near-degenerate cut (relative eigen-gap below 1e-3)."""
     import numpy as np
     import torch
 
@@ -155,6 +156,8 @@ def accuracy_vs_oracle(eng, w, ref, dev):
             "e_mean_rel": float(abs(e.mean() - e_ref.mean()) / abs(e_ref.mean())),
             "o_frob_rel": float(np.linalg.norm(o - o_ref) / np.linalg.norm(o_ref)),
             "min_gap": float(res.gap.min().item()),
+            # chains with a near-degenerate cut (relative eigen-gap below 1e-3 at some truncation)
+            "near_degenerate": float((res.gap.cpu().numpy() < 1e-3).mean()),
             # chains with an accept decision within 1e-4 of its threshold (|min(1, ratio) - u|)
             "near_threshold": float((res.margin.cpu().numpy() < 1e-4).mean()) if res.margin is not None else None}
 
