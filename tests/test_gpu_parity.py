@@ -13,8 +13,8 @@ import pytest
 import torch
 
 from oracle import peps as oracle
-from tests.helpers import (CONFIG2_MAX_TOL, CONFIG2_MEDIAN_TOL, TRUNC_MAX_TOL, TRUNC_MEDIAN_TOL, assert_parity,
-                           accuracy, complex_tensors, fp32, hamiltonian, make_case, oracle_sweep)
+from tests.helpers import (CONFIG2_MAX_TOL, CONFIG2_MEDIAN_TOL, E_BAR, O_BAR, TRUNC_MAX_TOL, TRUNC_MEDIAN_TOL,
+                           assert_parity, accuracy, complex_tensors, fp32, hamiltonian, make_case, oracle_sweep)
 from vmc_gb300.engine import PEPSEngine
 from vmc_gb300.lowering import pack_tensors
 
@@ -103,8 +103,9 @@ def test_config2_heisenberg_8x8_D4_chi16_subset(cuda_device):
 
 def test_config2_variational_8x8_D4_chi16(cuda_device):
     """8x8 Heisenberg, D=4, Variational(16) with 2 sweeps, 64 chains against the oracle.  The QR/ALS
-    compression has no eigen-gap amplification: the host emulation of the same kernel gives a median
-    amplitude error of 8e-6 and a batch-mean E_loc error of 1.6e-5 of the energy scale."""
+    compression has no eigen-gap amplification, so the FP32 tier meets the accuracy bars here (measured
+    on sm_103a: batch-mean E 1.1e-6 of the energy scale, O_k 2.5e-5; on 256 other chains 3.6e-6 and
+    5.9e-5)."""
     shape, D, chi = (8, 8), 4, 16
     H = hamiltonian("heisenberg", shape)
     T, cfg, u = make_case(shape, D, 64, seed=0)
@@ -113,8 +114,8 @@ def test_config2_variational_8x8_D4_chi16(cuda_device):
     acc = accuracy(res, c2, ctx, le)
     assert acc["same_configs"] >= 0.9, acc
     assert acc["amp_rel_median"] < 1e-4 and acc["amp_rel_max"] < 1e-2, acc
-    assert acc["e_mean_scaled"] < 1e-4 and acc["eloc_rel_max"] < 1e-2, acc
-    assert acc["o_frob"] < 1e-3, acc
+    assert acc["e_mean_scaled"] < E_BAR and acc["eloc_rel_max"] < 1e-2, acc
+    assert acc["o_frob"] < O_BAR, acc
 
 
 def test_amp_grad_and_local_energy_match_oracle(cuda_device):
