@@ -70,3 +70,19 @@ def test_parameter_space_dense_uses_the_kernel_and_agrees(cuda_device):
     m = E.mean(0)
     ref = E.T @ E / 300 - m[:, None] * m[None, :]
     assert float(torch.linalg.norm(S - ref) / torch.linalg.norm(ref)) < 1e-12
+
+
+def test_parameter_space_dense_site_ordering_uses_the_kernel(cuda_device):
+    g = torch.Generator(device=cuda_device)
+    g.manual_seed(9)
+    pps = (40, 70, 25, 65)
+    ncols = sum(pps)
+    o = torch.randn((257, ncols), generator=g, device=cuda_device, dtype=torch.float32)
+    p = torch.randint(0, 2, (257, ncols), generator=g, device=cuda_device, dtype=torch.int8)
+    jac = gq.SlicedJacobian(o, p, (2,) * len(pps), gq.SiteOrdering(pps))
+    assert gq._kernel_gram(jac) and gq._site_from_slice_order(jac) is not None
+    S = gq.QGT(jac, gq.ParameterSpace()).to_dense()
+    E = torch.cat(list(gq.iter_sliced_blocks(jac)), dim=1)
+    m = E.mean(0)
+    ref = E.T @ E / 257 - m[:, None] * m[None, :]
+    assert float(torch.linalg.norm(S - ref) / torch.linalg.norm(ref)) < 1e-12

@@ -105,3 +105,21 @@ def test_sliced_gram_params_rejects_bad_arguments(emu_lib):
         _abi.VMC_ERR_INVALID
     assert emu_lib.vmc_sliced_gram_params(None, None, None, 4, 8, 8, 2, None) == _abi.VMC_ERR_INVALID
     assert emu_lib.vmc_sliced_gram_params(None, None, None, 0, 0, 1, 2, None) == _abi.VMC_OK
+
+
+def test_site_order_is_the_slice_order_permuted():
+    """The ParameterSpace S of a site-ordered sliced Jacobian (jacobian.py:36-46) is the slice-ordered S
+    with rows and columns permuted by qgt._site_from_slice_order (how the GPU path reuses its kernel)."""
+    rng = np.random.default_rng(3)
+    pps = (3, 5, 2, 4)
+    ncols = sum(pps)
+    o = torch.from_numpy(rng.standard_normal((9, ncols)).astype(np.float32))
+    p = torch.from_numpy(rng.integers(0, 2, (9, ncols)).astype(np.int8))
+    sd = (2,) * len(pps)
+    site = gq.SlicedJacobian(o, p, sd, gq.SiteOrdering(pps))
+    slc = gq.SlicedJacobian(o, p, sd, gq.SliceOrdering())
+    S_site = gq.QGT(site, gq.ParameterSpace()).to_dense()
+    S_slice = gq.QGT(slc, gq.ParameterSpace()).to_dense()
+    idx = gq._site_from_slice_order(site)
+    assert torch.allclose(S_slice.index_select(0, idx).index_select(1, idx), S_site, rtol=1e-12, atol=1e-14)
+    assert gq._site_from_slice_order(slc) is None

@@ -119,6 +119,24 @@ def sliced_centring(jac: SlicedJacobian):
     return (o64 * mean.gather(0, pl)).sum(dim=1), (mean * mean).sum()
 
 
+def _site_from_slice_order(jac):
+    """For a site-ordered sliced Jacobian (jacobian.py:36-46): the slice-order index (k * ncols + c) of
+    every site-order column of the expanded Jacobian ([site 0: slice 0 columns, slice 1 columns, ...]
+    [site 1: ...]); None for another ordering or when the parameter counts do not cover the columns."""
+    if not isinstance(jac, SlicedJacobian) or not isinstance(jac.ordering, SiteOrdering):
+        return None
+    ncols = jac.o.shape[1]
+    pps = jac.ordering.params_per_site
+    if sum(pps) != ncols or len(jac.sliced_dims) != len(pps):
+        return None
+    idx, off = [], 0
+    for site, n_s in enumerate(pps):
+        for k in range(jac.sliced_dims[site]):
+            idx.extend(k * ncols + off + j for j in range(n_s))
+        off += n_s
+    return torch.tensor(idx, dtype=torch.long)
+
+
 def _kernel_gram(jac) -> bool:
     return (isinstance(jac, SlicedJacobian) and jac.o.device.type == "cuda" and jac.o.dtype == torch.float32
             and jac.p.dtype == torch.int8)
@@ -163,8 +181,11 @@ class QGT:
         """qgt.py:173-223."""
         if isinstance(self.space, SampleSpace):
             return _sample_space_dense(self.jac, self.n_blocks)
-        if (_kernel_gram(self.jac) and isinstance(self.jac.ordering, SliceOrdering) and self.jac.phys_dim == 2):
-            # O_exp^T O_exp from the sliced rows (vmc_sliced_gram_params), less the centring term
+        perm = _site_from_slice_order(self.jac)
+        if _kernel_gram(self.jac) and self.jac.phys_dim == 2 and all(k == 2 for k in self.jac.sliced_dims) and \
+                (isinstance(self.jac.ordering, SliceOrdering) or perm is not None):
+            # O_exp^T O_exp from the sliced rows (vmc_sliced_gram_params, slice order), less the centring
+            # term; a site-ordered Jacobian takes the same matrix with rows and columns permuted
             from .linalg import sliced_gram_params
 
             n = self.jac.o.shape[0]
@@ -175,6 +196,9 @@ class QGT:
             mean.scatter_add_(0, self.jac.p.long(), o64)
             m = (mean / n).reshape(-1)
             S -= m[:, None] * m[None, :]
+            if not isinstance(self.jac.ordering, SliceOrdering):
+                idx = perm.to(S.device)
+                S = S.index_select(0, idx).index_select(1, idx)
             return S
         O = _dense_O(self.jac)
         m = O.mean(dim=0)
