@@ -5,7 +5,9 @@
  * types cross this boundary.  Device pointers are CUDA device addresses;
  * `stream` is a cudaStream_t passed as void*.  Every compute entry point is
  * stream-ordered and allocates nothing: the caller owns all buffers and
- * passes a workspace sized by vmc_workspace_size().
+ * passes a workspace sized by vmc_workspace_size().  A call over zero chains
+ * (n == 0) returns VMC_OK and reads or writes none of its buffers, which may
+ * then be null (vmc_peps_vjp still zeroes out_grad: a sum over no samples).
  *
  * The entry points replace, for a batch of chains, the reference's PEPS
  * kernels (fliingelephant/VMC, Python/JAX):

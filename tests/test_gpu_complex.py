@@ -86,3 +86,32 @@ def test_real_time_rk4_on_the_gpu(cuda_device):
     assert drv.step_count == 2 and abs(drv.t - 0.02) < 1e-12
     assert drv._tensors[0][0].dtype == torch.complex64
     assert np.isfinite(drv.energy["mean"].real) and np.isfinite(drv.energy["variance"])
+
+
+def test_complex_density_matrix_matches_oracle(cuda_device):
+    """DensityMatrix on complex64 tensors (strategy.py:153-176), chi <= D so every kept eigenvector of
+    rho = theta^H theta has a nonzero eigenvalue: one transition + estimate against the complex128 oracle."""
+    from tests.helpers import oracle_sweep
+
+    shape, D, chi, n = (4, 4), 3, 3, 16
+    H = hamiltonian("tfim", shape)
+    T = complex_tensors(shape, D, seed=7)
+    rng = np.random.default_rng(7)
+    cfg = rng.integers(0, 2, (n, 16)).astype(np.int32)
+    u = rng.random((n, 16))
+    eng = PEPSEngine(shape, D, chi, 2, "DensityMatrix", operator=H, device=cuda_device, dtype="complex64")
+    tens = torch.from_numpy(pack_tensors(T)).to(cuda_device)
+    c = torch.from_numpy(cfg.copy()).to(cuda_device)
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, torch.from_numpy(u).to(cuda_device), cache)
+    torch.cuda.synchronize()
+    eng.raise_on_status()
+    c2, ctx, le = oracle_sweep(T, shape, D, "DensityMatrix", chi, H, cfg, u)
+    same = np.all(res.configs.cpu().numpy() == c2, axis=1)
+    assert np.all(same | (res.margin.cpu().numpy() < 1e-4))
+    amp = np.exp(res.logamp.cpu().numpy() + 1j * res.sign.cpu().numpy())
+    assert np.max(np.abs(amp[same] / ctx.amp[same] - 1)) < 1e-4
+    o, o_ref = res.O.cpu().numpy()[same], le.local_log_derivatives[same]
+    assert np.max(np.linalg.norm(o - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1)) < 5e-5
+    e, e_ref = res.E.cpu().numpy()[same], le.local_estimate[same]
+    assert np.max(np.abs(e - e_ref) / np.maximum(1.0, np.abs(e_ref))) < 5e-5

@@ -609,8 +609,9 @@ static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float
                          const double* uniforms, const int32_t* deltas, int n, void* cache, int full_gradient,
                          float* out_O, int8_t* out_p, double* out_E, double* logamp, double* sign, float* margin,
                          float* gap, void* ws, size_t ws_bytes, int32_t* status) {
-  if (!pl || !tensors || !configs || n < 0 || !ws || !status) return VMC_ERR_INVALID;
-  if (n == 0) return VMC_OK;
+  if (!pl || n < 0) return VMC_ERR_INVALID;
+  if (n == 0) return VMC_OK;  // no chain: no buffer is read or written
+  if (!tensors || !configs || !ws || !status) return VMC_ERR_INVALID;
   if (ws_bytes < vmc_workspace_size(pl, n)) return VMC_ERR_WORKSPACE;
   return run_job(pl, stream,
                  chain_job(pl, mode, tensors, nullptr, configs, uniforms, deltas, n, cache, full_gradient, out_O,
@@ -621,7 +622,7 @@ static vmc_status launch(const vmc_plan* pl, void* stream, int mode, const float
 vmc_status vmc_peps_init_cache(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* configs,
                                int n_chains, void* cache, void* workspace, size_t workspace_bytes,
                                int32_t* status_dev) {
-  if (!cache) return VMC_ERR_INVALID;
+  if (!cache && n_chains > 0) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_INIT, tensors, const_cast<int32_t*>(configs), nullptr, nullptr, n_chains, cache, 0,
                 nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, workspace, workspace_bytes,
                 status_dev);
@@ -632,8 +633,9 @@ vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors
                           int full_gradient, float* out_O, int8_t* out_p, double* out_E, double* out_logamp,
                           double* out_sign, float* out_margin, float* out_gap, void* workspace,
                           size_t workspace_bytes, int32_t* status_dev) {
-  if (!pl || !uniforms || !cache_inout || !out_E || !out_logamp || !out_sign) return VMC_ERR_INVALID;
-  if (needs_deltas(pl->hp) && !deltas) return VMC_ERR_INVALID;
+  if (!pl || (n_chains > 0 && (!uniforms || !cache_inout || !out_E || !out_logamp || !out_sign)))
+    return VMC_ERR_INVALID;
+  if (n_chains > 0 && needs_deltas(pl->hp) && !deltas) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_SWEEP, tensors, configs_inout, uniforms, deltas, n_chains, cache_inout,
                 full_gradient, out_O, out_p, out_E, out_logamp, out_sign, out_margin, out_gap, workspace,
                 workspace_bytes, status_dev);
@@ -642,7 +644,7 @@ vmc_status vmc_peps_sweep(const vmc_plan* pl, void* stream, const float* tensors
 vmc_status vmc_peps_vjp(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples, int n,
                         const double* weights, double* out_grad, void* workspace, size_t workspace_bytes,
                         int32_t* status_dev) {
-  if (!pl || !tensors || !samples || n < 0 || !weights || !out_grad || !workspace || !status_dev)
+  if (!pl || n < 0 || !out_grad || (n > 0 && (!tensors || !samples || !weights || !workspace || !status_dev)))
     return VMC_ERR_INVALID;
   if (pl->hp.gi) return VMC_ERR_UNSUPPORTED;
   const size_t grad_bytes = (size_t)pl->hp.np_sliced * pl->hp.d * pl->hp.es * sizeof(double);
@@ -671,11 +673,11 @@ vmc_status vmc_peps_sweep_recompute(const vmc_plan* pl, void* stream, const floa
                                     float* out_O, int8_t* out_p, double* out_E, double* out_logamp,
                                     double* out_sign, float* out_margin, float* out_gap, void* workspace,
                                     size_t workspace_bytes, int32_t* status_dev) {
-  if (!pl || !tensors || !configs_inout || !uniforms || !out_E || !out_logamp || !out_sign || n_chains < 0 ||
-      !workspace || !status_dev)
+  if (!pl || n_chains < 0) return VMC_ERR_INVALID;
+  if (n_chains == 0) return VMC_OK;
+  if (!tensors || !configs_inout || !uniforms || !out_E || !out_logamp || !out_sign || !workspace || !status_dev)
     return VMC_ERR_INVALID;
   if (needs_deltas(pl->hp) && !deltas) return VMC_ERR_INVALID;
-  if (n_chains == 0) return VMC_OK;
   if (workspace_bytes < vmc_sweep_recompute_workspace_size(pl, n_chains)) return VMC_ERR_WORKSPACE;
   const int grid = n_slots(pl, n_chains);
   float* wsf = static_cast<float*>(workspace);
@@ -721,7 +723,8 @@ static vmc_status noalloc_scratch(void** out) {
 vmc_status vmc_peps_amp_grad_noalloc(const vmc_plan* pl, void* stream, const float* tensors,
                                      const int32_t* samples, int n, int full_gradient, float* out_O,
                                      double* out_logamp, double* out_sign, float* out_gap, int32_t* status_dev) {
-  if (!pl || !tensors || !samples || n < 0 || !out_logamp || !out_sign || !status_dev) return VMC_ERR_INVALID;
+  if (!pl || n < 0 || (n > 0 && (!tensors || !samples || !out_logamp || !out_sign || !status_dev)))
+    return VMC_ERR_INVALID;
   const size_t perm_bytes = (size_t)pl->hp.perm_floats * 4, slot_bytes = (size_t)pl->hp.slot_floats * 4;
   if (perm_bytes + slot_bytes > VMC_NOALLOC_SCRATCH_BYTES) return VMC_ERR_SCRATCH;
   if (n == 0) return VMC_OK;
@@ -739,7 +742,7 @@ vmc_status vmc_peps_amp_grad_noalloc(const vmc_plan* pl, void* stream, const flo
 vmc_status vmc_peps_amp_grad(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples, int n,
                              int full_gradient, float* out_O, double* out_logamp, double* out_sign, float* out_gap,
                              void* workspace, size_t workspace_bytes, int32_t* status_dev) {
-  if (!pl || !out_logamp || !out_sign) return VMC_ERR_INVALID;
+  if (!pl || (n > 0 && (!out_logamp || !out_sign))) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_AMPGRAD, tensors, const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr,
                 full_gradient, out_O, nullptr, nullptr, out_logamp, out_sign, nullptr, out_gap, workspace,
                 workspace_bytes, status_dev);
@@ -748,7 +751,7 @@ vmc_status vmc_peps_amp_grad(const vmc_plan* pl, void* stream, const float* tens
 vmc_status vmc_peps_local_energy(const vmc_plan* pl, void* stream, const float* tensors, const int32_t* samples,
                                  int n, const double* logamp, const double* sign, double* out_E, void* workspace,
                                  size_t workspace_bytes, int32_t* status_dev) {
-  if (!pl || !logamp || !sign || !out_E) return VMC_ERR_INVALID;
+  if (!pl || (n > 0 && (!logamp || !sign || !out_E))) return VMC_ERR_INVALID;
   return launch(pl, stream, MODE_ENERGY, tensors, const_cast<int32_t*>(samples), nullptr, nullptr, n, nullptr, 0,
                 nullptr, nullptr, out_E, const_cast<double*>(logamp), const_cast<double*>(sign), nullptr, nullptr,
                 workspace, workspace_bytes, status_dev);
