@@ -233,13 +233,23 @@ __device__ inline T cta_top_eigenvalues(const T* d, const T* e, T* e2, int n, in
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int i = tid; i < n - 1; i += nt) e2[i] = e[i] * e[i];
   __syncthreads();
+  // Gershgorin interval and the largest e^2: every warp reduces over all rows (strided over its lanes,
+  // then shuffles; min and max are exact, so each thread ends with the same values without a barrier)
   T lo = Tol<T>::big, hi = -Tol<T>::big, e2max = T(0.);
-  for (int i = 0; i < n; ++i) {
+  for (int i = tid & 31; i < n; i += (nt < 32 ? nt : 32)) {
     const T r = (i > 0 ? vabs(e[i - 1]) : T(0.)) + (i < n - 1 ? vabs(e[i]) : T(0.));
     lo = vmin(lo, d[i] - r);
     hi = vmax(hi, d[i] + r);
     if (i < n - 1) e2max = vmax(e2max, e2[i]);
   }
+#ifndef VMC_HOST_EMULATION
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = vmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = vmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    e2max = vmax(e2max, __shfl_xor_sync(0xffffffffu, e2max, o));
+  }
+#endif
   const T tnorm = vmax(vabs(lo), vabs(hi));
   const T pivmin = T(1e-30) * vmax(T(1.), e2max);
   const T span = hi - lo;
@@ -669,12 +679,21 @@ __device__ inline double top_eigenvalues(const EigScratchT<double>& w, int n, in
   }
   __syncthreads();
   cta_top_eigenvalues(d32, e32, e2_32, n, kk, lam32);
+  // FP64 Gershgorin interval, warp-strided as in cta_top_eigenvalues (FP64 operations issue at a
+  // fraction of the FP32 rate, so no thread walks all n rows)
   double lo = 1.7e308, hi = -1.7e308;
-  for (int i = 0; i < n; ++i) {
+  for (int i = tid & 31; i < n; i += (nt < 32 ? nt : 32)) {
     const double r = (i > 0 ? fabs(w.e[i - 1]) : 0.0) + (i < n - 1 ? fabs(w.e[i]) : 0.0);
     lo = fmin(lo, w.d[i] - r);
     hi = fmax(hi, w.d[i] + r);
   }
+#ifndef VMC_HOST_EMULATION
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+#endif
   const double tnorm = fmax(fabs(lo), fabs(hi));
   // Near a root the evaluated p_n / p_n' carries rounding noise well above
   // 1e-13 |T|, so Newton stops at 1e-11 |T|: two inverse-iteration steps then
