@@ -8,6 +8,9 @@
  * passes a workspace sized by vmc_workspace_size().  A call over zero chains
  * (n == 0) returns VMC_OK and reads or writes none of its buffers, which may
  * then be null (vmc_peps_vjp still zeroes out_grad: a sum over no samples).
+ * Configuration values index the site tensors on the device unchecked: they
+ * must lie in [0, d) (gauge links of a GI plan in [0, N)); the Python layer
+ * (vmc_gb300.engine) refuses others before it launches.
  *
  * The entry points replace, for a batch of chains, the reference's PEPS
  * kernels (fliingelephant/VMC, Python/JAX):
@@ -226,8 +229,9 @@ vmc_status vmc_peps_init_cache(const vmc_plan* plan, void* stream, const float* 
  *   configs_inout[n_chains][n_sites] int32: updated in place.
  *   uniforms[n_chains][n_sites] float64 in [0,1): the reference's per-site
  *     jax.random.uniform(accept_key) draws (kernels.py:189-190).
- *   deltas[n_chains][n_sites] int32 in [1,d) or NULL when d <= 2: the flip
- *     offsets of kernels.py:170-175.
+ *   deltas[n_chains][n_sites] int32 or NULL when d <= 2: the flip offsets of
+ *     kernels.py:170-175, new = (s + delta) mod d with Python's non-negative
+ *     modulo, so any integer offset is valid (the reference draws [1, d)).
  *   cache_inout: the bottom-environment cache (read by the transition,
  *     rewritten by the estimate).
  * Outputs (any may be NULL except out_E):

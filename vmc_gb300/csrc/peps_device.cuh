@@ -760,7 +760,7 @@ __device__ __noinline__ void metropolis_row(const DevPlan& P, const Slot& S, Sha
     const int cur = spins[c];
     int flip = cur;
     if (P.d == 2) flip = 1 - cur;
-    else if (P.d > 2) flip = (cur + deltas[row * C + c]) % P.d;
+    else if (P.d > 2) flip = ((cur + deltas[row * C + c]) % P.d + P.d) % P.d;  // Python's modulo: any offset
     lenv_step1(Lc, T, Y1, ta, Lb, ba, U, tb);
     lenv_step23(Y1, perm_of(P, perm, s, P_LENV, cur), B, Y2, Lp0, ba, tb, Lb, U, Rb, V, bb);
     const int n_env = tb * Rb * bb;

@@ -167,11 +167,27 @@ class PEPSEngine:
         if tensors.numel() != self.n_params_full:
             raise ValueError(f"expected {self.n_params_full} packed parameters, got {tensors.numel()}")
 
+    # configuration values lie in [0, state_limit): spins below phys_dim (gauge links below N on a GI plan)
+    @property
+    def state_limit(self) -> int:
+        return self.phys_dim
+
     def _configs(self, configs):
         c = configs.reshape(-1, self.n_state)
         if c.dtype != torch.int32 or c.device != self.device or not c.is_contiguous():
             raise ValueError("configs must be a contiguous int32 (n, n_state) tensor on the engine device")
+        self._check_range(c)
         return c
+
+    def _check_range(self, c):
+        """The kernels index the site tensors with the configuration values unchecked, so a value outside
+        [0, state_limit) is refused here, before any launch: one min/max reduction and a host read.  Skipped
+        inside a CUDA-graph capture, whose configurations are the engine's own sweep outputs."""
+        if c.numel() == 0 or (c.device.type == "cuda" and torch.cuda.is_current_stream_capturing()):
+            return
+        lo, hi = torch.stack([c.min(), c.max()]).tolist()
+        if lo < 0 or hi >= self.state_limit:
+            raise ValueError(f"configuration values must lie in [0, {self.state_limit}); got [{lo}, {hi}]")
 
     def status(self, reset=True) -> int:
         v = int(self._status.item())

@@ -114,6 +114,10 @@ class GIEngine(PEPSEngine):
         if operator is not None:
             self.set_operator(operator)
 
+    @property
+    def state_limit(self) -> int:
+        return self.gi_N  # every entry of a sample is a link value (matter entries are 0)
+
     def _make_plan(self, lib, shape, dt, sid, n_sweeps, options, plan):
         return lib.vmc_gi_plan(ct.byref(shape), self.gi_N, self.bond_dim, self.chi, dt, sid, n_sweeps,
                                ct.byref(options) if options is not None else None, ct.byref(plan))
