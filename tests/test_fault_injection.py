@@ -115,3 +115,21 @@ def test_out_of_range_configurations_are_refused_on_the_gpu(cuda_device):
     shape, D, T, cfg, u = _case("float32")
     eng = PEPSEngine(shape, D, 4, 2, "ZipUp", operator=hamiltonian("heisenberg", shape), device=cuda_device)
     _check_refused(eng, torch.from_numpy(pack_tensors(T)).to(cuda_device), cfg, u, cuda_device)
+
+
+def test_public_api_refuses_out_of_range_configurations(emu_lib):
+    """Through the reference-facing calls: peps_apply (the torch.library operator) and init_cache of
+    build_mc_kernels."""
+    from vmc_gb300 import PEPS, ZipUp
+    from vmc_gb300.compat import peps_apply
+    from vmc_gb300.kernels import build_mc_kernels
+
+    shape, D, T, cfg, _ = _case("float32")
+    model = PEPS(shape=shape, bond_dim=D, contraction_strategy=ZipUp(4), device="cpu", lib=emu_lib, tensors=T)
+    bad = torch.from_numpy(cfg.copy())
+    bad[0, 0] = 7
+    with pytest.raises(ValueError, match="must lie in"):
+        peps_apply(model.packed(), bad, shape, None, model=model)
+    init_cache, _, _ = build_mc_kernels(model, hamiltonian("tfim", shape))
+    with pytest.raises(ValueError, match="must lie in"):
+        init_cache(model.tensors, bad)
