@@ -409,8 +409,8 @@ def time_sweeps(eng, tens, cfg0, uni, args, barrier, clock_index):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per sample of the fused kernel, from one ncu
 # capture of one sweep launch of 608 chains (one wave) of the 8x8 D4 chi16 workload per precision; every
-# chain reuses its CTA's slot, so a launch's traffic scales with its chains.  The captures are summarised
-# in profiles/peps_kernel_mixed_heis8x8_D4_chi16.md (both tiers, from `python -m vmc_gb300.profile_sweep`).
+# chain reuses its CTA's slot, so a launch's traffic scales with its chains.  The captured launches come
+# from `python -m vmc_gb300.profile_sweep --precision {fp32,mixed} --chains 608`.
 NCU_DRAM_BYTES_PER_SAMPLE = {("heis8x8_D4_chi16", "fp32"): (3.451871e9 + 7.283181e9) / 608,
                              ("heis8x8_D4_chi16", "mixed"): (3.722690e9 + 8.795817e9) / 608}
 

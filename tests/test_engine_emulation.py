@@ -67,7 +67,7 @@ def test_sweep_matches_oracle(emu_lib, shape, D, chi, strategy, model, full):
 
 
 def test_two_sweeps_reuse_the_bottom_cache(emu_lib):
-    """Cache turnover (REFACTOR.md cache semantics): the estimate's bottom envs feed the next transition."""
+    """Cache turnover (REFACTOR.md:39-52): the estimate's bottom envs feed the next transition."""
     shape, D, chi = (4, 4), 3, 6
     H = hamiltonian("heisenberg", shape)
     T, cfg, u = make_case(shape, D, 5, seed=11)
