@@ -44,3 +44,13 @@ def test_reference_arm_gi_workload_times_the_gi_oracle():
     assert d["impl"] == "reference" and "unavailable" not in d and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"] == d["e2e"]["value"]
     assert d["config"]["workload"] == "gi9x9"
+
+
+def test_reference_arm_other_ranks_exit_without_work():
+    """Under torchrun with N > 1 only rank 0 times the reference and prints; the others exit 0 at once."""
+    env = dict(os.environ, PYTHONPATH=str(ROOT), RANK="1", LOCAL_RANK="1", WORLD_SIZE="2")
+    res = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload",
+                          "tfim4x4_D2_chi4", "--steps", "1", "--warmup", "0"], cwd=ROOT, capture_output=True,
+                         text=True, timeout=120, env=env)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert not [l for l in res.stdout.splitlines() if l.startswith("{")]
