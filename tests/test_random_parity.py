@@ -1,0 +1,99 @@
+"""Randomised parity in the host emulation of the kernels: lattices up to 5x5, D in {2, 3}, d in {2, 3},
+every strategy, real and complex64 tensors, both precision tiers, sliced and full gradients, and random
+Hermitian operators (one-site, horizontal and vertical two-site terms and a diagonal term) against one
+transition + estimate of the FP64 oracle, from fixed seeds.  Plans beyond the engine's largest cut
+(NoTruncation bonds grow as D^rows) must be refused with VMC_ERR_UNSUPPORTED."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from tests.helpers import complex_tensors, fp32, make_case, oracle_sweep
+from vmc_gb300._abi import VMC_ERR_UNSUPPORTED, VmcError
+from vmc_gb300.engine import PEPSEngine
+from vmc_gb300.lowering import pack_tensors
+from vmc_gb300.operators import (DiagonalTerm, HorizontalTwoSiteTerm, LocalHamiltonian, OneSiteTerm,
+                                 VerticalTwoSiteTerm)
+
+
+def _hermitian(rng, n, cplx):
+    m = rng.standard_normal((n, n)) + (1j * rng.standard_normal((n, n)) if cplx else 0)
+    return m + m.conj().T
+
+
+def _operator(rng, shape, d, cplx):
+    R, C = shape
+    ops = []
+    for r in range(R):
+        for c in range(C):
+            if rng.random() < 0.7:
+                ops.append(OneSiteTerm(r, c, _hermitian(rng, d, cplx)))
+            if c < C - 1 and rng.random() < 0.7:
+                ops.append(HorizontalTwoSiteTerm(r, c, _hermitian(rng, d * d, cplx)))
+            if r < R - 1 and rng.random() < 0.7:
+                ops.append(VerticalTwoSiteTerm(r, c, _hermitian(rng, d * d, cplx)))
+    if R * C >= 2:
+        a = (int(rng.integers(R)), int(rng.integers(C)))
+        b = a
+        while b == a:
+            b = (int(rng.integers(R)), int(rng.integers(C)))
+        ops.append(DiagonalTerm((a, b), rng.standard_normal(d * d)))
+    return LocalHamiltonian(shape, tuple(ops))
+
+
+def _draw(seed):
+    rng = np.random.default_rng(seed)
+    shape = (int(rng.integers(1, 6)), int(rng.integers(1, 6)))
+    D, d = int(rng.integers(2, 4)), int(rng.choice([2, 2, 3]))
+    strategy = str(rng.choice(["ZipUp", "NoTruncation", "Variational", "DensityMatrix"]))
+    chi = 64 if strategy == "NoTruncation" else int(rng.integers(2, 7))
+    if strategy == "DensityMatrix":
+        chi = min(chi, D)  # every kept eigenvector has a nonzero eigenvalue
+    cplx = bool(rng.random() < 0.3)
+    mixed = (not cplx) and strategy != "Variational" and rng.random() < 0.4
+    return rng, shape, D, d, strategy, chi, cplx, "mixed" if mixed else "fp32", bool(rng.random() < 0.3)
+
+
+@pytest.mark.parametrize("seed", range(96))
+def test_random_case_matches_oracle(emu_lib, seed):
+    rng, shape, D, d, strategy, chi, cplx, precision, full = _draw(1000 + seed)
+    n, n_sites = 4, shape[0] * shape[1]
+    try:
+        eng = PEPSEngine(shape, D, chi, d, strategy, operator=None, device="cpu", lib=emu_lib,
+                         dtype="complex64" if cplx else "float32", options={"precision": precision})
+    except VmcError as e:
+        assert strategy == "NoTruncation" and e.status == VMC_ERR_UNSUPPORTED and D ** (shape[0] - 1) * D > 64
+        return
+    if cplx:
+        T = complex_tensors(shape, D, seed=seed, phys_dim=d)
+        cfg = rng.integers(0, d, (n, n_sites)).astype(np.int32)
+        u = rng.random((n, n_sites))
+    else:
+        T, cfg, u = make_case(shape, D, n, seed=seed, phys_dim=d)
+        T = fp32(T)
+    H = _operator(rng, shape, d, cplx)
+    eng.set_operator(H)
+    deltas = rng.integers(1, d, size=cfg.shape).astype(np.int32) if d > 2 else None
+    tens = torch.from_numpy(pack_tensors(T))
+    c = torch.from_numpy(cfg.copy())
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, torch.from_numpy(u), cache, deltas=None if deltas is None else torch.from_numpy(deltas),
+                    full_gradient=full)
+    assert eng.status() == 0
+    c2, ctx, le = oracle_sweep(T, shape, D, strategy, chi, H, cfg, u, full_gradient=full, deltas=deltas)
+    same = np.all(res.configs.numpy() == c2, axis=1)
+    assert np.all(same | (res.margin.numpy() < 1e-4))
+    if cplx:
+        amp = np.exp(res.logamp.numpy() + 1j * res.sign.numpy())
+    else:
+        amp = (res.sign * torch.exp(res.logamp)).numpy()
+    # FP32 rounding, and up to ~eps_fp32 / gap where a cut truncates with a small relative gap
+    tol = 2e-3 if float(res.gap.min()) < 1e-2 else 2e-4
+    assert np.max(np.abs(amp[same] / ctx.amp[same] - 1), initial=0) < tol
+    e, e_ref = res.E.numpy()[same], le.local_estimate[same]
+    assert np.max(np.abs(e - e_ref) / np.maximum(1.0, np.abs(e_ref)), initial=0) < tol
+    o, o_ref = res.O.numpy()[same], le.local_log_derivatives[same]
+    assert np.max(np.linalg.norm(o - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), initial=0) < tol
+    if not full:
+        assert np.array_equal(res.p.numpy()[same], le.active_slice_indices[same])
