@@ -97,3 +97,64 @@ def test_random_case_matches_oracle(emu_lib, seed):
     assert np.max(np.linalg.norm(o - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), initial=0) < tol
     if not full:
         assert np.array_equal(res.p.numpy()[same], le.active_slice_indices[same])
+
+
+def _draw_gi(seed):
+    rng = np.random.default_rng(seed)
+    shape = (int(rng.integers(2, 6)), int(rng.integers(2, 6)))
+    N = int(rng.choice([2, 2, 3]))
+    dmax = int(rng.integers(1, 3))
+    chi = None if rng.random() < 0.25 else int(rng.integers(2, 9))
+    return rng, shape, N, dmax, chi
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_gauge_invariant_case_matches_oracle(emu_lib, seed):
+    """Pure Z_N gauge (N = 2, 3), random lattices, degeneracies, chi and couplings (electric g, plaquette h)
+    against the GI oracle: one plaquette sweep, amplitudes, energies, O_k and slice indices."""
+    from oracle import gi as ogi
+    from oracle import peps as op
+    from vmc_gb300 import NoTruncation, ZipUp
+    from vmc_gb300.gi import GILocalHamiltonian, GIPEPS, GIPEPSConfig, build_electric_terms
+    from vmc_gb300.operators import PlaquetteTerm
+
+    rng, shape, N, dmax, chi = _draw_gi(2000 + seed)
+    (R, C), n = shape, 4
+    ocfg = ogi.GIConfig(shape, N, dmax)
+    T = [[t.astype(np.float32).astype(np.float64) for t in row] for row in ogi.init_tensors(ocfg, seed=seed)]
+    model = GIPEPS(config=GIPEPSConfig(shape=shape, N=N, phys_dim=1, Qx=0, degeneracy_per_charge=(dmax,) * N),
+                   contraction_strategy=NoTruncation() if chi is None else ZipUp(chi), device="cpu", tensors=T,
+                   lib=emu_lib)
+    g, h = float(rng.uniform(0.2, 1.5)), float(rng.uniform(-1.5, 1.5))
+    plaq = [(r, c) for r in range(R - 1) for c in range(C - 1)]
+    H = GILocalHamiltonian(shape=shape, terms=build_electric_terms(shape, g, N)
+                           + tuple(PlaquetteTerm(row=r, col=c, coeff=h) for r, c in plaq))
+    diag = g * (2.0 - 2.0 * np.cos(2.0 * np.pi * np.arange(N) / N))
+    OH = ogi.GIHamiltonian(shape, tuple(ogi.PlaquetteTerm(r, c, h) for r, c in plaq)
+                           + tuple(ogi.LinkDiagonalTerm("h", ((r, c),), diag) for r in range(R) for c in range(C - 1))
+                           + tuple(ogi.LinkDiagonalTerm("v", ((r, c),), diag) for r in range(R - 1) for c in range(C)))
+    samples = ogi.random_physical_configuration(ocfg, n, seed=seed + 7)
+    u = rng.random((n, len(plaq)))
+    deltas = rng.integers(1, N, (n, len(plaq))) if N > 2 else np.ones((n, len(plaq)), dtype=np.int64)
+    eng = model.engine(H)
+    tens = model.packed()
+    c = torch.from_numpy(samples.astype(np.int32))
+    cache = eng.init_cache(tens, c.clone())
+    res = eng.sweep(tens, c.clone(), torch.from_numpy(u), cache,
+                    deltas=torch.from_numpy(deltas.astype(np.int32)) if N > 2 else None)
+    assert eng.status() == 0
+    strat = op.NoTruncation() if chi is None else op.ZipUp(chi)
+    s2, amp_ref, tops, margin = ogi.transition(T, ocfg, samples, deltas.reshape(n, R - 1, C - 1),
+                                               u.reshape(n, R - 1, C - 1), ogi.init_cache(T, ocfg, samples, strat),
+                                               strat)
+    same = np.all(res.configs.numpy() == s2, axis=1)
+    assert np.all(same | (margin < 1e-4))
+    grads, e_ref, _ = ogi.estimate(T, ocfg, s2, amp_ref, OH, strat, tops)
+    o_ref, p_ref = ogi.local_log_derivatives(T, ocfg, s2, grads, amp_ref)
+    tol = 2e-3 if float(res.gap.min()) < 1e-2 else 2e-4
+    amp = (res.sign * torch.exp(res.logamp)).numpy()
+    assert np.max(np.abs(amp[same] / amp_ref[same] - 1), initial=0) < tol
+    assert np.max(np.abs(res.E.numpy()[same] - e_ref[same]) / np.maximum(1.0, np.abs(e_ref[same])), initial=0) < tol
+    o_err = np.linalg.norm(res.O.numpy()[same] - o_ref[same], axis=1) / np.linalg.norm(o_ref[same], axis=1)
+    assert np.max(o_err, initial=0) < tol
+    assert np.array_equal(res.p.numpy()[same], p_ref[same])
