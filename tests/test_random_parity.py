@@ -158,3 +158,42 @@ def test_random_gauge_invariant_case_matches_oracle(emu_lib, seed):
     o_err = np.linalg.norm(res.O.numpy()[same] - o_ref[same], axis=1) / np.linalg.norm(o_ref[same], axis=1)
     assert np.max(o_err, initial=0) < tol
     assert np.array_equal(res.p.numpy()[same], p_ref[same])
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_sr_solve_matches_oracle(seed):
+    """The FP64 SR layer (QGT + DirectSolve, plain torch) on random sliced Jacobians: lattices, D, d in
+    {2, 3}, real or complex parameters, imaginary or real time, sample counts on both sides of the
+    parameter count, diagonal shifts 1e-4..1e-1, both spaces, against oracle/sr.py."""
+    from oracle import sr as osr
+    from tests.helpers import uniform_init_tensors
+    from tests.test_sr_and_distributed import _ComplexModel, _Model
+    from vmc_gb300 import qgt as gq
+    from vmc_gb300.preconditioners import SRPreconditioner
+    from oracle import peps as oracle
+
+    rng = np.random.default_rng(4000 + seed)
+    shape = (int(rng.integers(1, 4)), int(rng.integers(2, 4)))
+    D, d = int(rng.integers(2, 4)), int(rng.choice([2, 3]))
+    cplx = bool(rng.random() < 0.4)
+    n = int(rng.integers(4, 160))
+    param_space = bool(rng.random() < 0.5)
+    shift = float(10 ** rng.uniform(-4, -1))
+    gf = -1j if (cplx and rng.random() < 0.5) else -1.0
+    T = complex_tensors(shape, D, seed=seed, phys_dim=d) if cplx else uniform_init_tensors(shape, D, phys_dim=d,
+                                                                                             seed=seed)
+    om = oracle.PEPS(T, shape, D, phys_dim=d, strategy=oracle.NoTruncation())
+    cfg = rng.integers(0, d, size=(n, shape[0] * shape[1]))
+    amps, grads, p = oracle.value_and_grad(om, cfg)
+    o = grads / amps[:, None]
+    e = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+    x_ref, m_ref = osr.sr_apply(o, p, e, pps=oracle.params_per_site(om), sliced_dims=oracle.sliced_dims(om),
+                                n_samples=n, diag_shift=shift, grad_factor=gf, real_params=not cplx,
+                                space=osr.ParameterSpace() if param_space else osr.SampleSpace())
+    pre = SRPreconditioner(space=gq.ParameterSpace() if param_space else gq.SampleSpace(), diag_shift=shift)
+    m = (_ComplexModel if cplx else _Model)(shape, D, d, T)
+    upd, metrics = pre.apply(m, m.tensors, torch.zeros((n, shape[0] * shape[1])), torch.as_tensor(o),
+                             torch.as_tensor(p), torch.as_tensor(e), grad_factor=gf)
+    flat = torch.cat([u.reshape(-1) for row in upd for u in row]).to(torch.complex128).numpy()
+    assert np.linalg.norm(flat - x_ref) / np.linalg.norm(x_ref) < 1e-5  # FP32 updates
+    assert abs(float(metrics["residual_error"]) - m_ref["residual_error"]) < 1e-6 * max(1.0, m_ref["residual_error"])
