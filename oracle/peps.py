@@ -721,11 +721,19 @@ def value(model, samples):
 
 
 def value_and_grad(model, samples, *, full_gradient=False):
-    """compat.py:94-133 (full_gradient scatters the same hand-written adjoint)."""
+    """compat.py:94-133 (full_gradient scatters the same hand-written adjoint).  Samples pass through
+    spin_to_occupancy as in compat.py:119, which maps +-1 spins to 0/1 and, for d > 2, occupancy 2 to 1."""
     samples = np.atleast_2d(samples)
-    z = samples.shape[0]
+    return value_and_grad_occupancy(model, spin_to_occupancy(samples), full_gradient=full_gradient)
+
+
+def value_and_grad_occupancy(model, occupancies, *, full_gradient=False):
+    """The amplitudes and dpsi/dA of configurations given as occupancies 0..d-1, the convention of the
+    sampler kernels (kernels.py:54-88 index the site tensors with the configuration as given)."""
+    occupancies = np.atleast_2d(occupancies)
+    z = occupancies.shape[0]
     n_rows, n_cols = model.shape
-    spins = spin_to_occupancy(samples).reshape(z, n_rows, n_cols)
+    spins = np.asarray(occupancies, dtype=np.int64).reshape(z, n_rows, n_cols)
     amp, top_envs = forward_with_cache(model.tensors, spins, model.shape, model.strategy)
     env_grads = compute_all_gradients(model.tensors, spins, model.shape, model.strategy, top_envs)
     if full_gradient:
