@@ -8,8 +8,9 @@
 * ``_value`` / ``_grad`` / ``_value_and_grad`` (compat.py:67-133).
 * ``local_estimate`` (compat.py:136-194).
 
-Samples may be occupancies (0..d-1) or +-1 spins, like the reference's
-``spin_to_occupancy`` (src/vmc/utils/utils.py:55-57).
+For d = 2, samples may be 0/1 occupancies or +-1 spins, mapped by the reference's
+``spin_to_occupancy`` (src/vmc/utils/utils.py:55-57).  For d > 2 they are occupancies 0..d-1 taken as
+given, the sampler kernels' convention: the reference's (s + 1) // 2 would send occupancy 2 to 1.
 """
 from __future__ import annotations
 
