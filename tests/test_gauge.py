@@ -122,3 +122,38 @@ def test_qr_solve_with_gauge_removal_matches_the_dense_formulation(emu_lib, monk
     dv = (e - e.mean()) / n
     want = 2.0 * (Q @ (torch.linalg.pinv(oc, rtol=1e-12) @ dv))
     assert torch.linalg.norm(x - want) / torch.linalg.norm(want) < 1e-5
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_lattices_gauge_projection_and_null_directions(seed):
+    """Random lattices (1..4 x 1..4), D in {2, 3}, d in {2, 3}: U is orthonormal and removes every generator,
+    its rank is the numerical rank of the generators, and every bond generator annihilates the oracle's
+    exact log-derivatives."""
+    rng = np.random.default_rng(600 + seed)
+    shape = (int(rng.integers(1, 5)), int(rng.integers(1, 5)))
+    D, d = int(rng.integers(2, 4)), int(rng.choice([2, 3]))
+    R_, C_ = shape
+    T, cfg, _ = make_case(shape, D, 12, seed=seed, phys_dim=d)
+    T = fp32(T)
+    model = PEPS(shape=shape, bond_dim=D, phys_dim=d, contraction_strategy=NoTruncation(), device="cpu", tensors=T)
+    G = gauge_generators(model)
+    n_bonds = R_ * (C_ - 1) + (R_ - 1) * C_
+    assert G.shape[1] == n_bonds * D * D + 1
+    proj, info = compute_gauge_projection(GaugeConfig(), model, None, return_info=True)
+    U = proj.U
+    assert torch.allclose(U.T @ U, torch.eye(U.shape[1], dtype=U.dtype), atol=1e-12)
+    assert torch.linalg.norm(proj.project(G)) < 1e-10 * torch.linalg.norm(G)
+    # at most one per generator less one scalar dependency per plaquette; boundary tensors of rank < D
+    # (d < D at a corner) add exact dependencies X = u v^T with A u = 0 and v^T B = 0
+    assert info["rank"] <= n_bonds * D * D - (R_ - 1) * (C_ - 1) + 1
+    sv = np.linalg.svd(G.numpy(), compute_uv=False)
+    assert info["rank"] == int((sv > 1e-10 * sv[0]).sum())
+    om = oracle.PEPS(T, shape, D, phys_dim=d, strategy=oracle.NoTruncation())
+    amp, grads, _ = oracle.value_and_grad_occupancy(om, cfg, full_gradient=True)
+    O = grads / amp[:, None]
+    Gn = G.numpy()
+    if n_bonds:
+        Rr = np.random.default_rng(seed).standard_normal(Gn[:, :-1].shape)
+        Rr *= np.linalg.norm(Gn[:, :-1], axis=0) / np.linalg.norm(Rr, axis=0)
+        assert np.max(np.abs(O @ Gn[:, :-1])) < 1e-8 * np.median(np.abs(O @ Rr))
+    assert np.allclose(O @ Gn[:, -1], R_ * C_, rtol=1e-9)
