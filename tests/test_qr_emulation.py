@@ -117,3 +117,15 @@ def test_qr_solve_graded_spectrum(emu_lib, m, n, cplx):
     xp = np.linalg.pinv(oc, rcond=1e-12) @ dv
     assert np.linalg.norm(x.numpy() - xr) <= 1e-6 * np.linalg.norm(xr)
     assert np.linalg.norm(x.numpy() - xp) <= 1e-6 * np.linalg.norm(xp)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_shapes_and_scales_match_lapack(emu_lib, seed):
+    """Random m, n (min(m, n) <= 128, where xGEQP3 runs the unblocked xLAQP2), real or complex, column
+    scales over four decades and 1-3 right-hand sides."""
+    rng = np.random.default_rng(700 + seed)
+    m, n = int(rng.integers(1, 200)), int(rng.integers(1, 129))
+    cplx = bool(rng.random() < 0.5)
+    a = _rand(rng, (m, n), cplx) * 10.0 ** rng.uniform(-2, 2, n)
+    b = _rand(rng, (m, int(rng.integers(1, 4))), cplx)
+    _check(emu_lib, a, b)
