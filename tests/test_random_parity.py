@@ -233,3 +233,35 @@ def test_random_vjp_matches_oracle(emu_lib, seed):
     g = eng.vjp(torch.from_numpy(pack_tensors(T)), torch.from_numpy(cfg), torch.from_numpy(w)).numpy()
     assert eng.status() == 0
     assert np.linalg.norm(g - ref) / np.linalg.norm(ref) < 1e-4
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_truncating_mixed_tier_amplitudes(emu_lib, seed):
+    """The mixed tier on random actively truncating ZipUp / DensityMatrix cases (3..5 x 3..5, chi < D^2):
+    amplitudes at the FP64 level of the double-float chain (< 1e-10, against FP32's ~1e-6), O_k at the FP32
+    level of the environments."""
+    from tests.helpers import hamiltonian
+
+    rng = np.random.default_rng(9000 + seed)
+    shape = (int(rng.integers(3, 6)), int(rng.integers(3, 6)))
+    D = int(rng.integers(2, 4))
+    chi = int(rng.integers(2, D * D))
+    strategy = str(rng.choice(["ZipUp", "DensityMatrix"]))
+    if strategy == "DensityMatrix":
+        chi = min(chi, D)
+    T, cfg, u = make_case(shape, D, 4, seed=seed)
+    T = fp32(T)
+    H = hamiltonian(str(rng.choice(["heisenberg", "tfim"])), shape)
+    eng = PEPSEngine(shape, D, chi, 2, strategy, operator=H, device="cpu", lib=emu_lib,
+                     options={"precision": "mixed"})
+    tens = torch.from_numpy(pack_tensors(T))
+    c = torch.from_numpy(cfg.copy())
+    cache = eng.init_cache(tens, c)
+    res = eng.sweep(tens, c, torch.from_numpy(u), cache)
+    c2, ctx, le = oracle_sweep(T, shape, D, strategy, chi, H, cfg, u)
+    same = np.all(res.configs.numpy() == c2, axis=1)
+    assert np.all(same | (res.margin.numpy() < 1e-4))
+    amp = (res.sign * torch.exp(res.logamp)).numpy()
+    assert np.max(np.abs(amp[same] / ctx.amp[same] - 1), initial=0) < 1e-10
+    o, o_ref = res.O.numpy()[same], le.local_log_derivatives[same]
+    assert np.max(np.linalg.norm(o - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), initial=0) < 1e-5
