@@ -752,12 +752,17 @@ def value_and_grad_occupancy(model, occupancies, *, full_gradient=False):
 
 
 def local_estimate(model, samples, operator, amps):
-    """compat.py:136-194."""
-    samples = np.atleast_2d(samples)
+    """compat.py:136-194 (samples through spin_to_occupancy, as compat.py:162)."""
+    return local_estimate_occupancy(model, spin_to_occupancy(np.atleast_2d(samples)), operator, amps)
+
+
+def local_estimate_occupancy(model, occupancies, operator, amps):
+    """E_loc of configurations given as occupancies 0..d-1 (the sampler kernels' convention)."""
+    samples = np.atleast_2d(occupancies)
     z = samples.shape[0]
     shape = model.shape
     diagonal, one_site, horizontal, vertical, _ = bucket_terms(operator.terms, shape)
-    spins = spin_to_occupancy(samples).reshape(z, *shape)
+    spins = np.asarray(samples, dtype=np.int64).reshape(z, *shape)
     _, top_envs = forward_with_cache(model.tensors, spins, shape, model.strategy)
     _, energy, _ = compute_all_env_grads_and_energy(
         model.tensors, spins, np.asarray(amps), shape, model.strategy, top_envs,
