@@ -30,7 +30,9 @@ known-answer tests that do not depend on the reference's code:
 * MC energy / gradient against the exact full sum (tests/test_mc_energy_grad_evaluator.py:58-189);
 * slice-ordering reorder and slice-vs-site SR solve (tests/test_qgt.py:84-160);
 * solvers against dense solves (tests/test_qgt_solvers.py:15-46);
-* RK4 / Euler against expm (tests/test_integrators.py:25-69).
+* RK4 / Euler against expm (tests/test_integrators.py:25-69);
+* the first four again on random lattices, bond and physical dimensions (d = 2, 3), real and complex
+  tensors and random Hermitian operators.
 
 Truncated zip-up / variational amplitudes with ACTIVE truncation are pinned by
 no reference test (the reference only checks the exact regime); for those the
