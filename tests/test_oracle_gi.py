@@ -120,3 +120,25 @@ def test_plaquette_sweeps_sample_psi_squared():
                 counts[index[tuple(s)]] += 1
     freq = counts / counts.sum()
     assert np.abs(freq - target).max() < 0.02
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_gi_energies_equal_the_dense_hamiltonian(seed):
+    """Random lattices (2..3 x 2..4), N in {2, 3}, degeneracies 1-2 and couplings: the GI oracle's E_loc over
+    every gauge-invariant configuration equals (H psi)/psi of the dense Hamiltonian, and ZipUp in its exact
+    regime equals NoTruncation."""
+    rng = np.random.default_rng(600 + seed)
+    N = int(rng.choice([2, 3]))
+    shape = (int(rng.integers(2, 4)), int(rng.integers(2, 5 if N == 2 else 4)))
+    dmax = int(rng.integers(1, 3))
+    cfg = gi.GIConfig(shape, N, dmax)
+    T = gi.init_tensors(cfg, seed=seed)
+    H = gi.z2_pure_gauge_hamiltonian(shape, h=float(rng.uniform(-1.5, 1.5)), g=float(rng.uniform(0.2, 1.5)), N=N)
+    strat = op.NoTruncation()
+    e_exact, samples, psi, e_loc = gi.dense_hamiltonian_energy(T, cfg, H, strat)
+    top = _forward_top_envs(T, cfg, samples, strat)
+    _, energy, _ = gi.estimate(T, cfg, samples, psi, H, strat, top)
+    mask = np.abs(psi) > 1e-8 * np.abs(psi).max()
+    assert np.allclose(energy[mask], e_loc[mask], rtol=1e-9, atol=1e-9)
+    b = gi.amplitude(T, cfg, samples, op.ZipUp(256))
+    assert np.allclose(b, psi, rtol=1e-9, atol=1e-12 * np.abs(psi).max())
