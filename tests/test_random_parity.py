@@ -265,3 +265,42 @@ def test_random_truncating_mixed_tier_amplitudes(emu_lib, seed):
     assert np.max(np.abs(amp[same] / ctx.amp[same] - 1), initial=0) < 1e-10
     o, o_ref = res.O.numpy()[same], le.local_log_derivatives[same]
     assert np.max(np.linalg.norm(o - o_ref, axis=1) / np.linalg.norm(o_ref, axis=1), initial=0) < 1e-5
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_sample_and_parameter_space_solves_agree(seed):
+    """Push-through identity O^H (O O^H + l)^-1 v = (O^H O + l)^-1 O^H v: the SampleSpace and ParameterSpace
+    DirectSolve updates are the same vector, in the oracle (preconditioners.py:117-152) and in the FP64 torch
+    SR layer, on random sliced Jacobians (both sides of the parameter count, real and complex)."""
+    from oracle import peps as oracle
+    from oracle import sr as osr
+    from tests.helpers import uniform_init_tensors
+    from tests.test_sr_and_distributed import _ComplexModel, _Model
+    from vmc_gb300 import qgt as gq
+    from vmc_gb300.preconditioners import SRPreconditioner
+
+    rng = np.random.default_rng(7000 + seed)
+    shape, D, d = (int(rng.integers(1, 3)), int(rng.integers(2, 4))), int(rng.integers(2, 4)), int(rng.choice([2, 3]))
+    cplx = bool(rng.random() < 0.5)
+    n = int(rng.integers(4, 200))
+    shift = float(10 ** rng.uniform(-3, -1))
+    T = complex_tensors(shape, D, seed=seed, phys_dim=d) if cplx else uniform_init_tensors(shape, D, phys_dim=d,
+                                                                                             seed=seed)
+    om = oracle.PEPS(T, shape, D, phys_dim=d, strategy=oracle.NoTruncation())
+    cfg = rng.integers(0, d, size=(n, shape[0] * shape[1]))
+    amps, grads, p = oracle.value_and_grad(om, cfg)
+    o = grads / amps[:, None]
+    e = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+    kw = dict(pps=oracle.params_per_site(om), sliced_dims=oracle.sliced_dims(om), n_samples=n, diag_shift=shift,
+              grad_factor=-1.0, real_params=not cplx)
+    xs, _ = osr.sr_apply(o, p, e, space=osr.SampleSpace(), **kw)
+    xp, _ = osr.sr_apply(o, p, e, space=osr.ParameterSpace(), **kw)
+    assert np.linalg.norm(xs - xp) <= 1e-8 * np.linalg.norm(xp)
+    m = (_ComplexModel if cplx else _Model)(shape, D, d, T)
+    outs = []
+    for space in (gq.SampleSpace(), gq.ParameterSpace()):
+        upd, _ = SRPreconditioner(space=space, diag_shift=shift).apply(
+            m, m.tensors, torch.zeros((n, shape[0] * shape[1])), torch.as_tensor(o), torch.as_tensor(p),
+            torch.as_tensor(e), grad_factor=-1.0)
+        outs.append(torch.cat([u.reshape(-1) for row in upd for u in row]).to(torch.complex128).numpy())
+    assert np.linalg.norm(outs[0] - outs[1]) <= 1e-6 * np.linalg.norm(outs[1])  # FP32 updates
